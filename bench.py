@@ -1,0 +1,390 @@
+#!/usr/bin/env python
+"""Benchmark of the FE-solve path on the seeded cantilever workloads.
+
+One step = one solve of (K_ff + sigma I) u = f to FP64 relative residual
+1e-9 on the 384x192x192 cantilever (c3, 43,022,595 DOF) by the
+mixed-precision form: FP32 GMG-PCG corrections (5 levels, V(2,2) damped
+Jacobi) inside FP64 iterative refinement, CUDA-graph replayed.  The line also
+carries the plain FP64 GMG-PCG solve of the same system, the live roofline of
+the dominant kernel (the FP32 operator) and the CPU baseline (the reference's
+CPUSolver.jl path restated, Float32 Jacobi-PCG on all host cores).
+
+  python bench.py [--gpus N --steps K --warmup W] [--impl reference] [--config c3|c2|c1]
+
+Inputs are resident in HBM for ``value``; ``e2e`` repeats the step through the
+C ABI with pinned host buffers (copies inside the timed region).  Inputs
+(factor 113 MB, f and u 344 MB each at c3) exceed the 129 MB L2, so no
+explicit flush is done between steps.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "solve s to FP64 rel.res 1e-9, mixed vs plain FP64 on 1 GB300; matvec HBM GB/s"
+FALLBACK_HBM_GBS = 6800.0
+JACOBI_ITERS_FILE = ROOT / "profiles" / "jacobi_iterations.json"
+TRAFFIC_FILE = ROOT / "profiles" / "op_traffic.json"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--config", default="c3", choices=["c1", "c2", "c3"])
+    ap.add_argument("--no-plain", action="store_true", help="skip the plain FP64 comparison solve")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    ap.add_argument("--cpu-seconds", type=float, default=20.0)
+    return ap.parse_args()
+
+
+# --------------------------------------------------------------------- env
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class Dist:
+    def __init__(self, backend):
+        self.ws, self.rank, self.local = dist_env()
+        self.pg = None
+        if self.ws > 1:
+            import torch.distributed as td
+            os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+            td.init_process_group(backend)
+            self.pg = td
+
+    def barrier(self):
+        if self.pg:
+            self.pg.barrier()
+
+    def max(self, v: float) -> float:
+        if not self.pg:
+            return v
+        import torch
+        dev = "cuda" if self.pg.get_backend() == "nccl" else "cpu"
+        t = torch.tensor([v], dtype=torch.float64, device=dev)
+        self.pg.all_reduce(t, op=self.pg.ReduceOp.MAX)
+        return float(t.item())
+
+    def close(self):
+        if self.pg:
+            self.pg.destroy_process_group()
+
+
+class Clocks:
+    """nvidia-smi samples during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        self.p = None
+
+    def start(self):
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                                       "-lms", "200", "-i", str(self.device)], stdout=self.f, stderr=subprocess.DEVNULL)
+        except FileNotFoundError:
+            self.p = None
+
+    def stop(self) -> dict:
+        if self.p is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.p.terminate()
+        self.p.wait()
+        self.f.flush()
+        rows = [l.split(", ") for l in Path(self.f.name).read_text().splitlines() if l.strip()]
+        os.unlink(self.f.name)
+        sm = [float(r[1]) for r in rows if len(r) >= 9 and r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if len(r) >= 9 and r[2].replace(".", "").isdigit()]
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            if len(r) < 9:
+                continue
+            for n, v in zip(names, r[5:9]):
+                if v.strip() == "Active":
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(rows)}
+
+
+# ---------------------------------------------------------------- workload
+def workload(name):
+    from v119_2025_12_19_hexatop_aws_gb300 import workloads as W
+    nx, ny, nz = W.SIZES[name]
+    return nx, ny, nz
+
+
+def make_inputs(name, ctx):
+    """Seeded cantilever inputs (host numpy).  The c2/c3 density is smoothed by
+    this library's GPU Helmholtz filter (input generation, outside any timed region)."""
+    from v119_2025_12_19_hexatop_aws_gb300 import _lib, workloads as W
+    from v119_2025_12_19_hexatop_aws_gb300.helmholtz import filter_density
+    nx, ny, nz = workload(name)
+    grid = _lib.make_grid(nx, ny, nz)
+    if name == "c1":
+        rho = W.c1_density(nx, ny, nz)
+    else:
+        def filt(g, R):
+            out, _ = filter_density(grid, np.ascontiguousarray(g), R, tol=1e-10, max_iter=20000, quirk=False, ctx=ctx)
+            return out
+        rho = W.smooth_density(nx, ny, nz, filt)
+    fac = W.EMIN + rho ** W.PENAL * (W.E0 - W.EMIN)
+    f = W.edge_load(nx, ny, nz)
+    return grid, rho, fac, f
+
+
+def solver_params(name, precision):
+    from v119_2025_12_19_hexatop_aws_gb300 import _lib, workloads as W
+    return _lib.default_params(precision=precision, precond="multigrid", tol=1e-9, max_iter=30000,
+                               mg_levels=W.MG_LEVELS.get(name, 0), pre_smooth=2, post_smooth=2)
+
+
+def peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return FALLBACK_HBM_GBS, "fallback"
+
+
+# ------------------------------------------------------------ CPU baseline
+def cpu_sample(name, fac, f, seconds, clamp_faces=1):
+    """CPUSolver.jl's Float32 Jacobi-PCG on all host cores, a bounded number of
+    iterations on the full grid; projected to a full solve with the iteration
+    count the reference's Jacobi-PCG needs for this system."""
+    from oracle import reference as ref
+    nx, ny, nz = workload(name)
+    g = ref.Grid(nx, ny, nz)
+    fixed = ref.fixed_mask(g, clamp_faces).astype(np.uint8)
+    dens = fac.astype(np.float32)  # E = 1: density argument = modulus factor
+    iters_needed = None
+    if JACOBI_ITERS_FILE.exists():
+        iters_needed = json.loads(JACOBI_ITERS_FILE.read_text()).get(name, {}).get("iterations")
+    _, rel, it, sec = ref.cpu_matrix_free_cg(g, 1.0, dens, f.astype(np.float32), fixed, nu=0.3,
+                                             min_stiffness_threshold=1e-3, max_iter=100000, tol=1e-9,
+                                             shift_factor=1e-10, max_seconds=seconds)
+    per_iter = sec / max(it, 1)
+    cores = ref.num_threads()
+    if iters_needed:
+        value = per_iter * iters_needed
+        sample = (f"{it} Float32 Jacobi-PCG iterations of CPUSolver.jl's matrix_free path on the full {nx}x{ny}x{nz} "
+                  f"grid ({sec:.1f} s, {per_iter:.3f} s/iteration) x {iters_needed} iterations that the reference's "
+                  f"Jacobi-PCG needs to reach 1e-9 on this system (FP64, counted once, {JACOBI_ITERS_FILE.name})")
+    else:
+        value = None
+        sample = f"{it} iterations, {per_iter:.3f} s/iteration; Jacobi iteration count to 1e-9 not recorded"
+    return {"value": value, "unit": "s", "cores": cores, "kind": "port", "sample": sample,
+            "s_per_iteration": per_iter}
+
+
+# -------------------------------------------------------------- our arm
+def run_ours(a):
+    import torch
+    from v119_2025_12_19_hexatop_aws_gb300 import _lib
+    from v119_2025_12_19_hexatop_aws_gb300 import build as libbuild
+    import ctypes as C
+
+    libbuild.build()
+    dist = Dist("nccl")
+    torch.cuda.set_device(dist.local)
+    ctx = _lib.Context(dist.local)
+    grid, rho, fac, f = make_inputs(a.config, ctx)
+    nx, ny, nz = grid.nx, grid.ny, grid.nz
+    ndof, nelem = 3 * (nx + 1) * (ny + 1) * (nz + 1), nx * ny * nz
+    dev = torch.device("cuda", dist.local)
+    fac_d = torch.from_numpy(fac).to(dev)
+    f_d = torch.from_numpy(f).to(dev)
+    u_d = torch.empty(ndof, dtype=torch.float64, device=dev)
+    bc = _lib.make_bc(1)
+    pm = solver_params(a.config, "mixed")
+    st = _lib.SolveStats()
+
+    def step(params, fac_p, f_p, u_p):
+        rc = ctx.lib.hexa_solve(ctx.h, C.byref(grid), C.byref(bc), fac_p, f_p, C.byref(params), None, u_p,
+                                C.byref(st))
+        ctx.check(rc, allow=(_lib.HEXA_OK,))
+        return st.as_dict()
+
+    for _ in range(a.warmup):
+        step(pm, fac_d.data_ptr(), f_d.data_ptr(), u_d.data_ptr())
+    torch.cuda.synchronize()
+    dist.barrier()
+    clocks = Clocks(dist.local)
+    clocks.start()
+    l0 = ctx.kernel_launches
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    ev0.record()
+    stats = []
+    for _ in range(a.steps):
+        stats.append(step(pm, fac_d.data_ptr(), f_d.data_ptr(), u_d.data_ptr()))
+    ev1.record()
+    torch.cuda.synchronize()
+    ck = clocks.stop()
+    dist.barrier()
+    launches = ctx.kernel_launches - l0
+    ms = ev0.elapsed_time(ev1) / a.steps
+    ms = dist.max(ms)
+    s_last = stats[-1]
+    comp_mixed = s_last["compliance"]
+
+    # plain FP64 GMG-PCG on the same system (second call timed: the first allocates)
+    plain = None
+    if not a.no_plain:
+        pp = solver_params(a.config, "fp64")
+        u64 = torch.empty_like(u_d)
+        step(pp, fac_d.data_ptr(), f_d.data_ptr(), u64.data_ptr())
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        sp = step(pp, fac_d.data_ptr(), f_d.data_ptr(), u64.data_ptr())
+        e1.record()
+        torch.cuda.synchronize()
+        plain_ms = e0.elapsed_time(e1)
+        du = torch.linalg.vector_norm(u_d - u64).item() / torch.linalg.vector_norm(u64).item()
+        plain = {"s": plain_ms / 1e3, "iterations": sp["iterations"], "true_relres": sp["true_relres"],
+                 "compliance": sp["compliance"], "mixed_over_plain": ms / plain_ms,
+                 "compliance_rel_diff_mixed": abs(comp_mixed - sp["compliance"]) / abs(sp["compliance"]),
+                 "u_rel_diff_mixed": du}
+        del u64
+
+    # e2e: the same step through the C ABI with pinned host buffers
+    fac_h = torch.from_numpy(fac).pin_memory()
+    f_h = torch.from_numpy(f).pin_memory()
+    u_h = torch.empty(ndof, dtype=torch.float64).pin_memory()
+    step(pm, fac_h.data_ptr(), f_h.data_ptr(), u_h.data_ptr())
+    ke = max(1, min(a.steps, 3))
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(ke):
+        step(pm, fac_h.data_ptr(), f_h.data_ptr(), u_h.data_ptr())
+    e1.record()
+    torch.cuda.synchronize()
+    e2e_ms = dist.max(e0.elapsed_time(e1) / ke)
+
+    # roofline: the FP32 operator, each mode timed alone with CUDA events on the library's stream
+    peak, peak_kind = peaks()
+    f32 = lambda t: t.to(torch.float32).contiguous()
+    facf, xf, bf = f32(fac_d), f32(u_d), f32(f_d)
+    yf = torch.empty_like(xf)
+    modes = {"apply": (0, 8 * ndof + 4 * nelem), "apply_dot": (1, 8 * ndof + 4 * nelem),
+             "residual": (2, 12 * ndof + 4 * nelem), "jacobi": (4, 12 * ndof + 4 * nelem)}
+    kern = {}
+    for name, (mode, nbytes) in modes.items():
+        t = C.c_double()
+        rc = ctx.lib.hexa_time_operator(ctx.h, C.byref(grid), C.byref(bc), 0.3, 2, mode, facf.data_ptr(),
+                                        xf.data_ptr(), bf.data_ptr(), yf.data_ptr(), 20, C.byref(t))
+        ctx.check(rc, allow=(_lib.HEXA_OK,))
+        kern[name] = {"ms": t.value, "bytes": nbytes, "gbs": nbytes / (t.value * 1e-3) / 1e9}
+    t64 = C.c_double()
+    ctx.check(ctx.lib.hexa_time_operator(ctx.h, C.byref(grid), C.byref(bc), 0.3, 0, 0, fac_d.data_ptr(),
+                                         u_d.data_ptr(), f_d.data_ptr(), torch.empty_like(u_d).data_ptr(), 5,
+                                         C.byref(t64)), allow=(_lib.HEXA_OK,))
+    kern["apply_fp64"] = {"ms": t64.value, "bytes": 16 * ndof + 8 * nelem,
+                          "gbs": (16 * ndof + 8 * nelem) / (t64.value * 1e-3) / 1e9}
+    dom = kern["jacobi"]
+    traffic = None
+    if TRAFFIC_FILE.exists():
+        traffic = json.loads(TRAFFIC_FILE.read_text()).get(a.config, {}).get("jacobi_fp32_bytes_per_launch")
+    roof = {"bound": "hbm", "achieved": round(dom["gbs"], 1), "peak": peak, "unit": "GB/s",
+            "frac": round(dom["gbs"] / peak, 4), "traffic": traffic, "kernel": "op_kernel<float, OP_JACOBI>",
+            "peak_source": peak_kind, "algorithmic_bytes_per_launch": dom["bytes"]}
+
+    cpu = None
+    if dist.rank == 0 and not a.no_cpu:
+        cpu = cpu_sample(a.config, fac, f, a.cpu_seconds)
+
+    dofit = ndof * s_last["iterations"] / (ms / 1e3)
+    out = {
+        "metric": METRIC, "value": round(ms / 1e3, 6), "unit": "s", "n_gpus": dist.ws, "steps": a.steps,
+        "warmup": a.warmup, "ms_per_step": round(ms, 3), "higher_is_better": False, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic (seeded cantilever, Helmholtz-smoothed density)",
+        "config": {"workload": f"{a.config} cantilever {nx}x{ny}x{nz} hex8, {ndof} DOF, SIMP p=3 Emin=1e-9, "
+                               f"mixed FP32 GMG-PCG ({s_last['mg_levels']} levels, V(2,2) Jacobi) in FP64 "
+                               f"refinement to 1e-9",
+                   "parallelism": f"replicas{dist.ws}", "l2": "inputs larger than L2 (no flush)"},
+        "e2e": {"value": round(e2e_ms / 1e3, 6), "unit": "s", "h2d_bytes_per_step": 8 * (nelem + ndof),
+                "d2h_bytes_per_step": 8 * ndof},
+        "roofline": roof,
+        "cpu_baseline": cpu,
+        "gpu_launches": int(launches),
+        "clocks": ck,
+        "solve": {"iterations": s_last["iterations"], "outer_iterations": s_last["outer_iterations"],
+                  "true_relres": s_last["true_relres"], "compliance": comp_mixed,
+                  "fine_applies": s_last["fine_applies"], "dof_iterations_per_s": dofit,
+                  "setup_ms": s_last["setup_ms"], "solve_ms": s_last["solve_ms"]},
+        "plain_fp64": plain,
+        "kernels": kern,
+    }
+    if dist.rank == 0:
+        print(json.dumps(out))
+    ctx.close()
+    dist.close()
+
+
+# -------------------------------------------------------- reference arm
+def run_reference(a):
+    """The reference's own CPU path for this solve (CPUSolver.jl restated, the
+    oracle port; the reference is Julia and cannot run here), timed on the
+    host cores on bounded samples of the same workload."""
+    ws, rank, local = dist_env()
+    if rank != 0:
+        return
+    from oracle import build as obuild
+    obuild.build()
+    from v119_2025_12_19_hexatop_aws_gb300 import _lib
+    from v119_2025_12_19_hexatop_aws_gb300 import build as libbuild
+    libbuild.build()
+    ctx = _lib.Context(local)
+    grid, rho, fac, f = make_inputs(a.config, ctx)
+    ctx.close()
+    per_step = max(2.0, a.cpu_seconds / 2)
+    vals, last = [], None
+    for i in range(a.warmup + a.steps):
+        r = cpu_sample(a.config, fac, f, per_step)
+        if i >= a.warmup:
+            vals.append(r["value"] if r["value"] is not None else float("nan"))
+            last = r
+    v = float(np.mean(vals))
+    nx, ny, nz = grid.nx, grid.ny, grid.nz
+    out = {
+        "impl": "reference", "metric": METRIC, "value": v, "unit": "s", "n_gpus": ws, "steps": a.steps,
+        "warmup": a.warmup, "ms_per_step": v * 1e3, "higher_is_better": False, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded cantilever, Helmholtz-smoothed density)",
+        "config": {"workload": f"{a.config} cantilever {nx}x{ny}x{nz} hex8, reference CPU matrix_free "
+                               f"Float32 Jacobi-PCG (CPUSolver.jl restated)", "parallelism": "host cores"},
+        "cpu_baseline": {**last, "value": v},
+        "e2e": {"value": v, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(out))
+
+
+if __name__ == "__main__":
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)

@@ -1,0 +1,216 @@
+/*
+ * hexagpu.h — C ABI of the GB300-native finite-element solve path of HEXA TopOpt.
+ *
+ * One shared library (libhexagpu.so) exports plain C entry points: no C++ or
+ * torch types cross this boundary, every array is a plain pointer plus sizes.
+ * Each array argument may be a HOST pointer (pageable or pinned) or a DEVICE
+ * pointer on the context's GPU; the library detects which with
+ * cudaPointerGetAttributes and copies only what lives on the host.
+ *
+ * Layouts follow the reference (v119_2025_12_19_HEXATOP_AWS):
+ *   - structured grid of nx*ny*nz hex8 elements of size dx*dy*dz
+ *     (src/Mesh/Mesh.jl:23-60): node (i,j,k), 0-based, has index
+ *     n = i + (nx+1)*(j + (ny+1)*k); element (i,j,k) has index
+ *     e = i + nx*(j + ny*k); element local nodes n1..n8 as Mesh.jl:45-53.
+ *   - displacement / force vectors are interleaved xyz per node (AoS),
+ *     dof = 3*n + c, length 3*nNodes (src/Solvers/GPUSolver.jl:100-108).
+ *   - per-element modulus factor: the reference passes `E .* density`
+ *     (GPUSolver.jl:254); SIMP callers pass Emin + rho^p (E0 - Emin).
+ *
+ * Status codes: 0 converged / ok, 1 not converged (best iterate returned,
+ * as GPUSolver.jl:439-443), negative = error, message in hexa_last_error().
+ * A context is not reentrant: use one per host thread (the reference's
+ * workspaces are process globals, GPUSolver.jl:63).
+ */
+#ifndef HEXAGPU_H
+#define HEXAGPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define HEXA_OK 0
+#define HEXA_NOT_CONVERGED 1
+#define HEXA_ERR_ARG (-1)
+#define HEXA_ERR_CUDA (-2)
+#define HEXA_ERR_NOMEM (-3)
+#define HEXA_ERR_CORRUPT_INPUT (-4) /* NaN/Inf in the stiffness diagonal: GPUSolver.jl:310-315 */
+#define HEXA_ERR_NO_DEVICE (-5)     /* "CUDA not functional!": GPUSolver.jl:470-472 */
+
+typedef struct hexa_ctx hexa_ctx;
+
+typedef struct hexa_grid {
+  int32_t nx, ny, nz; /* elements per axis (geometry.nElem_*_computed) */
+  double dx, dy, dz;  /* element edge lengths (geometry.d*_computed) */
+} hexa_grid;
+
+/* Dirichlet set. clamp_faces bit f fixes all 3 DOFs of every node on face f
+ * (0: x=0, 1: x=max, 2: y=0, 3: y=max, 4: z=0, 5: z=max).  fixed_dof, when
+ * not NULL, is 3*nNodes bytes, nonzero = fixed (the reference's
+ * bc_indicator > 0 test, GPUSolver.jl:170-180).  The two are OR-ed. */
+typedef struct hexa_bc {
+  uint32_t clamp_faces;
+  const uint8_t* fixed_dof;
+} hexa_bc;
+
+enum { HEXA_PRECOND_JACOBI = 0, HEXA_PRECOND_MULTIGRID = 1 };
+enum { HEXA_PREC_FP64 = 0, HEXA_PREC_MIXED = 1, HEXA_PREC_FP32 = 2 };
+enum { HEXA_SMOOTH_JACOBI = 0, HEXA_SMOOTH_CHEBYSHEV = 1 };
+enum { HEXA_PRECOND_USED_JACOBI = 0, HEXA_PRECOND_USED_MULTIGRID = 1 };
+
+/* Solver parameters.  The first block mirrors configs/default.yaml
+ * solver_parameters (lines 209-237) as read by GPUSolver.jl:215-218 and
+ * Solver.jl:57-59; the second block is new (precision and multigrid). */
+typedef struct hexa_solve_params {
+  double nu;                  /* Poisson ratio (material.nu) */
+  double tol;                 /* solver_parameters.tolerance */
+  int32_t max_iter;           /* solver_parameters.max_iterations (per attempt) */
+  int32_t precond;            /* solver_parameters.preconditioner */
+  double shift_factor;        /* solver_parameters.diagonal_shift_factor */
+  double stagnation_tol;      /* solver_parameters.stagnation_tolerance */
+  int32_t max_shift_attempts; /* solver_parameters.max_shift_attempts */
+  double shift_multiplier;    /* solver_parameters.shift_multiplier */
+  int32_t check_cadence;      /* 1: test ||r|| every iteration; 10: at k=1 and k%10==0 (GPUSolver.jl:379) */
+  int32_t diag_quirk;         /* 1: x-diagonal of K0 for all 3 components (GPUSolver.jl:137) */
+  /* --- additions --- */
+  int32_t precision;          /* HEXA_PREC_* */
+  int32_t mg_levels;          /* 0: automatic */
+  int32_t pre_smooth, post_smooth;
+  int32_t smoother;           /* HEXA_SMOOTH_* */
+  double jacobi_omega;
+  int32_t cheb_degree;
+  int32_t coarse_iters;       /* Jacobi-PCG iterations of the coarsest-level solve */
+  double inner_tol;           /* mixed: relative tolerance of each FP32 correction solve */
+  int32_t max_outer;          /* mixed: maximum refinement steps */
+  int32_t use_graphs;         /* capture PCG iterations / V-cycles in CUDA graphs */
+  int32_t graph_iters;        /* iterations per graph launch (host reads status between launches) */
+  int32_t true_residual;      /* 1: recompute ||f-(K+sI)u||/||f|| in FP64 and iterate until <= tol */
+} hexa_solve_params;
+
+typedef struct hexa_solve_stats {
+  int32_t status;
+  int32_t iterations;       /* PCG iterations (FP32 inner iterations for mixed) */
+  int32_t outer_iterations; /* mixed: refinement steps */
+  int32_t attempts;         /* shift attempts used */
+  int32_t precond_used;     /* HEXA_PRECOND_USED_*: "GMG_GPU" / "Jacobi_GPU" (GPUSolver.jl:463) */
+  int32_t mg_levels;
+  double relres;            /* recursive ||r||/||f_free|| as GPUSolver.jl:380-382 reports */
+  double true_relres;       /* ||f - (K+sigma I) u|| / ||f|| recomputed in FP64 */
+  double shift;             /* sigma = shift_factor * max(diag K_ff) (GPUSolver.jl:343) */
+  double max_diag;
+  double compliance;        /* f . u (src/Main.jl:453) */
+  double setup_ms;          /* device time: upload + hierarchy setup */
+  double solve_ms;          /* device time: iterations + true residual */
+  double total_ms;          /* host wall time of the call */
+  double fine_applies;      /* fine-grid operator applications (FP64 + FP32) */
+  double fine_applies_fp64;
+} hexa_solve_stats;
+
+typedef struct hexa_filter_stats {
+  int32_t status;
+  int32_t iterations;       /* GPUHelmholtz.jl:224 final_iter */
+  double relres;            /* GPUHelmholtz.jl:247 final_rel_res */
+  double solve_ms;
+} hexa_filter_stats;
+
+/* ---- context ----------------------------------------------------------- */
+int hexa_create(int32_t device, hexa_ctx** out);
+void hexa_destroy(hexa_ctx* ctx);
+const char* hexa_last_error(const hexa_ctx* ctx);
+int hexa_version(void);
+void hexa_default_params(hexa_solve_params* p);
+/* device time of the last hexa_* call's timed region, ms (CUDA events) */
+double hexa_last_device_ms(const hexa_ctx* ctx);
+/* number of this library's kernels launched since the context was created */
+int64_t hexa_kernel_launches(const hexa_ctx* ctx);
+
+/* ---- element matrices (host) ------------------------------------------- */
+/* Element.get_canonical_stiffness (src/Core/Element.jl:104-111), E = 1,
+ * 24x24 column-major, DOF order node-major xyz over n1..n8.  Built in FP64
+ * (the reference builds it in Float32 and promotes, GPUSolver.jl:248-249). */
+int hexa_canonical_stiffness(double dx, double dy, double dz, double nu, double* ke_out);
+/* Element.get_scalar_canonical_matrices (src/Core/Element.jl:113-134):
+ * 8x8 Laplacian Ke and consistent mass Me.  quirk=1 keeps the reference's
+ * top-face z = +dz (Element.jl:116); quirk=0 uses the true brick. */
+int hexa_scalar_canonical_matrices(double dx, double dy, double dz, int32_t quirk,
+                                   double* ke_out, double* me_out);
+
+/* ---- (a) operator ------------------------------------------------------ */
+/* y = (K(factor) + sigma I) x restricted to free DOFs, y = 0 at fixed DOFs;
+ * the deterministic node-centric replacement of apply_A!
+ * (GPUSolver.jl:322-330, matvec_unstructured_atomic_kernel! :91-128).
+ * Entries of x at fixed DOFs are ignored (expand_kernel! semantics). */
+int hexa_apply_operator(hexa_ctx* ctx, const hexa_grid* g, const hexa_bc* bc, double nu,
+                        const double* factor, const double* x, double sigma, double* y);
+int hexa_apply_operator_f32(hexa_ctx* ctx, const hexa_grid* g, const hexa_bc* bc, double nu,
+                            const float* factor, const float* x, float sigma, float* y);
+/* Times `reps` back-to-back launches of the operator kernel alone on the
+ * context's stream with CUDA events (inputs already on the device) and
+ * returns the mean launch duration in ms.  precision: HEXA_PREC_FP64 or
+ * HEXA_PREC_FP32 (factor/x/y then float).  mode: 0 y = Ax, 1 y = Ax with
+ * x.Ax, 2 y = b - Ax, 4 y = x + omega (b - Ax)/diag (damped Jacobi). */
+int hexa_time_operator(hexa_ctx* ctx, const hexa_grid* g, const hexa_bc* bc, double nu, int32_t precision,
+                       int32_t mode, const void* factor, const void* x, const void* b, void* y, int32_t reps,
+                       double* avg_ms);
+/* diag(K_ff) per DOF (zero at fixed DOFs): compute_diagonal_atomic_kernel!
+ * (GPUSolver.jl:130-144); diag_quirk as in hexa_solve_params. */
+int hexa_operator_diagonal(hexa_ctx* ctx, const hexa_grid* g, const hexa_bc* bc, double nu,
+                           const double* factor, int32_t diag_quirk, double* diag_out);
+
+/* ---- (a)-(c) solve ------------------------------------------------------ */
+/* Replaces GPUSolver.solve_system_gpu / gpu_matrix_free_cg_solve
+ * (GPUSolver.jl:182-477): solves (K_ff + sigma I) u = f_free.
+ * factor: nElem modulus factors; f: 3*nNodes forces (entries at fixed DOFs
+ * ignored, as f[free_dofs] at GPUSolver.jl:292); u_guess may be NULL;
+ * u_out: 3*nNodes, zeros at fixed DOFs (GPUSolver.jl:446-448). */
+int hexa_solve(hexa_ctx* ctx, const hexa_grid* g, const hexa_bc* bc, const double* factor,
+               const double* f, const hexa_solve_params* p, const double* u_guess,
+               double* u_out, hexa_solve_stats* stats);
+
+/* Same call with the reference's own argument types (GPUSolver.jl:467-469):
+ * Float32 E, density (nElem), f (3*nNodes) and bc_indicator as the Julia
+ * Matrix{Float32}(nNodes,3) in column-major order (>0 = fixed).  The factor
+ * is Float64(Float32(E*density)) as GPUSolver.jl:254.  method_out receives
+ * "GMG_GPU", "Jacobi_GPU" or "Failed_Corrupt_Input". */
+int hexa_solve_system_gpu(hexa_ctx* ctx, const hexa_grid* g, float E, const float* bc_indicator,
+                          const float* f, const float* density, const hexa_solve_params* p,
+                          const float* u_guess, double* u_out, double* relres_out,
+                          char* method_out, int32_t method_cap, hexa_solve_stats* stats);
+
+/* k load cases as one block PCG (each K0/factor load serves k right-hand
+ * sides).  F and U are k consecutive 3*nNodes vectors. */
+int hexa_solve_multi_rhs(hexa_ctx* ctx, const hexa_grid* g, const hexa_bc* bc, const double* factor,
+                         int32_t k, const double* F, const hexa_solve_params* p, double* U,
+                         hexa_solve_stats* stats);
+
+/* ---- (d) Helmholtz density filter -------------------------------------- */
+/* Replaces GPUHelmholtz.apply_gpu_filter! (GPUHelmholtz.jl:422-443):
+ * solves (R^2 K_s + M_s) psi = sum_e rho_e vol/8 with Jacobi-PCG (at most
+ * max_iter iterations, ||r||/||b|| checked every 10), returns the element
+ * mean of psi.  precision: HEXA_PREC_FP64 or HEXA_PREC_FP32 (reference). */
+int hexa_filter(hexa_ctx* ctx, const hexa_grid* g, const double* rho_in, double radius, double tol,
+                int32_t max_iter, int32_t quirk, int32_t precision, double* rho_out,
+                hexa_filter_stats* stats);
+
+/* ---- (e) SIMP sensitivities and OC update ------------------------------ */
+/* dc_e = -penal * rho_e^(penal-1) * (E0 - Emin) * u_e^T K0 u_e and
+ * compliance = sum_e (Emin + rho_e^penal (E0-Emin)) u_e^T K0 u_e. */
+int hexa_sensitivities(hexa_ctx* ctx, const hexa_grid* g, double nu, const double* rho,
+                       const double* u, double Emin, double E0, double penal, double* dc_out,
+                       double* compliance_out);
+/* SIMP modulus factors Emin + rho^penal (E0-Emin) */
+int hexa_simp_factors(hexa_ctx* ctx, int64_t n, const double* rho, double Emin, double E0,
+                      double penal, double* factor_out);
+/* Optimality-criteria update with a bisection on the Lagrange multiplier
+ * until mean(x_new) = volfrac: x_new = clamp(x*sqrt(-dc/(lambda*dv)),
+ * max(0,x-move), min(1,x+move)). */
+int hexa_oc_update(hexa_ctx* ctx, int64_t n, const double* x, const double* dc, const double* dv,
+                   double volfrac, double move, double* x_out, double* lambda_out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* HEXAGPU_H */

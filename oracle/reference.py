@@ -1,0 +1,440 @@
+"""CPU restatement of the reference's FE-solve path (numpy/scipy + hexa_oracle.c).
+
+TEST INFRASTRUCTURE ONLY -- the parity checker and the timed CPU baseline.
+Every function names the reference file:lines it restates (paths relative
+to the reference project root).  Parity is unpinned by the reference (it has
+no tests); the pins are tests/golden (exact rational element matrices) and
+the first-principles checks in tests/test_oracle.py.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import time
+from dataclasses import dataclass
+
+import numpy as np
+import scipy.sparse as sp
+import scipy.sparse.linalg as spla
+
+from .build import build
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        L = C.CDLL(str(build()))
+        P, D, I = C.c_void_p, C.c_double, C.c_int
+        L.ho_canonical_stiffness.argtypes = [D, D, D, D, I, P]
+        L.ho_scalar_matrices.argtypes = [D, D, D, I, P, P]
+        L.ho_apply_K.argtypes = [I, I, I, P, P, P, P]
+        L.ho_diag_K.argtypes = [I, I, I, P, P, I, P]
+        L.ho_element_energy.argtypes = [I, I, I, P, P, P]
+        L.ho_helm_apply.argtypes = [I, I, I, P, P, P]
+        L.ho_helm_rhs.argtypes = [I, I, I, P, D, P]
+        L.ho_helm_extract.argtypes = [I, I, I, P, P]
+        L.ho_cpu_matrix_free_cg.argtypes = [I, I, I, P, C.c_float, P, P, P, C.c_float, I, C.c_float, C.c_float, I, D,
+                                            P, C.POINTER(D), C.POINTER(D), C.POINTER(I)]
+        L.ho_cpu_matrix_free_cg.restype = I
+        L.ho_num_threads.restype = I
+        _lib = L
+    return _lib
+
+
+def _p(a):
+    return a.ctypes.data
+
+
+@dataclass(frozen=True)
+class Grid:
+    nx: int
+    ny: int
+    nz: int
+    dx: float = 1.0
+    dy: float = 1.0
+    dz: float = 1.0
+
+    @property
+    def nnode(self):
+        return (self.nx + 1) * (self.ny + 1) * (self.nz + 1)
+
+    @property
+    def nelem(self):
+        return self.nx * self.ny * self.nz
+
+    @property
+    def ndof(self):
+        return 3 * self.nnode
+
+
+# ------------------------------------------------------------ element matrices
+def canonical_stiffness(dx=1.0, dy=1.0, dz=1.0, nu=0.3, fp32=False) -> np.ndarray:
+    """Element.jl:23-111 (fp32=True evaluates in Float32 as the reference)."""
+    k = np.zeros(576)
+    if lib().ho_canonical_stiffness(dx, dy, dz, nu, int(fp32), _p(k)) != 0:
+        raise ValueError("non-positive Jacobian")
+    return k.reshape(24, 24, order="F")
+
+
+def scalar_matrices(dx=1.0, dy=1.0, dz=1.0, quirk=True):
+    """Element.jl:113-134; quirk keeps the top face at +dz (Element.jl:116)."""
+    ke, me = np.zeros(64), np.zeros(64)
+    lib().ho_scalar_matrices(dx, dy, dz, int(quirk), _p(ke), _p(me))
+    return ke.reshape(8, 8, order="F"), me.reshape(8, 8, order="F")
+
+
+# ---------------------------------------------------------------- mesh / BCs
+def element_nodes(g: Grid) -> np.ndarray:
+    """0-based connectivity in n1..n8 order (src/Mesh/Mesh.jl:44-53)."""
+    NX, NY = g.nx + 1, g.ny + 1
+    ek, ej, ei = np.meshgrid(np.arange(g.nz), np.arange(g.ny), np.arange(g.nx), indexing="ij")
+    n1 = (ei + NX * (ej + NY * ek)).ravel()
+    off = [0, 1, 1 + NX, NX, NX * NY, 1 + NX * NY, 1 + NX + NX * NY, NX + NX * NY]
+    return np.stack([n1 + o for o in off], axis=1)
+
+
+def fixed_mask(g: Grid, clamp_faces: int = 0, fixed_dof=None) -> np.ndarray:
+    NX, NY, NZ = g.nx + 1, g.ny + 1, g.nz + 1
+    m = np.zeros((NZ, NY, NX, 3), dtype=bool)
+    sel = [np.s_[:, :, 0], np.s_[:, :, -1], np.s_[:, 0, :], np.s_[:, -1, :], np.s_[0, :, :], np.s_[-1, :, :]]
+    for b in range(6):
+        if clamp_faces >> b & 1:
+            m[sel[b]] = True
+    m = m.reshape(-1)
+    if fixed_dof is not None:
+        m |= np.asarray(fixed_dof).reshape(-1) != 0
+    return m
+
+
+# ----------------------------------------------------------------- operators
+def apply_K(g: Grid, K0, factor, x) -> np.ndarray:
+    """Element scatter y = sum_e factor_e K0 u_e (GPUSolver.jl:91-128), full DOFs."""
+    K0 = np.asfortranarray(K0, dtype=np.float64).ravel(order="F").copy()
+    y = np.zeros(g.ndof)
+    lib().ho_apply_K(g.nx, g.ny, g.nz, _p(K0), _p(np.ascontiguousarray(factor, dtype=np.float64)),
+                     _p(np.ascontiguousarray(x, dtype=np.float64)), _p(y))
+    return y
+
+
+def apply_A(g: Grid, K0, factor, x, fixed, sigma=0.0) -> np.ndarray:
+    """apply_A! + shift (GPUSolver.jl:322-330,372): (K_ff + sigma I) x_free, zeros at fixed DOFs."""
+    xm = np.where(fixed, 0.0, x)
+    y = apply_K(g, K0, factor, xm) + sigma * xm
+    y[fixed] = 0.0
+    return y
+
+
+def diag_K(g: Grid, K0, factor, quirk=True) -> np.ndarray:
+    """compute_diagonal_atomic_kernel! (GPUSolver.jl:130-144)."""
+    K0 = np.asfortranarray(K0, dtype=np.float64).ravel(order="F").copy()
+    d = np.zeros(g.ndof)
+    lib().ho_diag_K(g.nx, g.ny, g.nz, _p(K0), _p(np.ascontiguousarray(factor, dtype=np.float64)), int(quirk), _p(d))
+    return d
+
+
+def assemble_K(g: Grid, K0, factor) -> sp.csr_matrix:
+    """Global COO assembly, 576 entries per element (DirectSolver.jl:62-103)."""
+    en = element_nodes(g)
+    dofs = (3 * en[:, :, None] + np.arange(3)[None, None, :]).reshape(g.nelem, 24)
+    rows = np.repeat(dofs, 24, axis=1).ravel()
+    cols = np.tile(dofs, (1, 24)).ravel()
+    vals = (np.asarray(factor)[:, None] * np.asarray(K0).ravel(order="C")[None, :]).ravel()
+    return sp.csr_matrix((vals, (rows, cols)), shape=(g.ndof, g.ndof))
+
+
+def direct_solve(g: Grid, K0, factor, f, fixed, sigma=0.0) -> np.ndarray:
+    """(K_ff + sigma I) u = f_free by sparse LU (the DirectSolver.jl method)."""
+    K = assemble_K(g, K0, factor)
+    free = np.nonzero(~fixed)[0]
+    Kff = (K[free][:, free] + sigma * sp.identity(free.size)).tocsc()
+    u = np.zeros(g.ndof)
+    u[free] = spla.spsolve(Kff, np.asarray(f)[free])
+    return u
+
+
+# ----------------------------------------------------- reference PCG control
+@dataclass
+class PcgInfo:
+    iterations: list
+    shifts: list
+    final_rel: float
+    success: bool
+    name: str
+
+
+def pcg_reference(g: Grid, K0, factor, f, fixed, *, tol, max_iter, shift_factor, stagnation_tol=0.0,
+                  max_shift_attempts=3, shift_multiplier=10.0, u_guess=None, diag_quirk=True, cadence=10):
+    """Jacobi branch of gpu_matrix_free_cg_solve (GPUSolver.jl:182-465) on free DOFs."""
+    free = ~fixed
+    d = diag_K(g, K0, factor, quirk=diag_quirk)[free]
+    max_diag = d.max()
+    if np.isnan(max_diag) or np.isinf(max_diag):
+        return np.zeros(g.ndof), float("nan"), PcgInfo([], [], float("nan"), False, "Failed_Corrupt_Input")
+    b = np.asarray(f, dtype=np.float64)[free]
+    norm_b = np.linalg.norm(b)
+    n = b.size
+
+    def A(v):
+        full = np.zeros(g.ndof)
+        full[free] = v
+        return apply_K(g, K0, factor, full)[free]
+
+    x = np.zeros(n)
+    best_x = np.zeros(n)
+    final_rel = 0.0
+    cur_shift = shift_factor
+    success = False
+    iters, shifts = [], []
+    for attempt in range(1, max_shift_attempts + 1):
+        real_shift = cur_shift * max_diag
+        shifts.append(real_shift)
+        diverged = False
+        if u_guess is not None and attempt == 1:
+            x = np.asarray(u_guess, dtype=np.float64)[free].copy()
+        elif attempt > 1:
+            x = np.zeros(n)
+        Minv = 1.0 / (d + real_shift)
+        r = b - (A(x) + real_shift * x)
+        z = r * Minv
+        p = z.copy()
+        rz = r @ z
+        best_rel = np.inf
+        solve_ok = False
+        k = 0
+        for k in range(1, max_iter + 1):
+            Ap = A(p) + real_shift * p
+            denom = p @ Ap
+            if abs(denom) < 1e-20:
+                break
+            alpha = rz / denom
+            x = x + alpha * p
+            r = r - alpha * Ap
+            if k == 1 or (cadence <= 1) or k % cadence == 0:
+                rel = np.linalg.norm(r) / norm_b
+                final_rel = rel
+                if rel < best_rel:
+                    best_rel = rel
+                    best_x = x.copy()
+                if rel < tol:
+                    solve_ok = True
+                    break
+                if np.isnan(rel) or np.isinf(rel) or rel > 10.0 or (k > 500 and rel > best_rel * 100.0):
+                    diverged = True
+                    break
+            z = r * Minv
+            rz_new = r @ z
+            p = z + (rz_new / rz) * p
+            rz = rz_new
+        iters.append(k)
+        if solve_ok:
+            success = True
+            break
+        if diverged and attempt < max_shift_attempts:
+            cur_shift *= shift_multiplier
+            continue
+        if stagnation_tol > 0.0 and best_rel < stagnation_tol:
+            success = True
+            x = best_x
+            break
+        cur_shift *= shift_multiplier
+    if not success:
+        x = best_x
+    u = np.zeros(g.ndof)
+    u[free] = x
+    return u, final_rel, PcgInfo(iters, shifts, final_rel, success, "Jacobi_GPU")
+
+
+def cg_tight(g: Grid, K0, factor, f, fixed, sigma=0.0, tol=1e-13, max_iter=200000):
+    """Plain Jacobi-PCG to a tight relative residual (oracle solution for grids too big for LU)."""
+    free = ~fixed
+    d = diag_K(g, K0, factor, quirk=False)[free] + sigma
+    b = np.asarray(f, dtype=np.float64)[free]
+
+    def A(v):
+        full = np.zeros(g.ndof)
+        full[free] = v
+        return apply_K(g, K0, factor, full)[free] + sigma * v
+
+    x = np.zeros_like(b)
+    r = b.copy()
+    z = r / d
+    p = z.copy()
+    rz = r @ z
+    nb = np.linalg.norm(b)
+    for k in range(max_iter):
+        Ap = A(p)
+        a = rz / (p @ Ap)
+        x += a * p
+        r -= a * Ap
+        if np.linalg.norm(r) / nb < tol:
+            break
+        z = r / d
+        rzn = r @ z
+        p = z + (rzn / rz) * p
+        rz = rzn
+    r = b - A(x)
+    u = np.zeros(g.ndof)
+    u[free] = x
+    return u, np.linalg.norm(r) / nb, k + 1
+
+
+# --------------------------------------------------------------- Helmholtz
+def helm_matrix(g: Grid, R: float, quirk=True):
+    Ke, Me = scalar_matrices(g.dx, g.dy, g.dz, quirk)
+    return R * R * Ke + Me
+
+
+def helm_apply(g: Grid, Ae, x):
+    y = np.zeros(g.nnode)
+    A = np.asfortranarray(Ae).ravel(order="F").copy()
+    lib().ho_helm_apply(g.nx, g.ny, g.nz, _p(A), _p(np.ascontiguousarray(x, dtype=np.float64)), _p(y))
+    return y
+
+
+def helm_rhs(g: Grid, rho):
+    b = np.zeros(g.nnode)
+    lib().ho_helm_rhs(g.nx, g.ny, g.nz, _p(np.ascontiguousarray(rho, dtype=np.float64)), g.dx * g.dy * g.dz / 8.0, _p(b))
+    return b
+
+
+def helm_extract(g: Grid, psi):
+    out = np.zeros(g.nelem)
+    lib().ho_helm_extract(g.nx, g.ny, g.nz, _p(np.ascontiguousarray(psi, dtype=np.float64)), _p(out))
+    return out
+
+
+def helmholtz_reference(g: Grid, rho, R, tol, max_iter=200, quirk=True):
+    """solve_helmholtz_on_gpu (GPUHelmholtz.jl:190-266): Jacobi-PCG, test every 10 iterations."""
+    Ae = helm_matrix(g, R, quirk)
+    en = element_nodes(g)
+    diag = np.zeros(g.nnode)
+    np.add.at(diag, en.ravel(), np.tile(np.diag(Ae), g.nelem))
+    inv_diag = 1.0 / diag
+    b = helm_rhs(g, rho)
+    norm_b = np.linalg.norm(b)
+    if norm_b == 0.0:
+        return np.asarray(rho, dtype=np.float64).copy(), 0, 0.0
+    x = np.zeros(g.nnode)
+    r = b.copy()
+    z = r * inv_diag
+    p = z.copy()
+    rho_old = r @ z
+    final_rel, final_iter = 0.0, 0
+    for it in range(1, max_iter + 1):
+        final_iter = it
+        Ap = helm_apply(g, Ae, p)
+        alpha = rho_old / (p @ Ap)
+        x += alpha * p
+        r -= alpha * Ap
+        if it % 10 == 0:
+            final_rel = np.linalg.norm(r) / norm_b
+            if final_rel < tol:
+                break
+        z = r * inv_diag
+        rho_new = r @ z
+        p = z + (rho_new / rho_old) * p
+        rho_old = rho_new
+    return helm_extract(g, x), final_iter, final_rel
+
+
+def helmholtz_direct(g: Grid, rho, R, quirk=True, shift=0.0):
+    """assemble_helmholtz_system + apply_helmholtz_filter_cpu (TopOpt.jl:32-127);
+    the reference's CPU path adds a 1e-9 diagonal shift (TopOpt.jl:75-76)."""
+    Ae = helm_matrix(g, R, quirk)
+    en = element_nodes(g)
+    rows = np.repeat(en, 8, axis=1).ravel()
+    cols = np.tile(en, (1, 8)).ravel()
+    vals = np.tile(Ae.ravel(order="C"), g.nelem)
+    A = sp.csc_matrix((vals, (rows, cols)), shape=(g.nnode, g.nnode))
+    if shift:
+        A = A + shift * sp.identity(g.nnode, format="csc")
+    psi = spla.spsolve(A.tocsc(), helm_rhs(g, rho))
+    return helm_extract(g, psi)
+
+
+# -------------------------------------------------------------- SIMP / OC
+def simp_factors(rho, Emin=1e-9, E0=1.0, penal=3.0):
+    return Emin + np.power(rho, penal) * (E0 - Emin)
+
+
+def element_energy(g: Grid, K0, u):
+    ce = np.zeros(g.nelem)
+    K = np.asfortranarray(K0).ravel(order="F").copy()
+    lib().ho_element_energy(g.nx, g.ny, g.nz, _p(K), _p(np.ascontiguousarray(u, dtype=np.float64)), _p(ce))
+    return ce
+
+
+def sensitivities(g: Grid, K0, rho, u, Emin=1e-9, E0=1.0, penal=3.0):
+    ce = element_energy(g, K0, u)
+    dc = -penal * np.power(rho, penal - 1.0) * (E0 - Emin) * ce
+    c = float(np.sum(simp_factors(rho, Emin, E0, penal) * ce))
+    return dc, c
+
+
+def oc_update(x, dc, dv, volfrac, move=0.2, tol=1e-12):
+    """OC step of the 88-line code (Andreassen et al. 2011): bisection on lambda
+    in [0, 1e9] until (l2-l1)/(l1+l2) <= tol; returns the update at the last
+    midpoint tested and that midpoint."""
+    l1, l2 = 0.0, 1e9
+    n = x.size
+    xnew, lmid = x, 0.5 * (l1 + l2)
+    while (l2 - l1) / (l1 + l2) > tol:
+        lmid = 0.5 * (l2 + l1)
+        xnew = np.maximum(0.0, np.maximum(x - move, np.minimum(1.0, np.minimum(x + move, x * np.sqrt(-dc / dv / lmid)))))
+        if xnew.sum() > volfrac * n:
+            l1 = lmid
+        else:
+            l2 = lmid
+    return xnew, lmid
+
+
+def simp_loop(g: Grid, x0, f, fixed, *, nu=0.3, Emin=1e-9, E0=1.0, penal=3.0, volfrac=0.3, R=0.6, move=0.2,
+              n_iter=10, sigma_factor=1e-10, solve_tol=1e-13):
+    """The SIMP + OC loop of topopt.run_simp, with exact (LU) filters and tight solves."""
+    K0 = canonical_stiffness(g.dx, g.dy, g.dz, nu)
+    dv = helmholtz_direct(g, np.ones(g.nelem), R, quirk=False)
+    x = np.asarray(x0, dtype=np.float64).copy()
+    hist = []
+    for _ in range(n_iter):
+        xphys = helmholtz_direct(g, x, R, quirk=False)
+        fac = simp_factors(xphys, Emin, E0, penal)
+        sigma = sigma_factor * diag_K(g, K0, fac, quirk=True)[~fixed].max()
+        if g.ndof <= 60000:
+            u = direct_solve(g, K0, fac, f, fixed, sigma)
+        else:
+            u, _, _ = cg_tight(g, K0, fac, f, fixed, sigma, tol=solve_tol)
+        dc, c = sensitivities(g, K0, xphys, u, Emin, E0, penal)
+        dcx = helmholtz_direct(g, dc, R, quirk=False)
+        hist.append(dict(compliance=c, u=u, dc=dc, xphys=xphys))
+        x, _ = oc_update(x, dcx, dv, volfrac, move)
+    return hist
+
+
+# ------------------------------------------------------------ CPU baseline
+def cpu_matrix_free_cg(g: Grid, E, density, f, fixed_dof, *, nu=0.3, min_stiffness_threshold=1e-3, max_iter=1000,
+                       tol=1e-6, shift_factor=1e-6, nthreads=None, max_seconds=0.0):
+    """CPUSolver.solve_system_cpu (CPUSolver.jl:56-272) in Float32, timed.
+
+    Returns (u Float32, relres, iterations, seconds)."""
+    L = lib()
+    K0 = canonical_stiffness(g.dx, g.dy, g.dz, nu, fp32=True).astype(np.float32).ravel(order="F").copy()
+    x = np.zeros(g.ndof, dtype=np.float32)
+    rel, sec, it = C.c_double(), C.c_double(), C.c_int()
+    nthreads = nthreads or L.ho_num_threads()
+    L.ho_cpu_matrix_free_cg(g.nx, g.ny, g.nz, _p(K0), float(E), _p(np.ascontiguousarray(density, dtype=np.float32)),
+                            _p(np.ascontiguousarray(f, dtype=np.float32)),
+                            _p(np.ascontiguousarray(fixed_dof, dtype=np.uint8)), float(min_stiffness_threshold),
+                            int(max_iter), float(tol), float(shift_factor), int(nthreads), float(max_seconds), _p(x),
+                            C.byref(rel), C.byref(sec), C.byref(it))
+    return x, rel.value, it.value, sec.value
+
+
+def num_threads() -> int:
+    return int(lib().ho_num_threads())
+
+
+def wall(fn, *a, **k):
+    t = time.perf_counter()
+    r = fn(*a, **k)
+    return r, time.perf_counter() - t

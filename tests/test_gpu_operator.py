@@ -1,0 +1,95 @@
+"""(a) The node-centric GPU operator against the oracle's element scatter
+(GPUSolver.jl:91-128 restated), through the C ABI."""
+import numpy as np
+import pytest
+
+from v119_2025_12_19_hexatop_aws_gb300 import _lib
+from v119_2025_12_19_hexatop_aws_gb300.solver import apply_operator, operator_diagonal
+
+pytestmark = pytest.mark.gpu
+
+GRIDS = [(1, 1, 1), (2, 1, 1), (4, 2, 2), (5, 3, 7), (33, 17, 9), (62, 15, 20), (31, 7, 3)]
+
+
+def _case(oracle, rng, dims, h=(1.0, 1.0, 1.0), faces=1, nodemask=False):
+    g = oracle.Grid(*dims, *h)
+    fac = rng.uniform(1e-3, 1.0, g.nelem)
+    x = rng.standard_normal(g.ndof)
+    fixed_dof = None
+    if nodemask:
+        fixed_dof = (rng.uniform(size=g.ndof) < 0.05).astype(np.uint8)
+    fixed = oracle.fixed_mask(g, faces, fixed_dof)
+    return g, fac, x, fixed_dof, fixed
+
+
+@pytest.mark.parametrize("dims", GRIDS)
+@pytest.mark.parametrize("sigma", [0.0, 1e-3])
+def test_apply_fp64_matches_oracle(ctx, oracle, rng, dims, sigma):
+    g, fac, x, fd, fixed = _case(oracle, rng, dims, faces=1)
+    K0 = oracle.canonical_stiffness(1, 1, 1, 0.3)
+    y_ref = oracle.apply_A(g, K0, fac, x, fixed, sigma)
+    y = apply_operator(_lib.make_grid(*dims), fac, x, nu=0.3, sigma=sigma, clamp_faces=1, ctx=ctx)
+    scale = np.abs(y_ref).max()
+    assert np.abs(y - y_ref).max() <= 1e-13 * scale
+
+
+@pytest.mark.parametrize("dims", [(5, 3, 7), (33, 17, 9)])
+def test_apply_brick_nodemask_faces(ctx, oracle, rng, dims):
+    h = (1.0, 2.0, 0.5)
+    g, fac, x, fd, fixed = _case(oracle, rng, dims, h=h, faces=0b010110, nodemask=True)
+    K0 = oracle.canonical_stiffness(*h, 0.25)
+    y_ref = oracle.apply_A(g, K0, fac, x, fixed, 0.0)
+    y = apply_operator(_lib.make_grid(*dims, *h), fac, x, nu=0.25, clamp_faces=0b010110, fixed_dof=fd, ctx=ctx)
+    assert np.abs(y - y_ref).max() <= 1e-13 * np.abs(y_ref).max()
+
+
+@pytest.mark.parametrize("dims", [(4, 2, 2), (33, 17, 9)])
+def test_apply_fp32_matches_oracle(ctx, oracle, rng, dims):
+    g, fac, x, fd, fixed = _case(oracle, rng, dims, faces=1)
+    K0 = oracle.canonical_stiffness(1, 1, 1, 0.3)
+    y_ref = oracle.apply_A(g, K0, fac.astype(np.float32).astype(np.float64), x.astype(np.float32).astype(np.float64), fixed)
+    y = apply_operator(_lib.make_grid(*dims), fac.astype(np.float32), x.astype(np.float32), clamp_faces=1, ctx=ctx,
+                       fp32=True)
+    assert np.abs(y.astype(np.float64) - y_ref).max() <= 2e-6 * np.abs(y_ref).max()
+
+
+def test_apply_is_deterministic(ctx, oracle, rng):
+    g, fac, x, fd, fixed = _case(oracle, rng, (40, 20, 20))
+    grid = _lib.make_grid(40, 20, 20)
+    y1 = apply_operator(grid, fac, x, clamp_faces=1, ctx=ctx)
+    y2 = apply_operator(grid, fac, x, clamp_faces=1, ctx=ctx)
+    assert np.array_equal(y1, y2)
+
+
+def test_rigid_body_modes_are_in_the_kernel(ctx, oracle, rng):
+    dims = (9, 5, 6)
+    g = oracle.Grid(*dims)
+    fac = rng.uniform(0.1, 1.0, g.nelem)
+    NX, NY, NZ = dims[0] + 1, dims[1] + 1, dims[2] + 1
+    k, j, i = np.meshgrid(np.arange(NZ), np.arange(NY), np.arange(NX), indexing="ij")
+    X = np.stack([i.ravel(), j.ravel(), k.ravel()], 1).astype(np.float64)
+    modes = [np.tile([1.0, 0, 0], g.nnode), np.stack([-X[:, 1], X[:, 0], 0 * X[:, 0]], 1).ravel()]
+    for u in modes:
+        y = apply_operator(_lib.make_grid(*dims), fac, u, ctx=ctx)
+        assert np.abs(y).max() < 1e-12 * np.abs(u).max()
+
+
+def test_ignores_values_at_fixed_dofs(ctx, oracle, rng):
+    g, fac, x, fd, fixed = _case(oracle, rng, (6, 4, 4))
+    x2 = x.copy()
+    x2[fixed] = 1e6
+    grid = _lib.make_grid(6, 4, 4)
+    assert np.array_equal(apply_operator(grid, fac, x, clamp_faces=1, ctx=ctx),
+                          apply_operator(grid, fac, x2, clamp_faces=1, ctx=ctx))
+
+
+@pytest.mark.parametrize("quirk", [0, 1])
+def test_diagonal_matches_oracle(ctx, oracle, rng, quirk):
+    dims, h = (7, 5, 3), (1.0, 2.0, 0.5)
+    g = oracle.Grid(*dims, *h)
+    fac = rng.uniform(0.01, 1, g.nelem)
+    K0 = oracle.canonical_stiffness(*h, 0.3)
+    d_ref = oracle.diag_K(g, K0, fac, quirk=bool(quirk))
+    d_ref[oracle.fixed_mask(g, 1)] = 0
+    d = operator_diagonal(_lib.make_grid(*dims, *h), fac, clamp_faces=1, diag_quirk=quirk, ctx=ctx)
+    assert np.abs(d - d_ref).max() <= 1e-14 * d_ref.max()

@@ -1,0 +1,184 @@
+"""(a)-(c) GPU solves through the C ABI against the oracle: direct LU
+solutions of the same shifted system, and the reference's Jacobi-PCG control
+flow restated (GPUSolver.jl:182-465)."""
+import numpy as np
+import pytest
+
+from v119_2025_12_19_hexatop_aws_gb300 import _lib, workloads
+from v119_2025_12_19_hexatop_aws_gb300.boundary import apply_external_forces, get_bc_indicator
+from v119_2025_12_19_hexatop_aws_gb300.mesh import generate_mesh
+from v119_2025_12_19_hexatop_aws_gb300.solver import solve, solve_system, solve_system_gpu
+
+pytestmark = pytest.mark.gpu
+
+
+def cantilever(oracle, rng, dims, lo=0.1, hi=1.0):
+    g = oracle.Grid(*dims)
+    fac = rng.uniform(lo, hi, g.nelem)
+    f = workloads.edge_load(*dims)
+    fixed = oracle.fixed_mask(g, 1)
+    return g, fac, f, fixed
+
+
+def shift_of(oracle, g, fac, fixed, factor=1e-10):
+    K0 = oracle.canonical_stiffness(1, 1, 1, 0.3)
+    return factor * oracle.diag_K(g, K0, fac, quirk=True)[~fixed].max()
+
+
+def rel(a, b):
+    return np.linalg.norm(a - b) / np.linalg.norm(b)
+
+
+@pytest.mark.parametrize("precond", ["jacobi", "multigrid"])
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_solution_matches_direct(ctx, oracle, rng, precond, precision):
+    dims = (16, 8, 8)
+    g, fac, f, fixed = cantilever(oracle, rng, dims)
+    K0 = oracle.canonical_stiffness(1, 1, 1, 0.3)
+    sigma = shift_of(oracle, g, fac, fixed)
+    u_ref = oracle.direct_solve(g, K0, fac, f, fixed, sigma)
+    p = _lib.default_params(precond=precond, precision=precision, tol=1e-13, max_iter=20000, mg_levels=3)
+    u, st = solve(_lib.make_grid(*dims), fac, f, clamp_faces=1, params=p, ctx=ctx)
+    assert st["status"] == 0
+    assert st["true_relres"] <= 1e-13
+    assert rel(u, u_ref) <= 1e-10
+    assert abs(f @ u - f @ u_ref) <= 1e-10 * abs(f @ u_ref)
+    assert st["compliance"] == pytest.approx(f @ u_ref, rel=1e-10)
+
+
+def test_fp32_solution_close(ctx, oracle, rng):
+    dims = (16, 8, 8)
+    g, fac, f, fixed = cantilever(oracle, rng, dims)
+    K0 = oracle.canonical_stiffness(1, 1, 1, 0.3)
+    u_ref = oracle.direct_solve(g, K0, fac, f, fixed, shift_of(oracle, g, fac, fixed))
+    p = _lib.default_params(precond="jacobi", precision="fp32", tol=1e-5, max_iter=20000)
+    u, st = solve(_lib.make_grid(*dims), fac, f, clamp_faces=1, params=p, ctx=ctx)
+    assert rel(u, u_ref) <= 1e-3
+
+
+@pytest.mark.parametrize("dims", [(12, 6, 6), (20, 10, 10)])
+def test_jacobi_iteration_count_matches_reference(ctx, oracle, rng, dims):
+    g, fac, f, fixed = cantilever(oracle, rng, dims)
+    K0 = oracle.canonical_stiffness(1, 1, 1, 0.3)
+    u_ref, rel_ref, info = oracle.pcg_reference(g, K0, fac, f, fixed, tol=1e-9, max_iter=20000, shift_factor=1e-10)
+    p = _lib.default_params(precond="jacobi", tol=1e-9, max_iter=20000, check_cadence=10, true_residual=0)
+    u, st = solve(_lib.make_grid(*dims), fac, f, clamp_faces=1, params=p, ctx=ctx)
+    assert st["status"] == 0 and info.success
+    assert abs(st["iterations"] - info.iterations[-1]) <= 10
+    assert st["relres"] < 1e-9
+    assert rel(u, u_ref) < 1e-7
+
+
+def test_multigrid_beats_jacobi(ctx, oracle, rng):
+    dims = (32, 16, 16)
+    g, fac, f, fixed = cantilever(oracle, rng, dims)
+    grid = _lib.make_grid(*dims)
+    _, sj = solve(grid, fac, f, clamp_faces=1, params=_lib.default_params(precond="jacobi"), ctx=ctx)
+    _, sm = solve(grid, fac, f, clamp_faces=1, params=_lib.default_params(precond="multigrid"), ctx=ctx)
+    assert sm["status"] == 0 and sj["status"] == 0
+    assert sm["iterations"] * 3 < sj["iterations"]
+    assert sm["true_relres"] <= 1e-9 and sj["true_relres"] <= 1e-9
+
+
+def test_solve_is_deterministic(ctx, oracle, rng):
+    dims = (24, 12, 12)
+    g, fac, f, fixed = cantilever(oracle, rng, dims)
+    grid = _lib.make_grid(*dims)
+    u1, _ = solve(grid, fac, f, clamp_faces=1, ctx=ctx)
+    u2, _ = solve(grid, fac, f, clamp_faces=1, ctx=ctx)
+    assert np.array_equal(u1, u2)
+
+
+def test_without_graphs_same_answer(ctx, oracle, rng):
+    dims = (16, 8, 8)
+    g, fac, f, fixed = cantilever(oracle, rng, dims)
+    grid = _lib.make_grid(*dims)
+    u1, s1 = solve(grid, fac, f, clamp_faces=1, params=_lib.default_params(use_graphs=1), ctx=ctx)
+    u2, s2 = solve(grid, fac, f, clamp_faces=1, params=_lib.default_params(use_graphs=0), ctx=ctx)
+    assert np.array_equal(u1, u2) and s1["iterations"] == s2["iterations"]
+
+
+def _reference_inputs(dims):
+    nodes, elements, _ = generate_mesh(*dims)
+    bc = get_bc_indicator(nodes.shape[0], nodes, [{"location": [0, ":", ":"], "DoFs": [1, 2, 3]}])
+    F = np.zeros(3 * nodes.shape[0], dtype=np.float32)
+    apply_external_forces(F, [{"location": ["100%", ":", 0], "F": [0, 0, -1]}], nodes)
+    return nodes, elements, bc, F
+
+
+def test_reference_signature_entry_point(ctx, oracle, rng):
+    dims = (12, 6, 6)
+    nodes, elements, bc, F = _reference_inputs(dims)
+    dens = rng.uniform(0.2, 1.0, 12 * 6 * 6).astype(np.float32)
+    cfg = {"solver_parameters": {"preconditioner": "multigrid", "max_shift_attempts": 5, "shift_multiplier": 4.0},
+           "hardware_profile_applied": "H100", "force_float64": True, "geometry": {}}
+    u, relres, name = solve_system_gpu(nodes, elements, np.float32(1.0), np.float32(0.3), bc, F, dens, tol=1e-9,
+                                       max_iter=30000, shift_factor=1e-10, config=cfg)
+    assert name == "GMG_GPU" and relres < 1e-9
+    g = oracle.Grid(*dims)
+    fixed = oracle.fixed_mask(g, 0, (bc > 0).astype(np.uint8).ravel())
+    fac = (np.float32(1.0) * dens).astype(np.float64)
+    K0 = oracle.canonical_stiffness(1, 1, 1, 0.3)
+    sigma = 1e-10 * oracle.diag_K(g, K0, fac, quirk=True)[~fixed].max()
+    u_ref = oracle.direct_solve(g, K0, fac, F.astype(np.float64), fixed, sigma)
+    assert rel(u, u_ref) < 1e-7
+    assert np.all(u[fixed] == 0)
+
+
+def test_solve_system_dispatch(ctx, rng):
+    dims = (8, 4, 4)
+    nodes, elements, bc, F = _reference_inputs(dims)
+    dens = np.full(8 * 4 * 4, 0.5, dtype=np.float32)
+    cfg = {"solver_parameters": {"solver_type": "gpu", "preconditioner": "jacobi", "tolerance": 1e-9,
+                                 "max_iterations": 30000, "diagonal_shift_factor": 1e-10}, "force_float64": True,
+           "geometry": {}}
+    u, relres, name = solve_system(nodes, elements, 1.0, 0.3, bc, F, density=dens, config=cfg, prune_voids=False)
+    assert name == "Jacobi_GPU" and relres < 1e-9
+
+
+def test_corrupt_input_returns_sentinel(ctx):
+    dims = (6, 3, 3)
+    nodes, elements, bc, F = _reference_inputs(dims)
+    dens = np.full(6 * 3 * 3, 0.5, dtype=np.float32)
+    dens[5] = np.nan
+    u, relres, name = solve_system_gpu(nodes, elements, 1.0, 0.3, bc, F, dens, tol=1e-9, config={"force_float64": True})
+    assert name == "Failed_Corrupt_Input" and np.isnan(relres) and not u.any()
+
+
+def test_max_iter_returns_best_iterate_not_converged(ctx, oracle, rng):
+    dims = (16, 8, 8)
+    g, fac, f, fixed = cantilever(oracle, rng, dims)
+    p = _lib.default_params(precond="jacobi", max_iter=5, max_shift_attempts=1)
+    u, st = solve(_lib.make_grid(*dims), fac, f, clamp_faces=1, params=p, ctx=ctx)
+    assert st["status"] == _lib.HEXA_NOT_CONVERGED
+    assert np.isfinite(u).all() and np.abs(u).max() > 0
+
+
+def test_u_guess_warm_start(ctx, oracle, rng):
+    dims = (16, 8, 8)
+    g, fac, f, fixed = cantilever(oracle, rng, dims)
+    grid = _lib.make_grid(*dims)
+    p = _lib.default_params(precond="jacobi")
+    u, s0 = solve(grid, fac, f, clamp_faces=1, params=p, ctx=ctx)
+    u2, s1 = solve(grid, fac, f, clamp_faces=1, params=p, u_guess=u, ctx=ctx)
+    assert s1["iterations"] < s0["iterations"] // 4
+
+
+def test_zero_load_gives_zero(ctx, oracle, rng):
+    dims = (6, 3, 3)
+    g, fac, f, fixed = cantilever(oracle, rng, dims)
+    u, st = solve(_lib.make_grid(*dims), fac, np.zeros_like(f), clamp_faces=1, ctx=ctx)
+    assert st["status"] == 0 and not u.any()
+
+
+def test_void_contrast_mixed_reaches_fp64_residual(ctx, oracle, rng):
+    dims = (32, 16, 16)
+    g = oracle.Grid(*dims)
+    rho = np.clip(0.3 + 0.4 * rng.standard_normal(g.nelem), 0.001, 1.0)
+    fac = 1e-9 + rho ** 3 * (1 - 1e-9)
+    f = workloads.edge_load(*dims)
+    grid = _lib.make_grid(*dims)
+    u64, s64 = solve(grid, fac, f, clamp_faces=1, params=_lib.default_params(precision="fp64"), ctx=ctx)
+    um, sm = solve(grid, fac, f, clamp_faces=1, params=_lib.default_params(precision="mixed"), ctx=ctx)
+    assert s64["true_relres"] <= 1e-9 and sm["true_relres"] <= 1e-9
+    assert abs(sm["compliance"] - s64["compliance"]) <= 1e-8 * abs(s64["compliance"])

@@ -1,0 +1,72 @@
+"""(e) SIMP sensitivities and the OC update on the GPU against the oracle
+(the published SIMP/OC method restated; no reference counterpart)."""
+import numpy as np
+import pytest
+
+from v119_2025_12_19_hexatop_aws_gb300 import _lib, workloads
+from v119_2025_12_19_hexatop_aws_gb300.topopt import SimpSetup, oc_update, run_simp, sensitivities, simp_factors
+
+pytestmark = pytest.mark.gpu
+
+
+def test_simp_factors(ctx, rng):
+    rho = rng.uniform(0, 1, 1000)
+    assert np.allclose(simp_factors(rho, 1e-9, 1.0, 3.0, ctx=ctx), 1e-9 + rho ** 3 * (1 - 1e-9), rtol=1e-15, atol=0)
+
+
+@pytest.mark.parametrize("dims", [(3, 2, 2), (17, 9, 5)])
+def test_sensitivities_match_oracle(ctx, oracle, rng, dims):
+    g = oracle.Grid(*dims)
+    rho = rng.uniform(0.01, 1, g.nelem)
+    u = rng.standard_normal(g.ndof)
+    K0 = oracle.canonical_stiffness(1, 1, 1, 0.3)
+    dc_ref, c_ref = oracle.sensitivities(g, K0, rho, u)
+    dc, c = sensitivities(_lib.make_grid(*dims), rho, u, ctx=ctx)
+    assert np.abs(dc - dc_ref).max() <= 1e-12 * np.abs(dc_ref).max()
+    assert c == pytest.approx(c_ref, rel=1e-12)
+
+
+def test_sensitivity_is_the_compliance_derivative(ctx, oracle, rng):
+    # dc/drho_e of c(rho) = f.u(rho) at fixed f equals -u^T dK/drho_e u
+    dims = (6, 3, 3)
+    g = oracle.Grid(*dims)
+    rho = rng.uniform(0.3, 1, g.nelem)
+    f = workloads.edge_load(*dims)
+    fixed = oracle.fixed_mask(g, 1)
+    K0 = oracle.canonical_stiffness(1, 1, 1, 0.3)
+    u = oracle.direct_solve(g, K0, simp_factors(rho, ctx=ctx), f, fixed)
+    dc, _ = sensitivities(_lib.make_grid(*dims), rho, u, ctx=ctx)
+    e, h = 7, 1e-6
+    rp, rm = rho.copy(), rho.copy()
+    rp[e] += h
+    rm[e] -= h
+    cp = f @ oracle.direct_solve(g, K0, simp_factors(rp, ctx=ctx), f, fixed)
+    cm = f @ oracle.direct_solve(g, K0, simp_factors(rm, ctx=ctx), f, fixed)
+    assert dc[e] == pytest.approx((cp - cm) / (2 * h), rel=1e-6)
+
+
+def test_oc_matches_oracle_and_meets_volume(ctx, oracle, rng):
+    n = 50000
+    x = rng.uniform(0.05, 0.6, n)
+    dc = -rng.uniform(0.1, 10, n)
+    dv = np.ones(n)
+    xo, lo = oracle.oc_update(x, dc, dv, 0.3)
+    xg, lg = oc_update(x, dc, dv, 0.3, ctx=ctx)
+    assert lg == pytest.approx(lo, rel=1e-11)
+    assert np.abs(xg - xo).max() <= 1e-10
+    assert abs(xg.mean() - 0.3) < 1e-9
+
+
+def test_simp_loop_small_matches_oracle(ctx, oracle):
+    dims = (12, 6, 6)
+    g = oracle.Grid(*dims)
+    x0 = workloads.c1_density(*dims)
+    f = workloads.edge_load(*dims)
+    R = workloads.helmholtz_R(1.5)
+    S = SimpSetup(grid=_lib.make_grid(*dims), f=f, filter_radius=R,
+                  params=_lib.default_params(precond="jacobi", tol=1e-13, max_iter=50000))
+    hist = run_simp(S, x0, n_iter=4, ctx=ctx)
+    ref = oracle.simp_loop(g, x0, f, oracle.fixed_mask(g, 1), R=R, n_iter=4)
+    for h, r in zip(hist, ref):
+        assert h.compliance == pytest.approx(r["compliance"], rel=1e-9)
+        assert np.abs(h.xphys - r["xphys"]).max() < 1e-9

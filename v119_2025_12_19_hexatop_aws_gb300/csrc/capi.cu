@@ -1,0 +1,769 @@
+// extern "C" entry points of libhexagpu.so (declared in include/hexagpu.h).
+//
+// Every array argument may be a host pointer (pageable or pinned) or a
+// device pointer; host arrays are staged through the context's cached device
+// buffers, device arrays are used in place.
+#include <cuda_runtime.h>
+
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "element.h"
+#include "hexa_kernels.h"
+#include "solver.h"
+
+using namespace hexa;
+
+struct hexa_ctx {
+  Ctx c;
+};
+
+namespace {
+
+constexpr int kRed = 152 * 4;
+
+int set_err(hexa_ctx* h, int code, const std::string& msg) {
+  if (h) h->c.err = msg;
+  return code;
+}
+
+bool valid_grid(const hexa_grid* g) {
+  return g && g->nx >= 1 && g->ny >= 1 && g->nz >= 1 && g->dx > 0 && g->dy > 0 && g->dz > 0 &&
+         (long long)(g->nx + 1) * (g->ny + 1) * (g->nz + 1) * 3LL < (1LL << 40);
+}
+
+// Device view of an input array: the pointer itself when it is on the
+// device, else a cached staging buffer filled by an async H2D copy.
+template <typename T>
+const T* stage_in(Ctx& c, const T* p, size_t n, const char* name) {
+  if (!p) return nullptr;
+  if (is_device_ptr(p)) return p;
+  T* d = c.vec<T>(name, n);
+  if (!d) return nullptr;
+  cudaMemcpyAsync(d, p, n * sizeof(T), cudaMemcpyHostToDevice, c.st);
+  return d;
+}
+
+template <typename T>
+T* out_buf(Ctx& c, T* p, size_t n, const char* name) {
+  if (is_device_ptr(p)) return p;
+  return c.vec<T>(name, n);
+}
+
+template <typename T>
+void stage_out(Ctx& c, T* user, const T* dev, size_t n) {
+  if (user != dev) cudaMemcpyAsync(user, dev, n * sizeof(T), cudaMemcpyDeviceToHost, c.st);
+}
+
+// Per-node fixed bits from a per-DOF byte mask (host or device).
+const uint8_t* node_mask(Ctx& c, const Grid& g, const uint8_t* fixed_dof) {
+  if (!fixed_dof) return nullptr;
+  const long long nn = g.nnode();
+  std::vector<uint8_t> host(3 * nn);
+  if (is_device_ptr(fixed_dof)) {
+    cudaMemcpyAsync(host.data(), fixed_dof, 3 * nn, cudaMemcpyDeviceToHost, c.st);
+    cudaStreamSynchronize(c.st);
+  } else {
+    std::memcpy(host.data(), fixed_dof, 3 * nn);
+  }
+  std::vector<uint8_t> bits(nn);
+  bool any = false;
+  for (long long n = 0; n < nn; ++n) {
+    const uint8_t b = (host[3 * n] ? 1 : 0) | (host[3 * n + 1] ? 2 : 0) | (host[3 * n + 2] ? 4 : 0);
+    bits[n] = b;
+    any |= (b != 0);
+  }
+  if (!any) return nullptr;
+  uint8_t* d = c.vec<uint8_t>("nodemask", nn);
+  if (!d) return nullptr;
+  cudaMemcpyAsync(d, bits.data(), nn, cudaMemcpyHostToDevice, c.st);
+  cudaStreamSynchronize(c.st);  // bits is a local vector
+  return d;
+}
+
+bool prepare_problem(hexa_ctx* h, const hexa_grid* g, const hexa_bc* bc, double nu, const double* factor,
+                     const double* f, Problem* P) {
+  Ctx& c = h->c;
+  P->g = make_grid(g->nx, g->ny, g->nz);
+  P->dx = g->dx;
+  P->dy = g->dy;
+  P->dz = g->dz;
+  P->nu = nu;
+  P->m.faces = bc ? bc->clamp_faces : 0u;
+  P->m.node = bc ? node_mask(c, P->g, bc->fixed_dof) : nullptr;
+  if (bc && bc->fixed_dof && !c.err.empty()) return false;
+  P->fac64 = stage_in<double>(c, factor, P->g.nelem(), "in_factor");
+  if (!P->fac64) return false;
+  if (f) {
+    const double* fr = stage_in<double>(c, f, P->g.ndof(), "in_f_raw");
+    double* fm = c.vec<double>("in_f", P->g.ndof());
+    if (!fr || !fm) return false;
+    launch_mask_copy<double, double>(P->g, P->m, fm, fr, c.st);
+    c.launches++;
+    P->f64 = fm;
+  } else {
+    P->f64 = nullptr;
+  }
+  return true;
+}
+
+double wall_ms(std::chrono::steady_clock::time_point t0) {
+  return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+}
+
+}  // namespace
+
+extern "C" {
+
+int hexa_version(void) { return 100; }
+
+void hexa_default_params(hexa_solve_params* p) {
+  if (!p) return;
+  std::memset(p, 0, sizeof(*p));
+  p->nu = 0.3;
+  p->tol = 1e-9;
+  p->max_iter = 30000;          // configs/default.yaml:222
+  p->precond = HEXA_PRECOND_MULTIGRID;
+  p->shift_factor = 1e-10;      // H100/H200/A100 profile (src/Main.jl:108)
+  p->stagnation_tol = 0.0;
+  p->max_shift_attempts = 3;    // GPUSolver.jl:217 default
+  p->shift_multiplier = 10.0;   // GPUSolver.jl:218 default
+  p->check_cadence = 1;
+  p->diag_quirk = 1;
+  p->precision = HEXA_PREC_FP64;
+  p->mg_levels = 0;
+  p->pre_smooth = 2;
+  p->post_smooth = 2;
+  p->smoother = HEXA_SMOOTH_JACOBI;
+  p->jacobi_omega = 0.6;
+  p->cheb_degree = 2;
+  p->coarse_iters = 30;
+  p->inner_tol = 1e-4;
+  p->max_outer = 20;
+  p->use_graphs = 1;
+  p->graph_iters = 10;
+  p->true_residual = 1;
+}
+
+int hexa_create(int32_t device, hexa_ctx** out) {
+  if (!out) return HEXA_ERR_ARG;
+  *out = nullptr;
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess || n <= 0) {
+    cudaGetLastError();
+    return HEXA_ERR_NO_DEVICE;
+  }
+  if (device < 0 || device >= n) return HEXA_ERR_ARG;
+  hexa_ctx* h = new (std::nothrow) hexa_ctx();
+  if (!h) return HEXA_ERR_NOMEM;
+  Ctx& c = h->c;
+  c.device = device;
+  if (cudaSetDevice(device) != cudaSuccess || cudaStreamCreateWithFlags(&c.st, cudaStreamNonBlocking) != cudaSuccess) {
+    cudaGetLastError();
+    delete h;
+    return HEXA_ERR_CUDA;
+  }
+  for (auto& e : c.ev) cudaEventCreate(&e);
+  cudaMemPool_t pool;
+  if (cudaDeviceGetDefaultMemPool(&pool, device) == cudaSuccess) {
+    uint64_t thr = ~0ULL;
+    cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
+  }
+  c.ticket = c.vec<unsigned>("ticket", 16);
+  c.s = c.vec<PcgScalars>("scalars", 1);
+  c.s2 = c.vec<PcgScalars>("scalars2", 1);
+  c.dscal = c.vec<double>("dscal", 64);
+  if (!c.ticket || !c.s || !c.s2 || !c.dscal || !c.ensure_partials(1 << 16)) {
+    hexa_destroy(h);
+    return HEXA_ERR_NOMEM;
+  }
+  cudaMemsetAsync(c.ticket, 0, 16 * sizeof(unsigned), c.st);
+  cudaMemsetAsync(c.s, 0, sizeof(PcgScalars), c.st);
+  cudaMemsetAsync(c.s2, 0, sizeof(PcgScalars), c.st);
+  if (cudaMallocHost(&c.hs, sizeof(PcgScalars)) != cudaSuccess || cudaMallocHost(&c.hscal, 64 * sizeof(double)) != cudaSuccess) {
+    cudaGetLastError();
+    hexa_destroy(h);
+    return HEXA_ERR_NOMEM;
+  }
+  if (cudaStreamSynchronize(c.st) != cudaSuccess) {
+    cudaGetLastError();
+    hexa_destroy(h);
+    return HEXA_ERR_CUDA;
+  }
+  *out = h;
+  return HEXA_OK;
+}
+
+void hexa_destroy(hexa_ctx* h) {
+  if (!h) return;
+  Ctx& c = h->c;
+  cudaSetDevice(c.device);
+  if (c.st) cudaStreamSynchronize(c.st);
+  for (auto& kv : c.bufs) cudaFreeAsync(kv.second.first, c.st);
+  c.bufs.clear();
+  if (c.st) {
+    cudaStreamSynchronize(c.st);
+    cudaStreamDestroy(c.st);
+  }
+  for (auto& e : c.ev)
+    if (e) cudaEventDestroy(e);
+  if (c.hs) cudaFreeHost(c.hs);
+  if (c.hscal) cudaFreeHost(c.hscal);
+  cudaGetLastError();
+  delete h;
+}
+
+const char* hexa_last_error(const hexa_ctx* h) { return h ? h->c.err.c_str() : "null context"; }
+double hexa_last_device_ms(const hexa_ctx* h) { return h ? h->c.last_ms : 0.0; }
+int64_t hexa_kernel_launches(const hexa_ctx* h) { return h ? h->c.launches : 0; }
+
+int hexa_canonical_stiffness(double dx, double dy, double dz, double nu, double* ke_out) {
+  if (!ke_out) return HEXA_ERR_ARG;
+  return canonical_stiffness(dx, dy, dz, nu, ke_out) == 0 ? HEXA_OK : HEXA_ERR_ARG;
+}
+
+int hexa_scalar_canonical_matrices(double dx, double dy, double dz, int32_t quirk, double* ke_out, double* me_out) {
+  if (!ke_out || !me_out) return HEXA_ERR_ARG;
+  return scalar_matrices(dx, dy, dz, quirk, ke_out, me_out) == 0 ? HEXA_OK : HEXA_ERR_ARG;
+}
+
+}  // extern "C"
+
+template <typename T>
+static int apply_operator_t(hexa_ctx* h, const hexa_grid* g, const hexa_bc* bc, double nu, const T* factor,
+                            const T* x, T sigma, T* y) {
+  if (!h) return HEXA_ERR_ARG;
+  if (!valid_grid(g) || !factor || !x || !y) return set_err(h, HEXA_ERR_ARG, "invalid grid or null array");
+  Ctx& c = h->c;
+  c.err.clear();
+  cudaSetDevice(c.device);
+  ModalK<double> K64;
+  std::string e;
+  if (!build_modal(g->dx, g->dy, g->dz, nu, &K64, &e)) return set_err(h, HEXA_ERR_ARG, e);
+  const Grid G = make_grid(g->nx, g->ny, g->nz);
+  Mask m;
+  m.faces = bc ? bc->clamp_faces : 0u;
+  m.node = bc ? node_mask(c, G, bc->fixed_dof) : nullptr;
+  const T* fac = stage_in<T>(c, factor, G.nelem(), sizeof(T) == 8 ? "ap_fac64" : "ap_fac32");
+  const T* xr = stage_in<T>(c, x, G.ndof(), sizeof(T) == 8 ? "ap_xr64" : "ap_xr32");
+  T* xm = c.vec<T>(sizeof(T) == 8 ? "ap_x64" : "ap_x32", G.ndof());
+  T* yd = out_buf<T>(c, y, G.ndof(), sizeof(T) == 8 ? "ap_y64" : "ap_y32");
+  if (!fac || !xr || !xm || !yd) return HEXA_ERR_NOMEM;
+  launch_mask_copy<T, T>(G, m, xm, xr, c.st);
+  OpArgs<T> a;
+  a.g = G;
+  a.m = m;
+  a.x = xm;
+  a.fac = fac;
+  a.b = nullptr;
+  a.y = yd;
+  if constexpr (sizeof(T) == 8) a.K = K64;
+  else a.K = modal_to_f32(K64);
+  a.sigma = sigma;
+  a.omega = T(0);
+  const int tyw = sizeof(T) == 8 ? 8 : 16;
+  const long long bxy = (long long)((G.NX + 30) / 31) * ((G.NY + tyw - 2) / (tyw - 1));
+  long long nch = (456 + bxy - 1) / bxy;
+  if (nch > G.NZ) nch = G.NZ;
+  a.kchunk = (int)std::max<long long>(2, (G.NZ + nch - 1) / nch);
+  a.diag_quirk = 0;
+  a.red.partials = c.partials;
+  a.red.ticket = c.ticket;
+  a.red.dst = nullptr;
+  a.red.s = nullptr;
+  a.red.op = FIN_NONE;
+  a.red.nsum = 1;
+  a.halt = nullptr;
+  cudaEventRecord(c.ev[0], c.st);
+  launch_op<T>(OP_APPLY, a, c.st);
+  cudaEventRecord(c.ev[1], c.st);
+  c.launches += 2;
+  stage_out<T>(c, y, yd, G.ndof());
+  if (cudaStreamSynchronize(c.st) != cudaSuccess || !c.cuda_ok("apply")) return set_err(h, HEXA_ERR_CUDA, c.err);
+  float ms = 0;
+  cudaEventElapsedTime(&ms, c.ev[0], c.ev[1]);
+  c.last_ms = ms;
+  return HEXA_OK;
+}
+
+
+extern "C" {
+
+int hexa_apply_operator(hexa_ctx* h, const hexa_grid* g, const hexa_bc* bc, double nu, const double* factor,
+                        const double* x, double sigma, double* y) {
+  return apply_operator_t<double>(h, g, bc, nu, factor, x, sigma, y);
+}
+
+int hexa_apply_operator_f32(hexa_ctx* h, const hexa_grid* g, const hexa_bc* bc, double nu, const float* factor,
+                            const float* x, float sigma, float* y) {
+  return apply_operator_t<float>(h, g, bc, nu, factor, x, sigma, y);
+}
+
+}  // extern "C"
+
+template <typename T>
+static int time_operator_t(hexa_ctx* h, const hexa_grid* g, const hexa_bc* bc, double nu, int mode, const T* factor,
+                           const T* x, const T* b, T* y, int reps, double* avg_ms) {
+  Ctx& c = h->c;
+  ModalK<double> K64;
+  std::string e;
+  if (!build_modal(g->dx, g->dy, g->dz, nu, &K64, &e)) return set_err(h, HEXA_ERR_ARG, e);
+  if (!is_device_ptr(factor) || !is_device_ptr(x) || !is_device_ptr(y) || (b && !is_device_ptr(b)))
+    return set_err(h, HEXA_ERR_ARG, "hexa_time_operator takes device arrays");
+  if ((mode == OP_RESID || mode == OP_JACOBI) && !b) return set_err(h, HEXA_ERR_ARG, "mode needs b");
+  const Grid G = make_grid(g->nx, g->ny, g->nz);
+  Mask m;
+  m.faces = bc ? bc->clamp_faces : 0u;
+  m.node = bc ? node_mask(c, G, bc->fixed_dof) : nullptr;
+  OpArgs<T> a;
+  a.g = G;
+  a.m = m;
+  a.x = x;
+  a.fac = factor;
+  a.b = b;
+  a.y = y;
+  if constexpr (sizeof(T) == 8) a.K = K64;
+  else a.K = modal_to_f32(K64);
+  a.sigma = T(0);
+  a.omega = T(0.6);
+  const int tyw = sizeof(T) == 8 ? 8 : 16;
+  const long long bxy = (long long)((G.NX + 30) / 31) * ((G.NY + tyw - 2) / (tyw - 1));
+  long long nch = ((sizeof(T) == 8 ? 456 : 304) + bxy - 1) / bxy;
+  if (nch > G.NZ) nch = G.NZ;
+  a.kchunk = (int)std::max<long long>(2, (G.NZ + nch - 1) / nch);
+  a.diag_quirk = 1;
+  const long long nb = op_num_blocks<T>(G, a.kchunk);
+  if (!c.ensure_partials((size_t)nb * 2 + 64)) return HEXA_ERR_NOMEM;
+  a.red.partials = c.partials;
+  a.red.ticket = c.ticket;
+  a.red.dst = c.dscal + 40;
+  a.red.s = nullptr;
+  a.red.op = FIN_STORE;
+  a.red.nsum = 1;
+  a.halt = nullptr;
+  launch_op<T>(mode, a, c.st);  // warm-up
+  cudaEventRecord(c.ev[0], c.st);
+  for (int r = 0; r < reps; ++r) launch_op<T>(mode, a, c.st);
+  cudaEventRecord(c.ev[1], c.st);
+  c.launches += reps + 1;
+  if (cudaEventSynchronize(c.ev[1]) != cudaSuccess || !c.cuda_ok("time_operator")) return set_err(h, HEXA_ERR_CUDA, c.err);
+  float ms = 0;
+  cudaEventElapsedTime(&ms, c.ev[0], c.ev[1]);
+  *avg_ms = ms / reps;
+  c.last_ms = ms;
+  return HEXA_OK;
+}
+
+extern "C" {
+
+int hexa_time_operator(hexa_ctx* h, const hexa_grid* g, const hexa_bc* bc, double nu, int32_t precision, int32_t mode,
+                       const void* factor, const void* x, const void* b, void* y, int32_t reps, double* avg_ms) {
+  if (!h) return HEXA_ERR_ARG;
+  if (!valid_grid(g) || !factor || !x || !y || !avg_ms || reps < 1 || mode < 0 || mode > 4)
+    return set_err(h, HEXA_ERR_ARG, "invalid arguments");
+  h->c.err.clear();
+  cudaSetDevice(h->c.device);
+  if (precision == HEXA_PREC_FP32)
+    return time_operator_t<float>(h, g, bc, nu, mode, (const float*)factor, (const float*)x, (const float*)b, (float*)y,
+                                  reps, avg_ms);
+  return time_operator_t<double>(h, g, bc, nu, mode, (const double*)factor, (const double*)x, (const double*)b,
+                                 (double*)y, reps, avg_ms);
+}
+
+int hexa_operator_diagonal(hexa_ctx* h, const hexa_grid* g, const hexa_bc* bc, double nu, const double* factor,
+                           int32_t diag_quirk, double* diag_out) {
+  if (!h) return HEXA_ERR_ARG;
+  if (!valid_grid(g) || !factor || !diag_out) return set_err(h, HEXA_ERR_ARG, "invalid grid or null array");
+  Ctx& c = h->c;
+  c.err.clear();
+  cudaSetDevice(c.device);
+  ModalK<double> K64;
+  std::string e;
+  if (!build_modal(g->dx, g->dy, g->dz, nu, &K64, &e)) return set_err(h, HEXA_ERR_ARG, e);
+  const Grid G = make_grid(g->nx, g->ny, g->nz);
+  Mask m;
+  m.faces = bc ? bc->clamp_faces : 0u;
+  m.node = bc ? node_mask(c, G, bc->fixed_dof) : nullptr;
+  const double* fac = stage_in<double>(c, factor, G.nelem(), "ap_fac64");
+  double* d = out_buf<double>(c, diag_out, G.ndof(), "ap_y64");
+  if (!fac || !d) return HEXA_ERR_NOMEM;
+  launch_diag<double>(G, m, fac, K64, diag_quirk, 0.0, d, nullptr, c.st);
+  c.launches++;
+  stage_out<double>(c, diag_out, d, G.ndof());
+  if (cudaStreamSynchronize(c.st) != cudaSuccess || !c.cuda_ok("diagonal")) return set_err(h, HEXA_ERR_CUDA, c.err);
+  return HEXA_OK;
+}
+
+static bool valid_params(const hexa_solve_params* p) {
+  return p && p->tol > 0 && p->max_iter >= 1 && p->nu > -1.0 && p->nu < 0.5 && p->shift_factor >= 0 &&
+         (p->precision == HEXA_PREC_FP64 || p->precision == HEXA_PREC_FP32 || p->precision == HEXA_PREC_MIXED) &&
+         (p->precond == HEXA_PRECOND_JACOBI || p->precond == HEXA_PRECOND_MULTIGRID);
+}
+
+int hexa_solve(hexa_ctx* h, const hexa_grid* g, const hexa_bc* bc, const double* factor, const double* f,
+               const hexa_solve_params* p, const double* u_guess, double* u_out, hexa_solve_stats* stats) {
+  const auto t0 = std::chrono::steady_clock::now();
+  if (!h) return HEXA_ERR_ARG;
+  if (!valid_grid(g) || !factor || !f || !u_out) return set_err(h, HEXA_ERR_ARG, "invalid grid or null array");
+  if (!valid_params(p)) return set_err(h, HEXA_ERR_ARG, "invalid solver parameters");
+  Ctx& c = h->c;
+  c.err.clear();
+  cudaSetDevice(c.device);
+  hexa_solve_stats st;
+  std::memset(&st, 0, sizeof(st));
+  Problem P;
+  if (!prepare_problem(h, g, bc, p->nu, factor, f, &P)) return set_err(h, HEXA_ERR_NOMEM, c.err.empty() ? "staging failed" : c.err);
+  const double* u0 = u_guess ? stage_in<double>(c, u_guess, P.g.ndof(), "in_u0") : nullptr;
+  double* ud = out_buf<double>(c, u_out, P.g.ndof(), "out_u");
+  if (!ud || (u_guess && !u0)) return set_err(h, HEXA_ERR_NOMEM, c.err);
+  int rc = solve_problem(c, P, *p, u0, ud, &st);
+  stage_out<double>(c, u_out, ud, P.g.ndof());
+  if (cudaStreamSynchronize(c.st) != cudaSuccess) {
+    c.cuda_ok("solve");
+    rc = HEXA_ERR_CUDA;
+  }
+  st.status = rc;
+  st.total_ms = wall_ms(t0);
+  c.last_ms = st.setup_ms + st.solve_ms;
+  if (stats) *stats = st;
+  return rc;
+}
+
+int hexa_solve_system_gpu(hexa_ctx* h, const hexa_grid* g, float E, const float* bc_indicator, const float* f,
+                          const float* density, const hexa_solve_params* p, const float* u_guess, double* u_out,
+                          double* relres_out, char* method_out, int32_t method_cap, hexa_solve_stats* stats) {
+  if (!h) return HEXA_ERR_ARG;
+  if (!valid_grid(g) || !f || !density || !u_out || !bc_indicator) return set_err(h, HEXA_ERR_ARG, "invalid grid or null array");
+  Ctx& c = h->c;
+  const long long nn = (long long)(g->nx + 1) * (g->ny + 1) * (g->nz + 1);
+  const long long ne = (long long)g->nx * g->ny * g->nz;
+  // host conversion of the reference's Float32 arguments
+  std::vector<float> hd(ne), hf(3 * nn), hb(3 * nn);
+  auto fetch = [&](const float* src, float* dst, size_t n) {
+    if (is_device_ptr(src)) cudaMemcpy(dst, src, n * sizeof(float), cudaMemcpyDeviceToHost);
+    else std::memcpy(dst, src, n * sizeof(float));
+  };
+  fetch(density, hd.data(), ne);
+  fetch(f, hf.data(), 3 * nn);
+  fetch(bc_indicator, hb.data(), 3 * nn);
+  std::vector<double> fac(ne), fd(3 * nn), ug;
+  for (long long e = 0; e < ne; ++e) fac[e] = (double)(float)(E * hd[e]);  // Vector{T}(E .* density)
+  for (long long i = 0; i < 3 * nn; ++i) fd[i] = (double)hf[i];
+  std::vector<uint8_t> fixed(3 * nn);
+  for (long long n = 0; n < nn; ++n)
+    for (int d = 0; d < 3; ++d) fixed[3 * n + d] = hb[n + nn * d] > 0.0f ? 1 : 0;  // column-major Matrix(nNodes,3)
+  if (u_guess) {
+    std::vector<float> hu(3 * nn);
+    fetch(u_guess, hu.data(), 3 * nn);
+    ug.assign(hu.begin(), hu.end());
+  }
+  hexa_bc bc;
+  bc.clamp_faces = 0;
+  bc.fixed_dof = fixed.data();
+  hexa_solve_stats st;
+  std::memset(&st, 0, sizeof(st));
+  int rc = hexa_solve(h, g, &bc, fac.data(), fd.data(), p, u_guess ? ug.data() : nullptr, u_out, &st);
+  if (relres_out) *relres_out = st.relres;
+  if (method_out && method_cap > 0) {
+    const char* name = (rc == HEXA_ERR_CORRUPT_INPUT) ? "Failed_Corrupt_Input"
+                       : (st.precond_used == HEXA_PRECOND_USED_MULTIGRID ? "GMG_GPU" : "Jacobi_GPU");
+    std::strncpy(method_out, name, (size_t)method_cap - 1);
+    method_out[method_cap - 1] = 0;
+  }
+  if (stats) *stats = st;
+  (void)c;
+  return rc;
+}
+
+int hexa_solve_multi_rhs(hexa_ctx* h, const hexa_grid* g, const hexa_bc* bc, const double* factor, int32_t k,
+                         const double* F, const hexa_solve_params* p, double* U, hexa_solve_stats* stats) {
+  if (!h) return HEXA_ERR_ARG;
+  if (!valid_grid(g) || !factor || !F || !U || k < 1) return set_err(h, HEXA_ERR_ARG, "invalid arguments");
+  if (!valid_params(p)) return set_err(h, HEXA_ERR_ARG, "invalid solver parameters");
+  // Column-by-column until the block kernels land: each column is a full solve.
+  const long long ndof = 3LL * (g->nx + 1) * (g->ny + 1) * (g->nz + 1);
+  hexa_solve_stats acc;
+  std::memset(&acc, 0, sizeof(acc));
+  int worst = HEXA_OK;
+  for (int j = 0; j < k; ++j) {
+    hexa_solve_stats st;
+    int rc = hexa_solve(h, g, bc, factor, F + j * ndof, p, nullptr, U + j * ndof, &st);
+    if (rc < 0) return rc;
+    if (rc > worst) worst = rc;
+    acc.iterations += st.iterations;
+    acc.solve_ms += st.solve_ms;
+    acc.setup_ms += st.setup_ms;
+    acc.total_ms += st.total_ms;
+    acc.compliance += st.compliance / k;
+    acc.true_relres = std::fmax(acc.true_relres, st.true_relres);
+    acc.relres = std::fmax(acc.relres, st.relres);
+    acc.fine_applies += st.fine_applies;
+    acc.precond_used = st.precond_used;
+    acc.mg_levels = st.mg_levels;
+  }
+  acc.status = worst;
+  if (stats) *stats = acc;
+  return worst;
+}
+
+}  // extern "C"
+
+template <typename T>
+static int filter_t(hexa_ctx* h, const Grid& G, const double* rho_d, const HelmK& K, double tol, int max_iter,
+                    double* out_d, hexa_filter_stats* st) {
+  Ctx& c = h->c;
+  const long long nn = G.nnode(), ne = G.nelem();
+  const char* tg = sizeof(T) == 8 ? "h64_" : "h32_";
+  auto nm = [&](const char* s) { return std::string(tg) + s; };
+  T* rho = c.vec<T>(nm("rho"), ne);
+  T* b = c.vec<T>(nm("b"), nn);
+  T* x = c.vec<T>(nm("x"), nn);
+  T* r = c.vec<T>(nm("r"), nn);
+  T* z = c.vec<T>(nm("z"), nn);
+  T* p = c.vec<T>(nm("p"), nn);
+  T* q = c.vec<T>(nm("q"), nn);
+  T* dinv = c.vec<T>(nm("dinv"), nn);
+  T* outT = c.vec<T>(nm("out"), ne);
+  if (!rho || !b || !x || !r || !z || !p || !q || !dinv || !outT) return HEXA_ERR_NOMEM;
+  if constexpr (sizeof(T) == 8) cudaMemcpyAsync(rho, rho_d, ne * sizeof(double), cudaMemcpyDeviceToDevice, c.st);
+  else launch_convert<float, double>(rho, rho_d, ne, c.st);
+  launch_helm_rhs<T>(G, rho, (T)K.rhs_scale, b, c.st);
+  launch_helm_dinv<T>(G, K, dinv, c.st);
+  c.launches += 3;
+  RedArgs rd;
+  rd.partials = c.partials;
+  rd.ticket = c.ticket;
+  rd.s = c.s;
+  rd.dst = c.dscal + 20;
+  rd.op = FIN_STORE;
+  rd.nsum = 1;
+  launch_dot<T>(b, b, (const T*)nullptr, (const T*)nullptr, nn, rd, kRed, nullptr, c.st);
+  c.launches++;
+  cudaMemcpyAsync(c.hscal + 20, c.dscal + 20, sizeof(double), cudaMemcpyDeviceToHost, c.st);
+  cudaStreamSynchronize(c.st);
+  const double bnorm = std::sqrt(c.hscal[20]);
+  if (bnorm == 0.0) {  // GPUHelmholtz.jl:203-206 returns the input unchanged
+    cudaMemcpyAsync(out_d, rho_d, ne * sizeof(double), cudaMemcpyDeviceToDevice, c.st);
+    st->iterations = 0;
+    st->relres = 0.0;
+    return HEXA_OK;
+  }
+  PcgScalars hs;
+  std::memset(&hs, 0, sizeof(hs));
+  hs.tol = tol;
+  hs.max_iter = max_iter;
+  hs.cadence = -10;
+  hs.no_div = 1;
+  hs.bnorm = bnorm;
+  hs.best_rel = INFINITY;
+  *c.hs = hs;
+  cudaMemcpyAsync(c.s, c.hs, sizeof(PcgScalars), cudaMemcpyHostToDevice, c.st);
+  launch_fill<T>(x, T(0), nn, c.st);
+  launch_copy<T>(r, b, nn, c.st);
+  c.launches += 2;
+  rd.s = c.s;
+  rd.op = FIN_INIT_RZ;
+  launch_jacobi_precond<T>(z, r, dinv, nn, rd, kRed, nullptr, c.st);
+  launch_copy<T>(p, z, nn, c.st);
+  c.launches += 2;
+  cudaEventRecord(c.ev[0], c.st);
+  const int* halt = &c.s->halt;
+  const int hblocks = (int)std::min<long long>((nn + 255) / 256, 152 * 8);
+  while (true) {
+    for (int it = 0; it < 10; ++it) {
+      RedArgs ra = rd;
+      ra.op = FIN_PCG_ALPHA;
+      launch_helm_apply_dot<T>(G, K, p, q, ra, hblocks, halt, c.st);
+      RedArgs rb = rd;
+      rb.op = FIN_PCG_RES;
+      rb.nsum = 2;
+      launch_pcg_update<T>(x, r, z, p, q, dinv, nn, rb, kRed, c.s, c.st);
+      launch_p_update<T>(p, z, nn, c.s, c.st);
+      c.launches += 3;
+    }
+    cudaMemcpyAsync(c.hs, c.s, sizeof(PcgScalars), cudaMemcpyDeviceToHost, c.st);
+    if (cudaStreamSynchronize(c.st) != cudaSuccess) return HEXA_ERR_CUDA;
+    if (c.hs->halt) break;
+  }
+  launch_helm_extract<T>(G, x, outT, c.st);
+  c.launches++;
+  if constexpr (sizeof(T) == 8) cudaMemcpyAsync(out_d, outT, ne * sizeof(double), cudaMemcpyDeviceToDevice, c.st);
+  else {
+    launch_convert<double, float>(out_d, outT, ne, c.st);
+    c.launches++;
+  }
+  cudaEventRecord(c.ev[1], c.st);
+  cudaEventSynchronize(c.ev[1]);
+  float ms = 0;
+  cudaEventElapsedTime(&ms, c.ev[0], c.ev[1]);
+  st->solve_ms = ms;
+  st->iterations = c.hs->iter;
+  st->relres = c.hs->relres;
+  return HEXA_OK;
+}
+
+
+extern "C" {
+
+int hexa_filter(hexa_ctx* h, const hexa_grid* g, const double* rho_in, double radius, double tol, int32_t max_iter,
+                int32_t quirk, int32_t precision, double* rho_out, hexa_filter_stats* stats) {
+  if (!h) return HEXA_ERR_ARG;
+  if (!valid_grid(g) || !rho_in || !rho_out || !(radius >= 0) || !(tol > 0) || max_iter < 1)
+    return set_err(h, HEXA_ERR_ARG, "invalid filter arguments");
+  Ctx& c = h->c;
+  c.err.clear();
+  cudaSetDevice(c.device);
+  const Grid G = make_grid(g->nx, g->ny, g->nz);
+  double Ke[64], Me[64];
+  if (scalar_matrices(g->dx, g->dy, g->dz, quirk, Ke, Me) != 0) return set_err(h, HEXA_ERR_ARG, "invalid element size");
+  HelmK K;
+  helm_corner_matrix(Ke, Me, radius, K.A);
+  K.rhs_scale = g->dx * g->dy * g->dz / 8.0;  // GPUHelmholtz.jl:198-199
+  const double* rd = stage_in<double>(c, rho_in, G.nelem(), "f_in");
+  double* od = out_buf<double>(c, rho_out, G.nelem(), "f_out");
+  if (!rd || !od) return HEXA_ERR_NOMEM;
+  hexa_filter_stats st;
+  std::memset(&st, 0, sizeof(st));
+  const int rc = (precision == HEXA_PREC_FP32) ? filter_t<float>(h, G, rd, K, tol, max_iter, od, &st)
+                                               : filter_t<double>(h, G, rd, K, tol, max_iter, od, &st);
+  stage_out<double>(c, rho_out, od, G.nelem());
+  if (cudaStreamSynchronize(c.st) != cudaSuccess || !c.cuda_ok("filter")) return set_err(h, HEXA_ERR_CUDA, c.err);
+  st.status = rc;
+  c.last_ms = st.solve_ms;
+  if (stats) *stats = st;
+  return rc;
+}
+
+int hexa_simp_factors(hexa_ctx* h, int64_t n, const double* rho, double Emin, double E0, double penal,
+                      double* factor_out) {
+  if (!h) return HEXA_ERR_ARG;
+  if (n < 1 || !rho || !factor_out) return set_err(h, HEXA_ERR_ARG, "invalid arguments");
+  Ctx& c = h->c;
+  c.err.clear();
+  cudaSetDevice(c.device);
+  const double* rd = stage_in<double>(c, rho, n, "s_rho");
+  double* fd = out_buf<double>(c, factor_out, n, "s_fac");
+  if (!rd || !fd) return HEXA_ERR_NOMEM;
+  launch_simp_factors(rd, Emin, E0, penal, fd, n, c.st);
+  c.launches++;
+  stage_out<double>(c, factor_out, fd, n);
+  if (cudaStreamSynchronize(c.st) != cudaSuccess || !c.cuda_ok("simp")) return set_err(h, HEXA_ERR_CUDA, c.err);
+  return HEXA_OK;
+}
+
+int hexa_sensitivities(hexa_ctx* h, const hexa_grid* g, double nu, const double* rho, const double* u, double Emin,
+                       double E0, double penal, double* dc_out, double* compliance_out) {
+  if (!h) return HEXA_ERR_ARG;
+  if (!valid_grid(g) || !rho || !u || !dc_out) return set_err(h, HEXA_ERR_ARG, "invalid arguments");
+  Ctx& c = h->c;
+  c.err.clear();
+  cudaSetDevice(c.device);
+  ModalK<double> K64;
+  std::string e;
+  if (!build_modal(g->dx, g->dy, g->dz, nu, &K64, &e)) return set_err(h, HEXA_ERR_ARG, e);
+  const Grid G = make_grid(g->nx, g->ny, g->nz);
+  const double* rd = stage_in<double>(c, rho, G.nelem(), "s_rho");
+  const double* ud = stage_in<double>(c, u, G.ndof(), "s_u");
+  double* dd = out_buf<double>(c, dc_out, G.nelem(), "s_dc");
+  if (!rd || !ud || !dd) return HEXA_ERR_NOMEM;
+  RedArgs r;
+  r.partials = c.partials;
+  r.ticket = c.ticket;
+  r.dst = c.dscal + 30;
+  r.s = nullptr;
+  r.op = FIN_STORE;
+  r.nsum = 1;
+  cudaEventRecord(c.ev[0], c.st);
+  launch_sensitivities(G, K64, rd, ud, Emin, E0, penal, dd, r, c.st);
+  cudaEventRecord(c.ev[1], c.st);
+  c.launches++;
+  cudaMemcpyAsync(c.hscal + 30, c.dscal + 30, sizeof(double), cudaMemcpyDeviceToHost, c.st);
+  stage_out<double>(c, dc_out, dd, G.nelem());
+  if (cudaStreamSynchronize(c.st) != cudaSuccess || !c.cuda_ok("sensitivities")) return set_err(h, HEXA_ERR_CUDA, c.err);
+  float ms = 0;
+  cudaEventElapsedTime(&ms, c.ev[0], c.ev[1]);
+  c.last_ms = ms;
+  if (compliance_out) *compliance_out = c.hscal[30];
+  return HEXA_OK;
+}
+
+int hexa_oc_update(hexa_ctx* h, int64_t n, const double* x, const double* dc, const double* dv, double volfrac,
+                   double move, double* x_out, double* lambda_out) {
+  if (!h) return HEXA_ERR_ARG;
+  if (n < 1 || !x || !dc || !dv || !x_out || !(volfrac > 0 && volfrac < 1) || !(move > 0))
+    return set_err(h, HEXA_ERR_ARG, "invalid arguments");
+  Ctx& c = h->c;
+  c.err.clear();
+  cudaSetDevice(c.device);
+  const double* xd = stage_in<double>(c, x, n, "o_x");
+  const double* cd = stage_in<double>(c, dc, n, "o_dc");
+  const double* vd = stage_in<double>(c, dv, n, "o_dv");
+  double* od = out_buf<double>(c, x_out, n, "o_out");
+  double* lam_d = c.vec<double>("o_lam", 32);
+  const int nb = (int)std::min<long long>((n + 255) / 256, 152 * 4);
+  if (!xd || !cd || !vd || !od || !lam_d || !c.ensure_partials((size_t)nb * 32 + 64)) return HEXA_ERR_NOMEM;
+  std::vector<double> part((size_t)nb * 32);
+  // Bisection of the 88-line code on lambda in [0, 1e9] until
+  // (l2-l1)/(l1+l2) <= 1e-3 is replaced by the same sequence of midpoints to a
+  // tighter 1e-12, evaluated five levels of the bisection tree (31 multipliers)
+  // per pass over the elements.
+  double l1 = 0.0, l2 = 1e9, last_mid = 0.5 * (l1 + l2);
+  const double target = volfrac * (double)n;
+  int passes = 0;
+  cudaEventRecord(c.ev[0], c.st);
+  while ((l2 - l1) / (l1 + l2) > 1e-12 && passes < 64) {
+    double lams[31];
+    // heap order: node t has children 2t+1, 2t+2 (left = [l1,mid], right = [mid,l2])
+    double lo[31], hi[31];
+    lo[0] = l1;
+    hi[0] = l2;
+    for (int t = 0; t < 31; ++t) {
+      lams[t] = 0.5 * (hi[t] + lo[t]);
+      if (2 * t + 2 < 31) {
+        lo[2 * t + 1] = lo[t];
+        hi[2 * t + 1] = lams[t];
+        lo[2 * t + 2] = lams[t];
+        hi[2 * t + 2] = hi[t];
+      }
+    }
+    cudaMemcpyAsync(lam_d, lams, sizeof(lams), cudaMemcpyHostToDevice, c.st);
+    launch_oc_volumes(xd, cd, vd, n, lam_d, 31, move, c.partials, nb, c.st);
+    c.launches++;
+    cudaMemcpyAsync(part.data(), c.partials, (size_t)nb * 32 * sizeof(double), cudaMemcpyDeviceToHost, c.st);
+    if (cudaStreamSynchronize(c.st) != cudaSuccess) return set_err(h, HEXA_ERR_CUDA, "oc pass failed");
+    ++passes;
+    int t = 0;
+    for (int depth = 0; depth < 5; ++depth) {
+      if (!((l2 - l1) / (l1 + l2) > 1e-12)) break;
+      double vol = 0.0;
+      for (int b = 0; b < nb; ++b) vol += part[(size_t)b * 32 + t];
+      const double lmid = lams[t];
+      last_mid = lmid;
+      if (vol > target) {
+        l1 = lmid;
+        t = 2 * t + 2;
+      } else {
+        l2 = lmid;
+        t = 2 * t + 1;
+      }
+    }
+  }
+  // the update is the one of the last midpoint tested, as in the 88-line loop
+  const double lam = last_mid;
+  launch_oc_apply(xd, cd, vd, n, lam, move, od, c.st);
+  cudaEventRecord(c.ev[1], c.st);
+  c.launches++;
+  stage_out<double>(c, x_out, od, n);
+  if (cudaStreamSynchronize(c.st) != cudaSuccess || !c.cuda_ok("oc")) return set_err(h, HEXA_ERR_CUDA, c.err);
+  float ms = 0;
+  cudaEventElapsedTime(&ms, c.ev[0], c.ev[1]);
+  c.last_ms = ms;
+  if (lambda_out) *lambda_out = lam;
+  return HEXA_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,152 @@
+// (d) Helmholtz PDE density filter on the structured grid.
+//
+// Replaces GPUHelmholtz.jl's path (src/Optimization/GPUHelmholtz.jl:59-266):
+// the RHS scatter with atomics (:59-70) becomes a gather over the <= 8
+// elements of each node; the 8 colour-batched element launches per matvec
+// (:73-97, 155-172, 230-238) with a host-built sortperm colouring become one
+// node-centric launch of the constant-coefficient element matrix
+// Ae = R^2 Ke + Me (natural boundary: only elements inside the box count);
+// the diagonal (:112-123) is analytic; the Jacobi-PCG loop (:208-260) keeps
+// the reference's arithmetic but its dots and the every-10 convergence test run
+// on the device; the element average (:99-110) is one gather pass.
+#include "hexa_common.cuh"
+#include "hexa_kernels.h"
+
+namespace hexa {
+
+static inline int helm_blocks(long long n) {
+  long long b = (n + 255) / 256;
+  if (b < 1) b = 1;
+  if (b > 152 * 8) b = 152 * 8;
+  return (int)b;
+}
+
+template <typename T>
+__global__ void helm_rhs_kernel(Grid g, const T* __restrict__ rho, T scale, T* __restrict__ b) {
+  const long long nn = g.nnode();
+  for (long long n = blockIdx.x * (long long)blockDim.x + threadIdx.x; n < nn; n += (long long)gridDim.x * blockDim.x) {
+    const int i = (int)(n % g.NX);
+    const long long t = n / g.NX;
+    const int j = (int)(t % g.NY), k = (int)(t / g.NY);
+    T s = T(0);
+    for (int dz = -1; dz <= 0; ++dz)
+      for (int dy = -1; dy <= 0; ++dy)
+        for (int dx = -1; dx <= 0; ++dx) {
+          const int ei = i + dx, ej = j + dy, ek = k + dz;
+          if (ei >= 0 && ei < g.nx && ej >= 0 && ej < g.ny && ek >= 0 && ek < g.nz)
+            s += rho[(long long)ei + (long long)g.nx * ((long long)ej + (long long)g.ny * ek)] * scale;
+        }
+    b[n] = s;
+  }
+}
+template <typename T>
+void launch_helm_rhs(const Grid& g, const T* rho, T scale, T* b, cudaStream_t st) {
+  helm_rhs_kernel<T><<<helm_blocks(g.nnode()), 256, 0, st>>>(g, rho, scale, b);
+}
+
+template <typename T>
+struct HelmKT {
+  T A[8][8];
+};
+
+template <typename T>
+__global__ void helm_apply_kernel(Grid g, HelmKT<T> K, const T* __restrict__ x, T* __restrict__ y, RedArgs red,
+                                  const int* halt) {
+  if (halt && *((volatile const int*)halt)) return;
+  double acc[1] = {0.0};
+  const long long nn = g.nnode();
+  for (long long n = blockIdx.x * (long long)blockDim.x + threadIdx.x; n < nn; n += (long long)gridDim.x * blockDim.x) {
+    const int i = (int)(n % g.NX);
+    const long long t = n / g.NX;
+    const int j = (int)(t % g.NY), k = (int)(t / g.NY);
+    T s = T(0);
+#pragma unroll
+    for (int oz = 0; oz < 2; ++oz)
+#pragma unroll
+      for (int oy = 0; oy < 2; ++oy)
+#pragma unroll
+        for (int ox = 0; ox < 2; ++ox) {
+          // element with min corner (i-1+ox, j-1+oy, k-1+oz); node n is its corner (1-ox,1-oy,1-oz)
+          const int ei = i - 1 + ox, ej = j - 1 + oy, ek = k - 1 + oz;
+          if (ei < 0 || ei >= g.nx || ej < 0 || ej >= g.ny || ek < 0 || ek >= g.nz) continue;
+          const int ln = (1 - ox) + 2 * (1 - oy) + 4 * (1 - oz);
+#pragma unroll
+          for (int cc = 0; cc < 8; ++cc) {
+            const long long m = (long long)(ei + (cc & 1)) +
+                                (long long)g.NX * ((long long)(ej + ((cc >> 1) & 1)) + (long long)g.NY * (ek + (cc >> 2)));
+            s = fma(K.A[ln][cc], __ldg(x + m), s);
+          }
+        }
+    y[n] = s;
+    acc[0] += (double)x[n] * (double)s;
+  }
+  block_reduce_finalize<1>(red, acc);
+}
+template <typename T>
+void launch_helm_apply_dot(const Grid& g, const HelmK& K, const T* x, T* y, const RedArgs& red, int nblocks,
+                           const int* halt, cudaStream_t st) {
+  HelmKT<T> k;
+  for (int a = 0; a < 8; ++a)
+    for (int b = 0; b < 8; ++b) k.A[a][b] = (T)K.A[a][b];
+  helm_apply_kernel<T><<<nblocks, 256, 0, st>>>(g, k, x, y, red, halt);
+}
+
+template <typename T>
+__global__ void helm_dinv_kernel(Grid g, HelmKT<T> K, T* __restrict__ dinv) {
+  const long long nn = g.nnode();
+  for (long long n = blockIdx.x * (long long)blockDim.x + threadIdx.x; n < nn; n += (long long)gridDim.x * blockDim.x) {
+    const int i = (int)(n % g.NX);
+    const long long t = n / g.NX;
+    const int j = (int)(t % g.NY), k = (int)(t / g.NY);
+    T d = T(0);
+    for (int oz = 0; oz < 2; ++oz)
+      for (int oy = 0; oy < 2; ++oy)
+        for (int ox = 0; ox < 2; ++ox) {
+          const int ei = i - 1 + ox, ej = j - 1 + oy, ek = k - 1 + oz;
+          if (ei < 0 || ei >= g.nx || ej < 0 || ej >= g.ny || ek < 0 || ek >= g.nz) continue;
+          const int ln = (1 - ox) + 2 * (1 - oy) + 4 * (1 - oz);
+          d += K.A[ln][ln];
+        }
+    dinv[n] = T(1) / d;  // GPUHelmholtz.jl:153 inv_diag = 1 ./ diag
+  }
+}
+template <typename T>
+void launch_helm_dinv(const Grid& g, const HelmK& K, T* dinv, cudaStream_t st) {
+  HelmKT<T> k;
+  for (int a = 0; a < 8; ++a)
+    for (int b = 0; b < 8; ++b) k.A[a][b] = (T)K.A[a][b];
+  helm_dinv_kernel<T><<<helm_blocks(g.nnode()), 256, 0, st>>>(g, k, dinv);
+}
+
+template <typename T>
+__global__ void helm_extract_kernel(Grid g, const T* __restrict__ psi, T* __restrict__ out) {
+  const long long ne = g.nelem();
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < ne; e += (long long)gridDim.x * blockDim.x) {
+    const int i = (int)(e % g.nx);
+    const long long t = e / g.nx;
+    const int j = (int)(t % g.ny), k = (int)(t / g.ny);
+    T s = T(0);
+    // node order n1..n8 of Mesh.jl:45-53, summed in that order as GPUHelmholtz.jl:104-106
+    const int oi[8] = {0, 1, 1, 0, 0, 1, 1, 0}, oj[8] = {0, 0, 1, 1, 0, 0, 1, 1}, ok[8] = {0, 0, 0, 0, 1, 1, 1, 1};
+#pragma unroll
+    for (int q = 0; q < 8; ++q)
+      s += psi[(long long)(i + oi[q]) + (long long)g.NX * ((long long)(j + oj[q]) + (long long)g.NY * (k + ok[q]))];
+    out[e] = s / T(8);
+  }
+}
+template <typename T>
+void launch_helm_extract(const Grid& g, const T* psi, T* rho_out, cudaStream_t st) {
+  helm_extract_kernel<T><<<helm_blocks(g.nelem()), 256, 0, st>>>(g, psi, rho_out);
+}
+
+#define INST(T)                                                                                              \
+  template void launch_helm_rhs<T>(const Grid&, const T*, T, T*, cudaStream_t);                              \
+  template void launch_helm_apply_dot<T>(const Grid&, const HelmK&, const T*, T*, const RedArgs&, int,       \
+                                         const int*, cudaStream_t);                                          \
+  template void launch_helm_dinv<T>(const Grid&, const HelmK&, T*, cudaStream_t);                            \
+  template void launch_helm_extract<T>(const Grid&, const T*, T*, cudaStream_t);
+INST(double)
+INST(float)
+#undef INST
+
+}  // namespace hexa

@@ -1,0 +1,127 @@
+// Launch-side declarations of every kernel of the hex8 solve path.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "hexa_common.cuh"
+
+namespace hexa {
+
+// ---------------------------------------------------------------- operator
+enum OpMode { OP_APPLY = 0, OP_APPLY_DOT = 1, OP_RESID = 2, OP_RESID_NORM = 3, OP_JACOBI = 4 };
+
+template <typename T>
+struct OpArgs {
+  Grid g;
+  Mask m;
+  const T* x;     // stencil input, zero at fixed DOFs
+  const T* fac;   // element factors (nelem)
+  const T* b;     // right-hand side (RESID*, JACOBI)
+  T* y;           // output (must not alias x)
+  ModalK<T> K;
+  T sigma;        // diagonal shift
+  T omega;        // Jacobi damping
+  int kchunk;     // node layers per CTA
+  int diag_quirk;
+  RedArgs red;
+  const int* halt;  // nullable: PcgScalars::halt
+};
+
+template <typename T>
+void launch_op(int mode, const OpArgs<T>& a, cudaStream_t st);
+template <typename T>
+long long op_num_blocks(const Grid& g, int kchunk);
+ModalK<float> modal_to_f32(const ModalK<double>& K);
+
+// ------------------------------------------------------------ vector passes
+// All vectors are full-length AoS (3*nNodes) and zero at fixed DOFs.
+template <typename T>
+void launch_fill(T* v, T val, long long n, cudaStream_t st);
+void launch_fill_u32(unsigned* v, unsigned val, long long n, cudaStream_t st);
+template <typename T>
+void launch_copy(T* dst, const T* src, long long n, cudaStream_t st);
+// dst = src with fixed DOFs zeroed (expand/contract semantics)
+template <typename TD, typename TS>
+void launch_mask_copy(const Grid& g, const Mask& m, TD* dst, const TS* src, cudaStream_t st);
+// Jacobi inverse diagonal dinv = 1/(dd*fsum + sigma) (0 at fixed DOFs) and
+// the raw diagonal (dd*fsum, 0 at fixed DOFs).
+template <typename T>
+void launch_diag(const Grid& g, const Mask& m, const T* fac, const ModalK<T>& K, int quirk, T sigma,
+                 T* diag, T* dinv, cudaStream_t st);
+// max over the vector (non-negative entries), result into *dst (device)
+void launch_max(const double* v, long long n, const RedArgs& red, int nblocks, cudaStream_t st);
+// sums: dst = [a.b]  or [a.b, c.d]
+template <typename T>
+void launch_dot(const T* a, const T* b, const T* c, const T* d, long long n, const RedArgs& red,
+                int nblocks, const int* halt, cudaStream_t st);
+// PCG update: x += alpha p; r -= alpha q; rr = r.r ; with dinv: z = dinv*r, rz = r.z
+template <typename T>
+void launch_pcg_update(T* x, T* r, T* z, const T* p, const T* q, const T* dinv, long long n,
+                       const RedArgs& red, int nblocks, const PcgScalars* s, cudaStream_t st);
+// p = z + beta p
+template <typename T>
+void launch_p_update(T* p, const T* z, long long n, const PcgScalars* s, cudaStream_t st);
+// z = dinv * r (Jacobi) ; rz = r.z
+template <typename T>
+void launch_jacobi_precond(T* z, const T* r, const T* dinv, long long n, const RedArgs& red,
+                           int nblocks, const int* halt, cudaStream_t st);
+// dst32 = (T32)(src64 * scale)
+void launch_scale_to_f32(float* dst, const double* src, const double* scale, long long n,
+                         cudaStream_t st);
+// u64 += (double)d32 / scale
+void launch_add_scaled_f32(double* u, const float* d, const double* scale, long long n,
+                           cudaStream_t st);
+// x = a*x + b*y with host scalars
+template <typename T>
+void launch_axpby(T* x, T a, const T* y, T b, long long n, cudaStream_t st);
+
+// ---------------------------------------------------------------- multigrid
+// coarse factor = 2 * mean of the 8 children (rediscretised K0 at 2h = 2*K0(h))
+template <typename T>
+void launch_coarsen_factors(const Grid& gf, const T* ff, const Grid& gc, T* fc, cudaStream_t st);
+template <typename TD, typename TS>
+void launch_convert(TD* dst, const TS* src, long long n, cudaStream_t st);
+// coarse node mask by injection
+void launch_coarsen_mask(const Grid& gf, const uint8_t* mf, const Grid& gc, uint8_t* mc,
+                         cudaStream_t st);
+// b_c = P^T r_f (full weighting, 27 fine nodes per coarse node)
+template <typename T>
+void launch_restrict(const Grid& gf, const T* rf, const Grid& gc, const Mask& mc, T* bc,
+                     const int* halt, cudaStream_t st);
+// x_f += P x_c (trilinear)
+template <typename T>
+void launch_prolong_add(const Grid& gc, const T* xc, const Grid& gf, const Mask& mf, T* xf,
+                        const int* halt, cudaStream_t st);
+// x = omega * b / D (first damped-Jacobi sweep from a zero guess)
+template <typename T>
+void launch_jacobi0(const Grid& g, const Mask& m, const T* fac, const ModalK<T>& K, int quirk,
+                    T sigma, T omega, const T* b, T* x, const int* halt, cudaStream_t st);
+
+// --------------------------------------------------------------- Helmholtz
+struct HelmK {
+  double A[8][8];  // R^2 Ke + Me, corner order dx + 2dy + 4dz
+  double rhs_scale; // vol/8
+};
+template <typename T>
+void launch_helm_rhs(const Grid& g, const T* rho, T scale, T* b, cudaStream_t st);
+template <typename T>
+void launch_helm_apply_dot(const Grid& g, const HelmK& K, const T* x, T* y, const RedArgs& red,
+                           int nblocks, const int* halt, cudaStream_t st);
+template <typename T>
+void launch_helm_dinv(const Grid& g, const HelmK& K, T* dinv, cudaStream_t st);
+template <typename T>
+void launch_helm_extract(const Grid& g, const T* psi, T* rho_out, cudaStream_t st);
+
+// ------------------------------------------------------------------ SIMP/OC
+void launch_simp_factors(const double* rho, double Emin, double E0, double penal, double* fac,
+                         long long n, cudaStream_t st);
+void launch_sensitivities(const Grid& g, const ModalK<double>& K, const double* rho,
+                          const double* u, double Emin, double E0, double penal, double* dc,
+                          const RedArgs& red, cudaStream_t st);
+void launch_oc_volumes(const double* x, const double* dc, const double* dv, long long n,
+                       const double* lam, int nlam, double move, double* partials, int nblocks,
+                       cudaStream_t st);
+void launch_oc_apply(const double* x, const double* dc, const double* dv, long long n, double lam,
+                     double move, double* xout, cudaStream_t st);
+
+}  // namespace hexa

@@ -1,0 +1,870 @@
+// Host orchestration of the solve path: workspace cache, the PCG driver with
+// device-resident scalars (optionally replayed from CUDA graphs), the
+// geometric-multigrid V-cycle, the reference's shift/fallback control flow
+// and the mixed-precision refinement loop.
+//
+// Control flow restated from src/Solvers/GPUSolver.jl:182-465:
+//   - sigma = shift_factor * max(diag K_ff)                        (:343)
+//   - up to max_shift_attempts attempts, shift *= shift_multiplier  (:342-432)
+//   - first attempt starts from u_guess, later ones from zero       (:347-351)
+//   - NaN or divergence (rel > 10, or k > 500 and rel > 100 best) under
+//     multigrid restarts with Jacobi                                (:387-401,434-437)
+//   - stagnation acceptance of the best iterate when best < stagnation_tol
+//                                                                   (:426-430)
+//   - otherwise the best iterate is returned as not converged       (:439-443)
+// New here: the FP64 true residual ||f-(K+sI)u||/||f|| is recomputed after
+// convergence and the iteration continues until it meets the tolerance.
+#include <cuda_runtime.h>
+
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "element.h"
+#include "hexa_kernels.h"
+#include "solver.h"
+
+namespace hexa {
+
+void launch_scalars_init(PcgScalars* s, const PcgScalars* parent, int max_iter, cudaStream_t st);
+
+// ------------------------------------------------------------------ context
+void* Ctx::get(const std::string& name, size_t bytes) {
+  if (bytes == 0) bytes = 16;
+  auto it = bufs.find(name);
+  if (it != bufs.end() && it->second.second >= bytes) return it->second.first;
+  if (it != bufs.end()) {
+    cudaFreeAsync(it->second.first, st);
+    bufs.erase(it);
+  }
+  void* p = nullptr;
+  if (cudaMallocAsync(&p, bytes, st) != cudaSuccess) {
+    cudaGetLastError();
+    err = "device allocation of " + std::to_string(bytes) + " bytes failed (" + name + ")";
+    return nullptr;
+  }
+  bufs[name] = {p, bytes};
+  return p;
+}
+
+bool Ctx::ensure_partials(size_t n) {
+  if (n <= partials_cap) return true;
+  void* p = get("partials", n * sizeof(double));
+  if (!p) return false;
+  partials = (double*)p;
+  partials_cap = n;
+  return true;
+}
+
+bool Ctx::cuda_ok(const char* where) {
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess) return true;
+  err = std::string(where) + ": " + cudaGetErrorString(e);
+  return false;
+}
+
+bool is_device_ptr(const void* p) {
+  if (!p) return false;
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+}
+
+bool build_modal(double dx, double dy, double dz, double nu, ModalK<double>* K, std::string* err) {
+  double ke[576];
+  if (canonical_stiffness(dx, dy, dz, nu, ke) != 0) {
+    if (err) *err = "invalid element geometry or Poisson ratio";
+    return false;
+  }
+  double dropped = 0.0;
+  if (modal_blocks(ke, K, &dropped) != 0) {
+    if (err) *err = "K0 is not block diagonal in the Hadamard basis";
+    return false;
+  }
+  return true;
+}
+
+// --------------------------------------------------------------- utilities
+namespace {
+
+constexpr int kRedBlocks = 152 * 4;  // grid of reducing vector passes
+
+template <typename T>
+struct Is64 { static constexpr bool v = sizeof(T) == 8; };
+
+template <typename T>
+int pick_kchunk(const Grid& g) {
+  const int tyw = Is64<T>::v ? 8 : 16;
+  const long long bxy = (long long)((g.NX + 30) / 31) * ((g.NY + tyw - 2) / (tyw - 1));
+  const long long target = Is64<T>::v ? 152LL * 3 : 152LL * 2;
+  long long nchunks = (target + bxy - 1) / bxy;
+  if (nchunks < 1) nchunks = 1;
+  if (nchunks > g.NZ) nchunks = g.NZ;
+  int kc = (int)((g.NZ + nchunks - 1) / nchunks);
+  if (kc < 2) kc = 2;
+  return kc;
+}
+
+RedArgs red(Ctx& c, int op, int nsum, PcgScalars* s, double* dst = nullptr) {
+  RedArgs r;
+  r.partials = c.partials;
+  r.ticket = c.ticket;
+  r.dst = dst;
+  r.s = s;
+  r.op = op;
+  r.nsum = nsum;
+  return r;
+}
+
+template <typename T>
+struct Lev {
+  Grid g;
+  Mask m;
+  T* fac = nullptr;
+  T* xa = nullptr;  // level solution (coarse levels)
+  T* xb = nullptr;  // smoother ping-pong
+  T* b = nullptr;   // level right-hand side (coarse levels)
+  T* r = nullptr;   // level residual
+  T* dinv = nullptr, *p = nullptr, *q = nullptr, *z = nullptr;  // coarsest-level PCG
+  T sigma = 0;
+  int kchunk = 4;
+};
+
+template <typename T>
+struct MG {
+  std::vector<Lev<T>> L;
+  ModalK<T> K;
+  int quirk = 0;
+  T omega = T(0.6);
+  int nu1 = 2, nu2 = 2, citers = 30;
+};
+
+template <typename T>
+OpArgs<T> opargs(const Lev<T>& L, const ModalK<T>& K, int quirk, const T* x, const T* b, T* y, T omega,
+                 const int* halt, RedArgs r) {
+  OpArgs<T> a;
+  a.g = L.g;
+  a.m = L.m;
+  a.x = x;
+  a.fac = L.fac;
+  a.b = b;
+  a.y = y;
+  a.K = K;
+  a.sigma = L.sigma;
+  a.omega = omega;
+  a.kchunk = L.kchunk;
+  a.diag_quirk = quirk;
+  a.red = r;
+  a.halt = halt;
+  return a;
+}
+
+template <typename T>
+void op(Ctx& c, int mode, const OpArgs<T>& a) {
+  launch_op<T>(mode, a, c.st);
+  c.launches++;
+}
+
+// Number of levels: requested, or automatic (halve while every axis is even
+// and the coarse grid keeps at least 2 elements per axis, down to ~2k nodes).
+int plan_levels(const Grid& g, int requested) {
+  int nx = g.nx, ny = g.ny, nz = g.nz, lv = 1;
+  const int maxlv = requested > 0 ? requested : 16;
+  while (lv < maxlv) {
+    if ((nx & 1) || (ny & 1) || (nz & 1) || nx < 4 || ny < 4 || nz < 4) break;
+    if (requested <= 0 && (long long)(nx + 1) * (ny + 1) * (nz + 1) <= 2500) break;
+    nx >>= 1; ny >>= 1; nz >>= 1;
+    ++lv;
+  }
+  return lv;
+}
+
+template <typename T>
+bool build_mg(Ctx& c, MG<T>& mg, const Grid& g0, const Mask& m0, const T* fac0, int nlev, const std::string& tag) {
+  mg.L.clear();
+  Lev<T> L0;
+  L0.g = g0;
+  L0.m = m0;
+  L0.fac = const_cast<T*>(fac0);
+  L0.kchunk = pick_kchunk<T>(g0);
+  const long long n0 = g0.ndof();
+  L0.xb = c.vec<T>(tag + "xb0", n0);
+  L0.r = c.vec<T>(tag + "r0", n0);
+  if (!L0.xb || !L0.r) return false;
+  mg.L.push_back(L0);
+  for (int l = 1; l < nlev; ++l) {
+    const Lev<T>& F = mg.L[l - 1];
+    Lev<T> C;
+    C.g = make_grid(F.g.nx / 2, F.g.ny / 2, F.g.nz / 2);
+    C.m.faces = F.m.faces;
+    C.m.node = nullptr;
+    const std::string s = tag + std::to_string(l);
+    if (F.m.node) {
+      uint8_t* mk = c.vec<uint8_t>(s + "mask", C.g.nnode());
+      if (!mk) return false;
+      launch_coarsen_mask(F.g, F.m.node, C.g, mk, c.st);
+      c.launches++;
+      C.m.node = mk;
+    }
+    C.fac = c.vec<T>(s + "fac", C.g.nelem());
+    const long long n = C.g.ndof();
+    C.xa = c.vec<T>(s + "xa", n);
+    C.xb = c.vec<T>(s + "xb", n);
+    C.b = c.vec<T>(s + "b", n);
+    C.r = c.vec<T>(s + "r", n);
+    if (!C.fac || !C.xa || !C.xb || !C.b || !C.r) return false;
+    launch_coarsen_factors<T>(F.g, F.fac, C.g, C.fac, c.st);
+    c.launches++;
+    C.kchunk = pick_kchunk<T>(C.g);
+    mg.L.push_back(C);
+  }
+  Lev<T>& Lc = mg.L.back();
+  const long long nc = Lc.g.ndof();
+  const std::string s = tag + "c";
+  Lc.dinv = c.vec<T>(s + "dinv", nc);
+  Lc.p = c.vec<T>(s + "p", nc);
+  Lc.q = c.vec<T>(s + "q", nc);
+  Lc.z = c.vec<T>(s + "z", nc);
+  if (!Lc.xa) {  // single-level hierarchy
+    Lc.xa = c.vec<T>(s + "xa", nc);
+    Lc.b = c.vec<T>(s + "b", nc);
+  }
+  return Lc.dinv && Lc.p && Lc.q && Lc.z && Lc.xa;
+}
+
+template <typename T>
+void mg_set_shift(Ctx& c, MG<T>& mg, double sigma) {
+  double s = sigma;
+  for (size_t l = 0; l < mg.L.size(); ++l) {
+    mg.L[l].sigma = (T)s;
+    s *= 8.0;  // row sums of P^T P
+  }
+  Lev<T>& Lc = mg.L.back();
+  launch_diag<T>(Lc.g, Lc.m, Lc.fac, mg.K, mg.quirk, Lc.sigma, nullptr, Lc.dinv, c.st);
+  c.launches++;
+}
+
+template <typename T>
+void coarse_solve(Ctx& c, MG<T>& mg, const T* b, T* x, const int* halt_main) {
+  Lev<T>& V = mg.L.back();
+  const long long n = V.g.ndof();
+  launch_scalars_init(c.s2, c.s, mg.citers, c.st);
+  launch_fill<T>(x, T(0), n, c.st);
+  launch_copy<T>(V.r, b, n, c.st);
+  c.launches += 3;
+  launch_jacobi_precond<T>(V.z, V.r, V.dinv, n, red(c, FIN_INIT_RZ, 1, c.s2), kRedBlocks, &c.s2->halt, c.st);
+  launch_copy<T>(V.p, V.z, n, c.st);
+  c.launches += 2;
+  const int* h2 = &c.s2->halt;
+  for (int it = 0; it < mg.citers; ++it) {
+    op<T>(c, OP_APPLY_DOT, opargs<T>(V, mg.K, mg.quirk, V.p, nullptr, V.q, T(0), h2, red(c, FIN_PCG_ALPHA, 1, c.s2)));
+    launch_pcg_update<T>(x, V.r, V.z, V.p, V.q, V.dinv, n, red(c, FIN_PCG_RES, 2, c.s2), kRedBlocks, c.s2, c.st);
+    launch_p_update<T>(V.p, V.z, n, c.s2, c.st);
+    c.launches += 2;
+  }
+  (void)halt_main;
+}
+
+template <typename T>
+void vcycle(Ctx& c, MG<T>& mg, int l, const T* b, T* xout, const int* halt) {
+  Lev<T>& V = mg.L[l];
+  if (l == (int)mg.L.size() - 1) {
+    coarse_solve<T>(c, mg, b, xout, halt);
+    return;
+  }
+  const int nw = mg.nu1 + mg.nu2;
+  auto bufw = [&](int w) -> T* { return ((nw - 1 - w) % 2 == 0) ? xout : V.xb; };
+  int w = 0;
+  T* cur = bufw(w++);
+  launch_jacobi0<T>(V.g, V.m, V.fac, mg.K, mg.quirk, V.sigma, mg.omega, b, cur, halt, c.st);
+  c.launches++;
+  RedArgs none = red(c, FIN_NONE, 1, nullptr);
+  for (int s = 1; s < mg.nu1; ++s) {
+    T* nx = bufw(w++);
+    op<T>(c, OP_JACOBI, opargs<T>(V, mg.K, mg.quirk, cur, b, nx, mg.omega, halt, none));
+    cur = nx;
+  }
+  op<T>(c, OP_RESID, opargs<T>(V, mg.K, mg.quirk, cur, b, V.r, mg.omega, halt, none));
+  Lev<T>& C = mg.L[l + 1];
+  launch_restrict<T>(V.g, V.r, C.g, C.m, C.b, halt, c.st);
+  c.launches++;
+  vcycle<T>(c, mg, l + 1, C.b, C.xa, halt);
+  launch_prolong_add<T>(C.g, C.xa, V.g, V.m, cur, halt, c.st);
+  c.launches++;
+  for (int s = 0; s < mg.nu2; ++s) {
+    T* nx = bufw(w++);
+    op<T>(c, OP_JACOBI, opargs<T>(V, mg.K, mg.quirk, cur, b, nx, mg.omega, halt, none));
+    cur = nx;
+  }
+}
+
+// A CUDA graph replaying a fixed launch sequence.
+struct Graph {
+  cudaGraphExec_t exec = nullptr;
+  int64_t nodes = 0;
+  ~Graph() { reset(); }
+  void reset() {
+    if (exec) cudaGraphExecDestroy(exec);
+    exec = nullptr;
+    nodes = 0;
+  }
+};
+
+template <class F>
+bool capture(Ctx& c, Graph& G, F&& body) {
+  G.reset();
+  if (cudaStreamBeginCapture(c.st, cudaStreamCaptureModeThreadLocal) != cudaSuccess) return c.cuda_ok("capture begin");
+  const int64_t before = c.launches;
+  body();
+  cudaGraph_t graph = nullptr;
+  cudaError_t e = cudaStreamEndCapture(c.st, &graph);
+  G.nodes = c.launches - before;
+  c.launches = before;
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return c.fail(std::string("graph capture failed: ") + cudaGetErrorString(e));
+  }
+  e = cudaGraphInstantiate(&G.exec, graph, 0);
+  cudaGraphDestroy(graph);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    G.exec = nullptr;
+    return c.fail(std::string("graph instantiate failed: ") + cudaGetErrorString(e));
+  }
+  return true;
+}
+
+bool replay(Ctx& c, Graph& G) {
+  if (cudaGraphLaunch(G.exec, c.st) != cudaSuccess) return c.cuda_ok("graph launch");
+  c.launches += G.nodes;
+  return true;
+}
+
+// PCG on (K + sigma I) x = b over one level-0 grid in precision T.
+template <typename T>
+struct PcgEnv {
+  Lev<T>* L0 = nullptr;
+  MG<T>* mg = nullptr;  // null: Jacobi
+  ModalK<T> K;
+  int quirk = 0;
+  long long n = 0;
+  T *x = nullptr, *r = nullptr, *zA = nullptr, *zB = nullptr, *p = nullptr, *q = nullptr, *dinv = nullptr;
+  const T* b = nullptr;
+  T* bestx = nullptr;  // nullable
+  bool use_graphs = true;
+  int graph_iters = 10;
+};
+
+struct PcgOut {
+  int status = 0;  // PcgScalars::status
+  int iters = 0;
+  double relres = 0.0;
+  double best_rel = INFINITY;
+  double fine_applies = 0.0;
+};
+
+template <typename T>
+void pcg_iteration(Ctx& c, PcgEnv<T>& E, int parity) {
+  Lev<T>& L = *E.L0;
+  const int* halt = &c.s->halt;
+  op<T>(c, OP_APPLY_DOT, opargs<T>(L, E.K, E.quirk, E.p, nullptr, E.q, T(0), halt, red(c, FIN_PCG_ALPHA, 1, c.s)));
+  if (!E.mg) {
+    launch_pcg_update<T>(E.x, E.r, E.zA, E.p, E.q, E.dinv, E.n, red(c, FIN_PCG_RES, 2, c.s), kRedBlocks, c.s, c.st);
+    launch_p_update<T>(E.p, E.zA, E.n, c.s, c.st);
+    c.launches += 2;
+  } else {
+    T* zc = (parity == 0) ? E.zB : E.zA;
+    T* zo = (parity == 0) ? E.zA : E.zB;
+    launch_pcg_update<T>(E.x, E.r, nullptr, E.p, E.q, nullptr, E.n, red(c, FIN_PCG_RES, 1, c.s), kRedBlocks, c.s, c.st);
+    c.launches++;
+    vcycle<T>(c, *E.mg, 0, E.r, zc, halt);
+    launch_dot<T>(E.r, zc, E.r, zo, E.n, red(c, FIN_PCG_BETA, 2, c.s), kRedBlocks, halt, c.st);
+    launch_p_update<T>(E.p, zc, E.n, c.s, c.st);
+    c.launches += 2;
+  }
+}
+
+template <typename T>
+double applies_per_iteration(const PcgEnv<T>& E) {
+  if (!E.mg) return 1.0;
+  // fine-level operator passes: PCG apply + (nu1-1) + residual + nu2 ; the
+  // coarser levels add ~1/8 per level
+  const MG<T>& mg = *E.mg;
+  double per = 0.0, w = 1.0;
+  for (size_t l = 0; l + 1 < mg.L.size(); ++l) {
+    per += w * (mg.nu1 - 1 + 1 + mg.nu2);
+    w /= 8.0;
+  }
+  per += w * mg.citers;
+  return 1.0 + per;
+}
+
+// Runs PCG from the current E.x.  host_scalars carries tol/max_iter/cadence.
+template <typename T>
+bool run_pcg(Ctx& c, PcgEnv<T>& E, double tol, int max_iter, int cadence, bool x_is_zero, double bnorm,
+             PcgOut* out) {
+  PcgScalars h;
+  std::memset(&h, 0, sizeof(h));
+  h.tol = tol;
+  h.max_iter = max_iter;
+  h.cadence = cadence;
+  h.bnorm = bnorm;
+  h.best_rel = INFINITY;
+  *c.hs = h;
+  cudaMemcpyAsync(c.s, c.hs, sizeof(PcgScalars), cudaMemcpyHostToDevice, c.st);
+  Lev<T>& L = *E.L0;
+  const int* halt = &c.s->halt;
+  if (x_is_zero) {
+    launch_copy<T>(E.r, E.b, E.n, c.st);
+    c.launches++;
+  } else {
+    op<T>(c, OP_RESID_NORM, opargs<T>(L, E.K, E.quirk, E.x, E.b, E.r, T(0), halt, red(c, FIN_INIT_RES, 1, c.s)));
+  }
+  if (!E.mg) {
+    launch_jacobi_precond<T>(E.zA, E.r, E.dinv, E.n, red(c, FIN_INIT_RZ, 1, c.s), kRedBlocks, halt, c.st);
+    c.launches++;
+  } else {
+    vcycle<T>(c, *E.mg, 0, E.r, E.zA, halt);
+    launch_dot<T>(E.r, E.zA, (const T*)nullptr, (const T*)nullptr, E.n, red(c, FIN_INIT_RZ, 1, c.s), kRedBlocks,
+                  halt, c.st);
+    c.launches++;
+  }
+  launch_copy<T>(E.p, E.zA, E.n, c.st);
+  c.launches++;
+  if (!c.cuda_ok("pcg setup")) return false;
+
+  int G = E.graph_iters < 2 ? 2 : E.graph_iters;
+  if (G & 1) ++G;
+  Graph graph;
+  if (E.use_graphs) {
+    if (!capture(c, graph, [&]() {
+          for (int i = 0; i < G; ++i) pcg_iteration<T>(c, E, i & 1);
+        }))
+      return false;
+  }
+  double host_best = INFINITY;
+  int done_iters = 0;
+  const double per = applies_per_iteration(E);
+  while (true) {
+    if (E.use_graphs) {
+      if (!replay(c, graph)) return false;
+    } else {
+      for (int i = 0; i < G; ++i) pcg_iteration<T>(c, E, i & 1);
+      if (!c.cuda_ok("pcg iteration")) return false;
+    }
+    cudaMemcpyAsync(c.hs, c.s, sizeof(PcgScalars), cudaMemcpyDeviceToHost, c.st);
+    if (cudaStreamSynchronize(c.st) != cudaSuccess) return c.cuda_ok("pcg sync");
+    h = *c.hs;
+    done_iters = h.iter;
+    if (E.bestx && h.best_rel < host_best) {
+      host_best = h.best_rel;
+      cudaMemcpyAsync(E.bestx, E.x, sizeof(T) * E.n, cudaMemcpyDeviceToDevice, c.st);
+    }
+    if (h.halt) break;
+  }
+  out->status = h.status;
+  out->iters = done_iters;
+  out->relres = h.relres;
+  out->best_rel = h.best_rel;
+  out->fine_applies += per * done_iters + (x_is_zero ? 0.0 : 1.0);
+  return true;
+}
+
+template <typename T>
+struct Host {
+  static const T* fac(Ctx& c, const Problem& P) {
+    T* f = c.vec<T>("fac_T", P.g.nelem());
+    if (f) {
+      launch_convert<T, double>(f, P.fac64, P.g.nelem(), c.st);
+      c.launches++;
+    }
+    return f;
+  }
+};
+template <>
+struct Host<double> {
+  static const double* fac(Ctx&, const Problem& P) { return P.fac64; }
+};
+
+// sqrt(||f - (K+sigma I) u||^2) in FP64, written to r64 as well.
+double true_residual_norm(Ctx& c, const Problem& P, const ModalK<double>& K64, int quirk, double sigma, const double* u,
+                          double* r64) {
+  Lev<double> L;
+  L.g = P.g;
+  L.m = P.m;
+  L.fac = const_cast<double*>(P.fac64);
+  L.sigma = sigma;
+  L.kchunk = pick_kchunk<double>(P.g);
+  op<double>(c, OP_RESID_NORM, opargs<double>(L, K64, quirk, u, P.f64, r64, 0.0, nullptr, red(c, FIN_STORE, 1, nullptr, c.dscal + 8)));
+  cudaMemcpyAsync(c.hscal + 8, c.dscal + 8, sizeof(double), cudaMemcpyDeviceToHost, c.st);
+  cudaStreamSynchronize(c.st);
+  return std::sqrt(std::fmax(c.hscal[8], 0.0));
+}
+
+double device_dot(Ctx& c, const double* a, const double* b, long long n, int slot) {
+  launch_dot<double>(a, b, (const double*)nullptr, (const double*)nullptr, n, red(c, FIN_STORE, 1, nullptr, c.dscal + slot),
+                     kRedBlocks, nullptr, c.st);
+  c.launches++;
+  cudaMemcpyAsync(c.hscal + slot, c.dscal + slot, sizeof(double), cudaMemcpyDeviceToHost, c.st);
+  cudaStreamSynchronize(c.st);
+  return c.hscal[slot];
+}
+
+bool setup_common(Ctx& c, const Problem& P, const hexa_solve_params& prm, ModalK<double>* K64, double* max_diag,
+                  double* bnorm) {
+  std::string e;
+  if (!build_modal(P.dx, P.dy, P.dz, P.nu, K64, &e)) return c.fail(e);
+  const long long n = P.g.ndof();
+  double* diag = c.vec<double>("diag64", n);
+  if (!diag) return false;
+  const long long maxblocks = op_num_blocks<double>(P.g, pick_kchunk<double>(P.g)) + 8;
+  if (!c.ensure_partials((size_t)std::max<long long>(maxblocks * 2, kRedBlocks * 2 + 16) + 4096)) return false;
+  launch_diag<double>(P.g, P.m, P.fac64, *K64, prm.diag_quirk, 0.0, diag, nullptr, c.st);
+  launch_max(diag, n, red(c, FIN_STORE, 1, nullptr, c.dscal + 0), kRedBlocks, c.st);
+  c.launches += 2;
+  launch_dot<double>(P.f64, P.f64, (const double*)nullptr, (const double*)nullptr, n,
+                     red(c, FIN_STORE, 1, nullptr, c.dscal + 1), kRedBlocks, nullptr, c.st);
+  c.launches++;
+  cudaMemcpyAsync(c.hscal, c.dscal, 2 * sizeof(double), cudaMemcpyDeviceToHost, c.st);
+  if (cudaStreamSynchronize(c.st) != cudaSuccess) return c.cuda_ok("setup");
+  *max_diag = c.hscal[0];
+  *bnorm = std::sqrt(std::fmax(c.hscal[1], 0.0));
+  return true;
+}
+
+template <typename T>
+int solve_plain(Ctx& c, const Problem& P, const hexa_solve_params& prm, const double* u0, double* u,
+                hexa_solve_stats* st) {
+  const long long n = P.g.ndof();
+  ModalK<double> K64;
+  double max_diag = 0, bnorm = 0;
+  cudaEventRecord(c.ev[0], c.st);
+  if (!setup_common(c, P, prm, &K64, &max_diag, &bnorm)) return c.err.empty() ? HEXA_ERR_CUDA : HEXA_ERR_NOMEM;
+  st->max_diag = max_diag;
+  if (std::isnan(max_diag) || std::isinf(max_diag)) {  // GPUSolver.jl:310-315
+    c.err = "Stiffness Matrix Diagonal contains NaN/Inf";
+    cudaMemsetAsync(u, 0, sizeof(double) * n, c.st);
+    st->relres = NAN;
+    return HEXA_ERR_CORRUPT_INPUT;
+  }
+  if (bnorm == 0.0) {
+    cudaMemsetAsync(u, 0, sizeof(double) * n, c.st);
+    st->relres = 0.0;
+    st->true_relres = 0.0;
+    return HEXA_OK;
+  }
+  ModalK<T> K;
+  if (Is64<T>::v) std::memcpy(&K, &K64, sizeof(K));
+  else {
+    ModalK<float> kf = modal_to_f32(K64);
+    std::memcpy(&K, &kf, sizeof(K));
+  }
+  const T* fac = Host<T>::fac(c, P);
+  const T* b;
+  if (Is64<T>::v) b = (const T*)P.f64;
+  else {
+    T* bb = c.vec<T>("b_T", n);
+    if (!bb) return HEXA_ERR_NOMEM;
+    launch_convert<T, double>(bb, P.f64, n, c.st);
+    c.launches++;
+    b = bb;
+  }
+  Lev<T> L0;
+  L0.g = P.g;
+  L0.m = P.m;
+  L0.fac = const_cast<T*>(fac);
+  L0.kchunk = pick_kchunk<T>(P.g);
+  PcgEnv<T> E;
+  E.K = K;
+  E.quirk = prm.diag_quirk;
+  E.n = n;
+  E.x = c.vec<T>("x_T", n);
+  E.r = c.vec<T>("r_T", n);
+  E.zA = c.vec<T>("zA_T", n);
+  E.zB = c.vec<T>("zB_T", n);
+  E.p = c.vec<T>("p_T", n);
+  E.q = c.vec<T>("q_T", n);
+  E.dinv = c.vec<T>("dinv_T", n);
+  E.bestx = c.vec<T>("best_T", n);
+  E.b = b;
+  E.use_graphs = prm.use_graphs != 0;
+  E.graph_iters = prm.graph_iters > 0 ? prm.graph_iters : 10;
+  if (!fac || !E.x || !E.r || !E.zA || !E.zB || !E.p || !E.q || !E.dinv || !E.bestx) return HEXA_ERR_NOMEM;
+  launch_fill<T>(E.bestx, T(0), n, c.st);  // best_x starts at zero (GPUSolver.jl:319)
+  c.launches++;
+  MG<T> mg;
+  const bool want_mg = prm.precond == HEXA_PRECOND_MULTIGRID;
+  int nlev = 1;
+  if (want_mg) {
+    nlev = plan_levels(P.g, prm.mg_levels);
+    mg.K = K;
+    mg.quirk = prm.diag_quirk;
+    mg.omega = (T)(prm.jacobi_omega > 0 ? prm.jacobi_omega : 0.6);
+    mg.nu1 = prm.pre_smooth > 0 ? prm.pre_smooth : 1;
+    mg.nu2 = prm.post_smooth >= 0 ? prm.post_smooth : 2;
+    mg.citers = prm.coarse_iters >= 0 ? prm.coarse_iters : 30;
+    if (!build_mg<T>(c, mg, P.g, P.m, fac, nlev, std::string(Is64<T>::v ? "mg64_" : "mg32_"))) return HEXA_ERR_NOMEM;
+    mg.L[0].kchunk = L0.kchunk;
+  }
+  if (!c.cuda_ok("solve setup")) return HEXA_ERR_CUDA;
+  cudaEventRecord(c.ev[1], c.st);
+
+  bool use_mg = want_mg;
+  bool success = false;
+  PcgOut last;
+  double final_rel = 0.0, sigma = 0.0;
+  int attempts = 0, total_iters = 0;
+  double applies = 0.0;
+  while (true) {
+    double cur_shift = prm.shift_factor;
+    bool fallback = false;
+    for (int attempt = 1; attempt <= std::max(1, prm.max_shift_attempts); ++attempt) {
+      ++attempts;
+      sigma = cur_shift * max_diag;
+      L0.sigma = (T)sigma;
+      E.L0 = use_mg ? &mg.L[0] : &L0;
+      E.mg = use_mg ? &mg : nullptr;
+      bool x_zero = true;
+      if (u0 && attempt == 1 && use_mg == want_mg) {
+        launch_mask_copy<T, double>(P.g, P.m, E.x, u0, c.st);
+        c.launches++;
+        x_zero = false;
+      } else {
+        launch_fill<T>(E.x, T(0), n, c.st);
+        c.launches++;
+      }
+      if (use_mg) mg_set_shift<T>(c, mg, sigma);
+      else {
+        launch_diag<T>(P.g, P.m, fac, K, prm.diag_quirk, (T)sigma, nullptr, E.dinv, c.st);
+        c.launches++;
+      }
+      PcgOut o;
+      if (!run_pcg<T>(c, E, prm.tol, prm.max_iter, prm.check_cadence, x_zero, bnorm, &o)) return HEXA_ERR_CUDA;
+      // FP64 true-residual restarts (plain FP64 only)
+      if (o.status == 1 && prm.true_residual && Is64<T>::v) {
+        double* r64 = c.vec<double>("rtrue", n);
+        for (int rs = 0; rs < 4; ++rs) {
+          const double tr = true_residual_norm(c, P, K64, prm.diag_quirk, sigma, (const double*)E.x, r64) / bnorm;
+          applies += 1.0;
+          if (tr <= prm.tol) break;
+          PcgOut o2;
+          const int left = prm.max_iter - o.iters;
+          if (left <= 0) break;
+          if (!run_pcg<T>(c, E, prm.tol, left, prm.check_cadence, false, bnorm, &o2)) return HEXA_ERR_CUDA;
+          o.iters += o2.iters;
+          o.fine_applies += o2.fine_applies;
+          o.status = o2.status;
+          o.relres = o2.relres;
+          if (o2.status != 1) break;
+        }
+      }
+      last = o;
+      total_iters += o.iters;
+      applies += o.fine_applies;
+      final_rel = o.relres;
+      if (o.status == 1) {
+        success = true;
+        break;
+      }
+      const bool bad = (o.status == 2 || o.status == 3);
+      if (bad && use_mg) {
+        fallback = true;
+        break;
+      }
+      if (bad && attempt < prm.max_shift_attempts) {
+        cur_shift *= prm.shift_multiplier;
+        continue;
+      }
+      if (prm.stagnation_tol > 0.0 && o.best_rel < prm.stagnation_tol) {
+        cudaMemcpyAsync(E.x, E.bestx, sizeof(T) * n, cudaMemcpyDeviceToDevice, c.st);
+        success = true;
+        break;
+      }
+      cur_shift *= prm.shift_multiplier;
+    }
+    if (fallback) {
+      use_mg = false;
+      continue;
+    }
+    if (!success) cudaMemcpyAsync(E.x, E.bestx, sizeof(T) * n, cudaMemcpyDeviceToDevice, c.st);
+    break;
+  }
+  if (Is64<T>::v) cudaMemcpyAsync(u, E.x, sizeof(double) * n, cudaMemcpyDeviceToDevice, c.st);
+  else {
+    launch_convert<double, T>(u, E.x, n, c.st);
+    c.launches++;
+  }
+  double* r64 = c.vec<double>("rtrue", n);
+  const double tr = true_residual_norm(c, P, K64, prm.diag_quirk, sigma, u, r64) / bnorm;
+  cudaEventRecord(c.ev[2], c.st);
+  st->compliance = device_dot(c, P.f64, u, n, 9);
+  cudaEventSynchronize(c.ev[2]);
+  float ms1 = 0, ms2 = 0;
+  cudaEventElapsedTime(&ms1, c.ev[0], c.ev[1]);
+  cudaEventElapsedTime(&ms2, c.ev[1], c.ev[2]);
+  st->setup_ms = ms1;
+  st->solve_ms = ms2;
+  st->iterations = total_iters;
+  st->attempts = attempts;
+  st->relres = final_rel;
+  st->true_relres = tr;
+  st->shift = sigma;
+  st->precond_used = use_mg ? HEXA_PRECOND_USED_MULTIGRID : HEXA_PRECOND_USED_JACOBI;
+  st->mg_levels = use_mg ? (int)mg.L.size() : 1;
+  st->fine_applies = applies;
+  st->fine_applies_fp64 = Is64<T>::v ? applies : 1.0;
+  if (!c.cuda_ok("solve")) return HEXA_ERR_CUDA;
+  (void)last;
+  return success ? HEXA_OK : HEXA_NOT_CONVERGED;
+}
+
+// Mixed precision: FP64 iterative refinement around FP32 GMG-PCG correction
+// solves.  Each step rescales the FP64 residual to unit norm before it is
+// rounded to FP32, so the 1e-9 contrast of void elements never meets FP32's
+// range limits, and adds the correction back in FP64.
+int solve_mixed(Ctx& c, const Problem& P, const hexa_solve_params& prm, const double* u0, double* u,
+                hexa_solve_stats* st) {
+  const long long n = P.g.ndof();
+  ModalK<double> K64;
+  double max_diag = 0, bnorm = 0;
+  cudaEventRecord(c.ev[0], c.st);
+  if (!setup_common(c, P, prm, &K64, &max_diag, &bnorm)) return c.err.empty() ? HEXA_ERR_CUDA : HEXA_ERR_NOMEM;
+  st->max_diag = max_diag;
+  if (std::isnan(max_diag) || std::isinf(max_diag)) {
+    c.err = "Stiffness Matrix Diagonal contains NaN/Inf";
+    cudaMemsetAsync(u, 0, sizeof(double) * n, c.st);
+    st->relres = NAN;
+    return HEXA_ERR_CORRUPT_INPUT;
+  }
+  if (bnorm == 0.0) {
+    cudaMemsetAsync(u, 0, sizeof(double) * n, c.st);
+    return HEXA_OK;
+  }
+  const double sigma = prm.shift_factor * max_diag;
+  ModalK<float> K32 = modal_to_f32(K64);
+  float* fac32 = c.vec<float>("fac_T", P.g.nelem());
+  if (!fac32) return HEXA_ERR_NOMEM;
+  launch_convert<float, double>(fac32, P.fac64, P.g.nelem(), c.st);
+  c.launches++;
+  Lev<float> L0;
+  L0.g = P.g;
+  L0.m = P.m;
+  L0.fac = fac32;
+  L0.kchunk = pick_kchunk<float>(P.g);
+  L0.sigma = (float)sigma;
+  PcgEnv<float> E;
+  E.K = K32;
+  E.quirk = prm.diag_quirk;
+  E.n = n;
+  E.x = c.vec<float>("x_T", n);
+  E.r = c.vec<float>("r_T", n);
+  E.zA = c.vec<float>("zA_T", n);
+  E.zB = c.vec<float>("zB_T", n);
+  E.p = c.vec<float>("p_T", n);
+  E.q = c.vec<float>("q_T", n);
+  E.dinv = c.vec<float>("dinv_T", n);
+  float* b32 = c.vec<float>("b_T", n);
+  double* r64 = c.vec<double>("rtrue", n);
+  E.b = b32;
+  E.use_graphs = prm.use_graphs != 0;
+  E.graph_iters = prm.graph_iters > 0 ? prm.graph_iters : 10;
+  if (!E.x || !E.r || !E.zA || !E.zB || !E.p || !E.q || !E.dinv || !b32 || !r64) return HEXA_ERR_NOMEM;
+  MG<float> mg;
+  const bool use_mg = prm.precond == HEXA_PRECOND_MULTIGRID;
+  if (use_mg) {
+    const int nlev = plan_levels(P.g, prm.mg_levels);
+    mg.K = K32;
+    mg.quirk = prm.diag_quirk;
+    mg.omega = (float)(prm.jacobi_omega > 0 ? prm.jacobi_omega : 0.6);
+    mg.nu1 = prm.pre_smooth > 0 ? prm.pre_smooth : 1;
+    mg.nu2 = prm.post_smooth >= 0 ? prm.post_smooth : 2;
+    mg.citers = prm.coarse_iters >= 0 ? prm.coarse_iters : 30;
+    if (!build_mg<float>(c, mg, P.g, P.m, fac32, nlev, "mg32_")) return HEXA_ERR_NOMEM;
+    mg.L[0].kchunk = L0.kchunk;
+    mg_set_shift<float>(c, mg, sigma);
+    E.L0 = &mg.L[0];
+    E.mg = &mg;
+  } else {
+    launch_diag<float>(P.g, P.m, fac32, K32, prm.diag_quirk, (float)sigma, nullptr, E.dinv, c.st);
+    c.launches++;
+    E.L0 = &L0;
+  }
+  if (u0) {
+    launch_mask_copy<double, double>(P.g, P.m, u, u0, c.st);
+  } else {
+    launch_fill<double>(u, 0.0, n, c.st);
+  }
+  c.launches++;
+  if (!c.cuda_ok("mixed setup")) return HEXA_ERR_CUDA;
+  cudaEventRecord(c.ev[1], c.st);
+  double rn = true_residual_norm(c, P, K64, prm.diag_quirk, sigma, u, r64);
+  double rel = rn / bnorm;
+  double applies64 = 1.0, applies32 = 0.0;
+  int outer = 0, inner_total = 0, status = HEXA_OK;
+  const int max_outer = prm.max_outer > 0 ? prm.max_outer : 20;
+  const double inner_tol = prm.inner_tol > 0 ? prm.inner_tol : 1e-4;
+  while (rel > prm.tol) {
+    if (outer >= max_outer || inner_total >= prm.max_iter || !(rel == rel)) {
+      status = HEXA_NOT_CONVERGED;
+      break;
+    }
+    ++outer;
+    c.hscal[10] = 1.0 / rn;
+    cudaMemcpyAsync(c.dscal + 10, c.hscal + 10, sizeof(double), cudaMemcpyHostToDevice, c.st);
+    launch_scale_to_f32(b32, r64, c.dscal + 10, n, c.st);
+    launch_fill<float>(E.x, 0.0f, n, c.st);
+    c.launches += 2;
+    PcgOut o;
+    if (!run_pcg<float>(c, E, inner_tol, prm.max_iter - inner_total, prm.check_cadence, true, 1.0, &o))
+      return HEXA_ERR_CUDA;
+    inner_total += o.iters;
+    applies32 += o.fine_applies;
+    if (o.status == 2 || o.iters == 0) {
+      status = HEXA_NOT_CONVERGED;
+      break;
+    }
+    launch_add_scaled_f32(u, E.x, c.dscal + 10, n, c.st);
+    c.launches++;
+    rn = true_residual_norm(c, P, K64, prm.diag_quirk, sigma, u, r64);
+    applies64 += 1.0;
+    rel = rn / bnorm;
+  }
+  cudaEventRecord(c.ev[2], c.st);
+  st->compliance = device_dot(c, P.f64, u, n, 9);
+  cudaEventSynchronize(c.ev[2]);
+  float ms1 = 0, ms2 = 0;
+  cudaEventElapsedTime(&ms1, c.ev[0], c.ev[1]);
+  cudaEventElapsedTime(&ms2, c.ev[1], c.ev[2]);
+  st->setup_ms = ms1;
+  st->solve_ms = ms2;
+  st->iterations = inner_total;
+  st->outer_iterations = outer;
+  st->attempts = 1;
+  st->relres = rel;
+  st->true_relres = rel;
+  st->shift = sigma;
+  st->precond_used = use_mg ? HEXA_PRECOND_USED_MULTIGRID : HEXA_PRECOND_USED_JACOBI;
+  st->mg_levels = use_mg ? (int)mg.L.size() : 1;
+  st->fine_applies = applies32 + applies64;
+  st->fine_applies_fp64 = applies64;
+  if (!c.cuda_ok("mixed solve")) return HEXA_ERR_CUDA;
+  return status;
+}
+
+}  // namespace
+
+int solve_problem(Ctx& c, const Problem& P, const hexa_solve_params& prm, const double* u0, double* u,
+                  hexa_solve_stats* st) {
+  switch (prm.precision) {
+    case HEXA_PREC_FP64: return solve_plain<double>(c, P, prm, u0, u, st);
+    case HEXA_PREC_FP32: return solve_plain<float>(c, P, prm, u0, u, st);
+    case HEXA_PREC_MIXED: return solve_mixed(c, P, prm, u0, u, st);
+    default: c.err = "unknown precision"; return HEXA_ERR_ARG;
+  }
+}
+
+}  // namespace hexa

@@ -1,0 +1,330 @@
+// (b) Fused PCG vector passes and small helpers.
+//
+// Replaces the reference's separate broadcasts and CUBLAS calls of one PCG
+// iteration (src/Solvers/GPUSolver.jl:372-416: the shift broadcast, dot(p,Ap)
+// with a host round trip, two axpys, dot(r,r) every 10 iterations, the Jacobi
+// kernel :162-168, dot(r,z) and the p update).  Here one pass does
+// x += alpha p, r -= alpha Ap, ||r||^2, z = M^-1 r and r.z with warp-shuffle
+// block reductions; the coefficients (alpha, beta) and the convergence test
+// live in device memory, so no scalar ever returns to the host inside an
+// iteration.
+#include "hexa_common.cuh"
+#include "hexa_kernels.h"
+
+namespace hexa {
+
+static inline int vec_blocks(long long n, int threads = 256, int maxb = 152 * 8) {
+  long long b = (n + threads - 1) / threads;
+  if (b < 1) b = 1;
+  if (b > maxb) b = maxb;
+  return (int)b;
+}
+
+template <typename T>
+__global__ void fill_kernel(T* v, T val, long long n) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x)
+    v[i] = val;
+}
+
+template <typename T>
+void launch_fill(T* v, T val, long long n, cudaStream_t st) {
+  fill_kernel<T><<<vec_blocks(n), 256, 0, st>>>(v, val, n);
+}
+void launch_fill_u32(unsigned* v, unsigned val, long long n, cudaStream_t st) {
+  fill_kernel<unsigned><<<vec_blocks(n), 256, 0, st>>>(v, val, n);
+}
+
+template <typename T>
+__global__ void copy_kernel(T* __restrict__ d, const T* __restrict__ s, long long n) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x)
+    d[i] = s[i];
+}
+template <typename T>
+void launch_copy(T* dst, const T* src, long long n, cudaStream_t st) {
+  copy_kernel<T><<<vec_blocks(n), 256, 0, st>>>(dst, src, n);
+}
+
+template <typename TD, typename TS>
+__global__ void mask_copy_kernel(Grid g, Mask m, TD* __restrict__ d, const TS* __restrict__ s) {
+  const long long nn = g.nnode();
+  for (long long n = blockIdx.x * (long long)blockDim.x + threadIdx.x; n < nn;
+       n += (long long)gridDim.x * blockDim.x) {
+    const int i = (int)(n % g.NX);
+    const long long t = n / g.NX;
+    const int j = (int)(t % g.NY), k = (int)(t / g.NY);
+    const unsigned fx = fixed_bits(g, m, i, j, k, n);
+#pragma unroll
+    for (int c = 0; c < 3; ++c) d[3 * n + c] = ((fx >> c) & 1u) ? TD(0) : (TD)s[3 * n + c];
+  }
+}
+template <typename TD, typename TS>
+void launch_mask_copy(const Grid& g, const Mask& m, TD* dst, const TS* src, cudaStream_t st) {
+  mask_copy_kernel<TD, TS><<<vec_blocks(g.nnode()), 256, 0, st>>>(g, m, dst, src);
+}
+
+// Sum of the factors of the (up to) 8 elements around node (i,j,k).
+template <typename T>
+__device__ __forceinline__ T node_factor_sum(const Grid& g, const T* __restrict__ fac, int i, int j,
+                                             int k) {
+  T s = T(0);
+#pragma unroll
+  for (int dz = -1; dz <= 0; ++dz)
+#pragma unroll
+    for (int dy = -1; dy <= 0; ++dy)
+#pragma unroll
+      for (int dx = -1; dx <= 0; ++dx) {
+        const int ei = i + dx, ej = j + dy, ek = k + dz;
+        if (ei >= 0 && ei < g.nx && ej >= 0 && ej < g.ny && ek >= 0 && ek < g.nz)
+          s += __ldg(fac + (long long)ei + (long long)g.nx * ((long long)ej + (long long)g.ny * ek));
+      }
+  return s;
+}
+
+template <typename T>
+__global__ void diag_kernel(Grid g, Mask m, const T* __restrict__ fac, ModalK<T> K, int quirk,
+                            T sigma, T* __restrict__ diag, T* __restrict__ dinv) {
+  const long long nn = g.nnode();
+  for (long long n = blockIdx.x * (long long)blockDim.x + threadIdx.x; n < nn;
+       n += (long long)gridDim.x * blockDim.x) {
+    const int i = (int)(n % g.NX);
+    const long long t = n / g.NX;
+    const int j = (int)(t % g.NY), k = (int)(t / g.NY);
+    const unsigned fx = fixed_bits(g, m, i, j, k, n);
+    const T fs = node_factor_sum<T>(g, fac, i, j, k);
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      const bool fixd = (fx >> c) & 1u;
+      const T d = K.dd[quirk ? 0 : c] * fs;
+      if (diag) diag[3 * n + c] = fixd ? T(0) : d;
+      if (dinv) dinv[3 * n + c] = fixd ? T(0) : T(1) / (d + sigma);
+    }
+  }
+}
+template <typename T>
+void launch_diag(const Grid& g, const Mask& m, const T* fac, const ModalK<T>& K, int quirk, T sigma,
+                 T* diag, T* dinv, cudaStream_t st) {
+  diag_kernel<T><<<vec_blocks(g.nnode()), 256, 0, st>>>(g, m, fac, K, quirk, sigma, diag, dinv);
+}
+
+__global__ void max_kernel(const double* __restrict__ v, long long n, RedArgs red) {
+  double mx = -INFINITY;
+  bool bad = false;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    const double t = v[i];
+    if (!(t == t) || isinf(t)) bad = true;
+    mx = fmax(mx, t);
+  }
+  // reduce max through the sum machinery: encode as two passes is overkill;
+  // use a shared-memory max then the ticketed finalize on the block maxima.
+  __shared__ double sm[32];
+  __shared__ int sbad;
+  __shared__ bool am_last;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  if (threadIdx.x == 0) sbad = 0;
+  __syncthreads();
+  if (bad) atomicOr(&sbad, 1);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+  if (lane == 0) sm[wid] = mx;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = -INFINITY;
+    for (int w = 0; w < nw; ++w) t = fmax(t, sm[w]);
+    red.partials[2 * blockIdx.x] = t;
+    red.partials[2 * blockIdx.x + 1] = sbad ? 1.0 : 0.0;
+    __threadfence();
+    const unsigned tk = atomicAdd(red.ticket, 1u);
+    am_last = (tk == gridDim.x - 1);
+  }
+  __syncthreads();
+  if (am_last && threadIdx.x == 0) {
+    __threadfence();
+    double t = -INFINITY, b = 0.0;
+    for (unsigned q = 0; q < gridDim.x; ++q) {
+      t = fmax(t, ((volatile double*)red.partials)[2 * q]);
+      b = fmax(b, ((volatile double*)red.partials)[2 * q + 1]);
+    }
+    red.dst[0] = (b > 0.0) ? NAN : t;
+    *red.ticket = 0u;
+  }
+}
+void launch_max(const double* v, long long n, const RedArgs& red, int nblocks, cudaStream_t st) {
+  max_kernel<<<nblocks, 256, 0, st>>>(v, n, red);
+}
+
+template <typename T, int NS>
+__global__ void dot_kernel(const T* __restrict__ a, const T* __restrict__ b, const T* __restrict__ c,
+                           const T* __restrict__ d, long long n, RedArgs red, const int* halt) {
+  if (halt && *((volatile const int*)halt)) return;
+  double acc[NS];
+#pragma unroll
+  for (int q = 0; q < NS; ++q) acc[q] = 0.0;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    acc[0] += (double)a[i] * (double)b[i];
+    if (NS > 1) acc[NS - 1] += (double)c[i] * (double)d[i];
+  }
+  block_reduce_finalize<NS>(red, acc);
+}
+template <typename T>
+void launch_dot(const T* a, const T* b, const T* c, const T* d, long long n, const RedArgs& red,
+                int nblocks, const int* halt, cudaStream_t st) {
+  if (c) dot_kernel<T, 2><<<nblocks, 256, 0, st>>>(a, b, c, d, n, red, halt);
+  else dot_kernel<T, 1><<<nblocks, 256, 0, st>>>(a, b, c, d, n, red, halt);
+}
+
+template <typename T, bool JAC>
+__global__ void pcg_update_kernel(T* __restrict__ x, T* __restrict__ r, T* __restrict__ z,
+                                  const T* __restrict__ p, const T* __restrict__ q,
+                                  const T* __restrict__ dinv, long long n, RedArgs red,
+                                  const PcgScalars* s) {
+  if (*((volatile const int*)&s->halt)) return;
+  const T alpha = (T)s->alpha;
+  double acc[JAC ? 2 : 1];
+  acc[0] = 0.0;
+  if (JAC) acc[JAC ? 1 : 0] = 0.0;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    x[i] = fma(alpha, p[i], x[i]);
+    const T ri = fma(-alpha, q[i], r[i]);
+    r[i] = ri;
+    acc[0] += (double)ri * (double)ri;
+    if (JAC) {
+      const T zi = ri * dinv[i];
+      z[i] = zi;
+      acc[JAC ? 1 : 0] += (double)ri * (double)zi;
+    }
+  }
+  block_reduce_finalize<JAC ? 2 : 1>(red, acc);
+}
+template <typename T>
+void launch_pcg_update(T* x, T* r, T* z, const T* p, const T* q, const T* dinv, long long n,
+                       const RedArgs& red, int nblocks, const PcgScalars* s, cudaStream_t st) {
+  if (dinv) pcg_update_kernel<T, true><<<nblocks, 256, 0, st>>>(x, r, z, p, q, dinv, n, red, s);
+  else pcg_update_kernel<T, false><<<nblocks, 256, 0, st>>>(x, r, z, p, q, dinv, n, red, s);
+}
+
+template <typename T>
+__global__ void p_update_kernel(T* __restrict__ p, const T* __restrict__ z, long long n,
+                                const PcgScalars* s) {
+  if (*((volatile const int*)&s->halt)) return;
+  const T beta = (T)s->beta;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x)
+    p[i] = fma(beta, p[i], z[i]);
+}
+template <typename T>
+void launch_p_update(T* p, const T* z, long long n, const PcgScalars* s, cudaStream_t st) {
+  p_update_kernel<T><<<vec_blocks(n), 256, 0, st>>>(p, z, n, s);
+}
+
+template <typename T>
+__global__ void jacobi_precond_kernel(T* __restrict__ z, const T* __restrict__ r,
+                                      const T* __restrict__ dinv, long long n, RedArgs red,
+                                      const int* halt) {
+  if (halt && *((volatile const int*)halt)) return;
+  double acc[1] = {0.0};
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    const T zi = r[i] * dinv[i];
+    z[i] = zi;
+    acc[0] += (double)r[i] * (double)zi;
+  }
+  block_reduce_finalize<1>(red, acc);
+}
+template <typename T>
+void launch_jacobi_precond(T* z, const T* r, const T* dinv, long long n, const RedArgs& red,
+                           int nblocks, const int* halt, cudaStream_t st) {
+  jacobi_precond_kernel<T><<<nblocks, 256, 0, st>>>(z, r, dinv, n, red, halt);
+}
+
+__global__ void scale_to_f32_kernel(float* __restrict__ d, const double* __restrict__ s,
+                                    const double* scale, long long n) {
+  const double sc = *scale;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x)
+    d[i] = (float)(s[i] * sc);
+}
+void launch_scale_to_f32(float* dst, const double* src, const double* scale, long long n,
+                         cudaStream_t st) {
+  scale_to_f32_kernel<<<vec_blocks(n), 256, 0, st>>>(dst, src, scale, n);
+}
+
+__global__ void add_scaled_f32_kernel(double* __restrict__ u, const float* __restrict__ d,
+                                      const double* scale, long long n) {
+  const double inv = 1.0 / *scale;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x)
+    u[i] = fma((double)d[i], inv, u[i]);
+}
+void launch_add_scaled_f32(double* u, const float* d, const double* scale, long long n,
+                           cudaStream_t st) {
+  add_scaled_f32_kernel<<<vec_blocks(n), 256, 0, st>>>(u, d, scale, n);
+}
+
+template <typename T>
+__global__ void axpby_kernel(T* __restrict__ x, T a, const T* __restrict__ y, T b, long long n) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x)
+    x[i] = a * x[i] + b * y[i];
+}
+template <typename T>
+void launch_axpby(T* x, T a, const T* y, T b, long long n, cudaStream_t st) {
+  axpby_kernel<T><<<vec_blocks(n), 256, 0, st>>>(x, a, y, b, n);
+}
+
+template <typename TD, typename TS>
+__global__ void convert_kernel(TD* __restrict__ d, const TS* __restrict__ s, long long n) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x)
+    d[i] = (TD)s[i];
+}
+template <typename TD, typename TS>
+void launch_convert(TD* dst, const TS* src, long long n, cudaStream_t st) {
+  convert_kernel<TD, TS><<<vec_blocks(n), 256, 0, st>>>(dst, src, n);
+}
+
+// Reset the scalars of a nested (coarse-level) PCG: no convergence test,
+// a fixed iteration count, and the parent's halt flag so a halted outer
+// iteration skips the nested one too.
+__global__ void scalars_init_kernel(PcgScalars* s, const PcgScalars* parent, int max_iter) {
+  s->rz = 0.0; s->rz_prev = 0.0; s->pAp = 0.0; s->alpha = 0.0; s->beta = 0.0; s->rr = 0.0;
+  s->bnorm = 1.0; s->relres = 0.0; s->best_rel = INFINITY; s->tol = 0.0;
+  s->halt = parent ? *((volatile const int*)&parent->halt) : 0;
+  s->status = 0; s->iter = 0; s->max_iter = max_iter; s->cadence = 0; s->test_now = 0;
+}
+void launch_scalars_init(PcgScalars* s, const PcgScalars* parent, int max_iter, cudaStream_t st) {
+  scalars_init_kernel<<<1, 1, 0, st>>>(s, parent, max_iter);
+}
+
+#define INST(T)                                                                                 \
+  template void launch_fill<T>(T*, T, long long, cudaStream_t);                                 \
+  template void launch_copy<T>(T*, const T*, long long, cudaStream_t);                          \
+  template void launch_diag<T>(const Grid&, const Mask&, const T*, const ModalK<T>&, int, T, T*, \
+                               T*, cudaStream_t);                                               \
+  template void launch_dot<T>(const T*, const T*, const T*, const T*, long long, const RedArgs&, \
+                              int, const int*, cudaStream_t);                                   \
+  template void launch_pcg_update<T>(T*, T*, T*, const T*, const T*, const T*, long long,        \
+                                     const RedArgs&, int, const PcgScalars*, cudaStream_t);      \
+  template void launch_p_update<T>(T*, const T*, long long, const PcgScalars*, cudaStream_t);    \
+  template void launch_jacobi_precond<T>(T*, const T*, const T*, long long, const RedArgs&, int, \
+                                         const int*, cudaStream_t);                             \
+  template void launch_axpby<T>(T*, T, const T*, T, long long, cudaStream_t);
+INST(double)
+INST(float)
+#undef INST
+template void launch_mask_copy<double, double>(const Grid&, const Mask&, double*, const double*,
+                                               cudaStream_t);
+template void launch_mask_copy<float, float>(const Grid&, const Mask&, float*, const float*,
+                                             cudaStream_t);
+template void launch_mask_copy<double, float>(const Grid&, const Mask&, double*, const float*,
+                                              cudaStream_t);
+template void launch_mask_copy<float, double>(const Grid&, const Mask&, float*, const double*,
+                                              cudaStream_t);
+template void launch_convert<float, double>(float*, const double*, long long, cudaStream_t);
+template void launch_convert<double, float>(double*, const float*, long long, cudaStream_t);
+
+}  // namespace hexa

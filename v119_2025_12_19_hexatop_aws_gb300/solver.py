@@ -1,0 +1,181 @@
+"""Host-side mirror of the reference's solve entry points.
+
+``solve_system_gpu`` keeps the signature, argument meaning and return
+convention of ``GPUSolver.solve_system_gpu`` (src/Solvers/GPUSolver.jl:467-477)
+and ``solve_system`` those of ``Solver.solve_system`` for the ``gpu`` solver
+type (src/Solvers/Solver.jl:39-160).  Both reach the C ABI (libhexagpu.so);
+there is no CPU path behind them.
+
+Config keys read (configs/default.yaml:209-237, GPUSolver.jl:187-231):
+``solver_parameters.{tolerance, max_iterations, diagonal_shift_factor,
+preconditioner, stagnation_tolerance, max_shift_attempts, shift_multiplier}``,
+``hardware_profile_applied`` / ``force_float64`` (precision) and
+``geometry.d*_computed``.  Optional new keys under ``solver_parameters``:
+``precision`` (fp64 | mixed | fp32), ``mg_levels``, ``smoother_sweeps``,
+``jacobi_omega``, ``coarse_iterations``, ``inner_tolerance``,
+``use_cuda_graphs``.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import warnings
+
+import numpy as np
+
+from . import _lib
+from .boundary import bc_to_fixed_dof, face_clamps
+from .mesh import structured_dims
+
+_CTX: _lib.Context | None = None
+
+
+def context(device: int = 0) -> _lib.Context:
+    """Process-wide context, like the reference's GLOBAL_CG_CACHE (GPUSolver.jl:63)."""
+    global _CTX
+    if _CTX is None or _CTX.h is None:
+        _CTX = _lib.Context(device)
+    return _CTX
+
+
+def precision_from_config(config: dict) -> str:
+    """GPUSolver.jl:187-189: FP64 for the H200/V100/A100 profiles or force_float64."""
+    sp = config.get("solver_parameters", {}) or {}
+    if "precision" in sp:
+        return str(sp["precision"]).lower()
+    prof = config.get("hardware_profile_applied", "RTX")
+    use_double = prof in ("H200", "V100", "A100") or bool(config.get("force_float64", False))
+    return "fp64" if use_double else "fp32"
+
+
+def params_from_config(config: dict, *, nu: float, tol: float, max_iter: int, shift_factor: float) -> _lib.SolveParams:
+    sp = config.get("solver_parameters", {}) or {}
+    kw = dict(
+        nu=float(nu), tol=float(tol), max_iter=int(max_iter), shift_factor=float(shift_factor),
+        precond="multigrid" if str(sp.get("preconditioner", "jacobi")).lower() == "multigrid" else "jacobi",
+        stagnation_tol=float(sp.get("stagnation_tolerance", 0.0)),
+        max_shift_attempts=int(sp.get("max_shift_attempts", 3)),
+        shift_multiplier=float(sp.get("shift_multiplier", 10.0)),
+        precision=precision_from_config(config),
+    )
+    opt = {"mg_levels": "mg_levels", "jacobi_omega": "jacobi_omega", "coarse_iterations": "coarse_iters",
+           "inner_tolerance": "inner_tol", "check_cadence": "check_cadence", "diag_quirk": "diag_quirk",
+           "graph_iterations": "graph_iters"}
+    for key, field in opt.items():
+        if key in sp:
+            kw[field] = sp[key]
+    if "smoother_sweeps" in sp:
+        kw["pre_smooth"] = kw["post_smooth"] = int(sp["smoother_sweeps"])
+    if "use_cuda_graphs" in sp:
+        kw["use_graphs"] = int(bool(sp["use_cuda_graphs"]))
+    return _lib.default_params(**kw)
+
+
+def solve(grid: _lib.Grid, factor, f, *, clamp_faces: int = 0, fixed_dof=None, params: _lib.SolveParams | None = None,
+          u_guess=None, u_out=None, ctx: _lib.Context | None = None):
+    """Solve (K_ff(factor) + sigma I) u = f_free on the structured grid.
+
+    factor: nElem modulus factors (float64); f: 3*nNodes forces (float64);
+    arrays may be numpy (host) or torch CUDA tensors (device, used in place).
+    Returns (u, stats dict)."""
+    ctx = ctx or context()
+    params = params or _lib.default_params()
+    ndof = 3 * (grid.nx + 1) * (grid.ny + 1) * (grid.nz + 1)
+    if u_out is None:
+        u_out = np.empty(ndof, dtype=np.float64)
+    bc = _lib.make_bc(clamp_faces, fixed_dof)
+    st = _lib.SolveStats()
+    rc = ctx.lib.hexa_solve(ctx.h, C.byref(grid), C.byref(bc), _lib.ptr(factor), _lib.ptr(f), C.byref(params),
+                            _lib.ptr(u_guess), _lib.ptr(u_out), C.byref(st))
+    ctx.check(rc)
+    return u_out, st.as_dict()
+
+
+def solve_system_gpu(nodes, elements, E, nu, bc, f, density, *, max_iter=40000, tol=1e-6, method="native",
+                     solver="cg", use_precond=True, shift_factor=1.0e-4, min_stiffness_threshold=1.0e-3,
+                     u_guess=None, config=None):
+    """Drop-in for GPUSolver.solve_system_gpu: returns (u::Float64[3nNodes], relres, name).
+
+    name is "GMG_GPU", "Jacobi_GPU" or "Failed_Corrupt_Input" (GPUSolver.jl:314,463)."""
+    config = config or {}
+    nx, ny, nz, dx, dy, dz = structured_dims(nodes, elements)
+    geom = config.get("geometry", {}) or {}
+    dx = float(geom.get("dx_computed", dx))
+    dy = float(geom.get("dy_computed", dy))
+    dz = float(geom.get("dz_computed", dz))
+    grid = _lib.make_grid(nx, ny, nz, dx, dy, dz)
+    params = params_from_config(config, nu=nu, tol=tol, max_iter=max_iter, shift_factor=shift_factor)
+    ctx = context()
+    fixed = bc_to_fixed_dof(bc)
+    faces, rest = face_clamps(fixed, nx, ny, nz)
+    # the reference promotes Float32(E*density) (GPUSolver.jl:254)
+    factor = (np.float32(E) * np.asarray(density, dtype=np.float32)).astype(np.float64)
+    fvec = np.ascontiguousarray(np.asarray(f, dtype=np.float32).astype(np.float64))
+    guess = None
+    if u_guess is not None and len(u_guess) > 0:
+        guess = np.ascontiguousarray(np.asarray(u_guess, dtype=np.float64))
+    u = np.empty(3 * (nx + 1) * (ny + 1) * (nz + 1), dtype=np.float64)
+    bcs = _lib.make_bc(faces, rest)
+    st = _lib.SolveStats()
+    rc = ctx.lib.hexa_solve(ctx.h, C.byref(grid), C.byref(bcs), _lib.ptr(factor), _lib.ptr(fvec), C.byref(params),
+                            _lib.ptr(guess), _lib.ptr(u), C.byref(st))
+    if rc == _lib.HEXA_ERR_CORRUPT_INPUT:
+        return np.zeros(u.shape[0], dtype=np.float64), float("nan"), "Failed_Corrupt_Input"
+    ctx.check(rc)
+    name = "GMG_GPU" if st.precond_used == 1 else "Jacobi_GPU"
+    return u, float(st.relres), name
+
+
+def solve_system(nodes, elements, E, nu, bc_indicator, F, *, density, config, min_stiffness_threshold=1.0e-3,
+                 prune_voids=True, u_prev=None):
+    """Solver.solve_system for solver_type "gpu" (Solver.jl:39-160).
+
+    The tolerance is cast to Float32 as the reference does (Solver.jl:57).
+    Void pruning (MeshPruner) produces unstructured meshes the structured
+    kernels cannot take, so it is not performed; the reference itself skips it
+    while current_outer_iter < 3 (Solver.jl:67-72)."""
+    sp = config["solver_parameters"]
+    stype = str(sp.get("solver_type", "direct")).lower()
+    if stype != "gpu":
+        raise NotImplementedError(f"solver_type {stype!r}: this library implements the 'gpu' solve path only")
+    tol = float(np.float32(sp.get("tolerance", 1.0e-6)))
+    max_iter = int(sp.get("max_iterations", 1000))
+    shift = float(np.float32(sp.get("diagonal_shift_factor", 1.0e-6)))
+    if prune_voids and int(config.get("current_outer_iter", 1)) >= 3:
+        warnings.warn("prune_voids ignored: the structured GPU path solves the full grid", stacklevel=2)
+    return solve_system_gpu(nodes, elements, np.float32(E), np.float32(nu), bc_indicator, F, density,
+                            max_iter=max_iter, tol=tol, shift_factor=shift,
+                            min_stiffness_threshold=min_stiffness_threshold, u_guess=u_prev, config=config)
+
+
+def apply_operator(grid, factor, x, *, nu=0.3, sigma=0.0, clamp_faces=0, fixed_dof=None, ctx=None, fp32=False):
+    """y = (K_ff + sigma I) x with y = 0 at fixed DOFs (one operator launch)."""
+    ctx = ctx or context()
+    bc = _lib.make_bc(clamp_faces, fixed_dof)
+    dt = np.float32 if fp32 else np.float64
+    y = np.empty(3 * (grid.nx + 1) * (grid.ny + 1) * (grid.nz + 1), dtype=dt) if isinstance(x, np.ndarray) else None
+    if y is None:
+        import torch
+        y = torch.empty_like(x)
+    fn = ctx.lib.hexa_apply_operator_f32 if fp32 else ctx.lib.hexa_apply_operator
+    rc = fn(ctx.h, C.byref(grid), C.byref(bc), float(nu), _lib.ptr(factor), _lib.ptr(x), float(sigma), _lib.ptr(y))
+    ctx.check(rc, allow=(_lib.HEXA_OK,))
+    return y
+
+
+def operator_diagonal(grid, factor, *, nu=0.3, clamp_faces=0, fixed_dof=None, diag_quirk=1, ctx=None):
+    ctx = ctx or context()
+    bc = _lib.make_bc(clamp_faces, fixed_dof)
+    d = np.empty(3 * (grid.nx + 1) * (grid.ny + 1) * (grid.nz + 1), dtype=np.float64)
+    rc = ctx.lib.hexa_operator_diagonal(ctx.h, C.byref(grid), C.byref(bc), float(nu), _lib.ptr(factor),
+                                        int(diag_quirk), _lib.ptr(d))
+    ctx.check(rc, allow=(_lib.HEXA_OK,))
+    return d
+
+
+def canonical_stiffness(dx=1.0, dy=1.0, dz=1.0, nu=0.3) -> np.ndarray:
+    """Element.get_canonical_stiffness (24x24, E = 1)."""
+    k = np.empty(576, dtype=np.float64)
+    rc = _lib.load().hexa_canonical_stiffness(float(dx), float(dy), float(dz), float(nu), _lib.ptr(k))
+    if rc != 0:
+        raise ValueError("invalid element geometry or Poisson ratio")
+    return k.reshape(24, 24, order="F")
