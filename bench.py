@@ -291,7 +291,8 @@ def run_ours(a):
     facf, xf, bf = f32(fac_d), f32(u_d), f32(f_d)
     yf = torch.empty_like(xf)
     modes = {"apply": (0, 8 * ndof + 4 * nelem), "apply_dot": (1, 8 * ndof + 4 * nelem),
-             "residual": (2, 12 * ndof + 4 * nelem), "jacobi": (4, 12 * ndof + 4 * nelem)}
+             "residual": (2, 12 * ndof + 4 * nelem), "jacobi": (4, 12 * ndof + 4 * nelem),
+             "chebyshev": (5, 16 * ndof + 4 * nelem)}
     kern = {}
     for name, (mode, nbytes) in modes.items():
         t = C.c_double()
@@ -305,12 +306,12 @@ def run_ours(a):
                                          C.byref(t64)), allow=(_lib.HEXA_OK,))
     kern["apply_fp64"] = {"ms": t64.value, "bytes": 16 * ndof + 8 * nelem,
                           "gbs": (16 * ndof + 8 * nelem) / (t64.value * 1e-3) / 1e9}
-    dom = kern["jacobi"]
+    dom = kern["chebyshev"]
     traffic = None
     if TRAFFIC_FILE.exists():
-        traffic = json.loads(TRAFFIC_FILE.read_text()).get(a.config, {}).get("jacobi_fp32_bytes_per_launch")
+        traffic = json.loads(TRAFFIC_FILE.read_text()).get(a.config, {}).get("cheb2_fp32_bytes_per_launch")
     roof = {"bound": "hbm", "achieved": round(dom["gbs"], 1), "peak": peak, "unit": "GB/s",
-            "frac": round(dom["gbs"] / peak, 4), "traffic": traffic, "kernel": "op_kernel<float, OP_JACOBI>",
+            "frac": round(dom["gbs"] / peak, 4), "traffic": traffic, "kernel": "op_kernel<float, OP_CHEB2>",
             "peak_source": peak_kind, "algorithmic_bytes_per_launch": dom["bytes"]}
 
     cpu = None

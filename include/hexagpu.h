@@ -151,7 +151,8 @@ int hexa_apply_operator_f32(hexa_ctx* ctx, const hexa_grid* g, const hexa_bc* bc
  * context's stream with CUDA events (inputs already on the device) and
  * returns the mean launch duration in ms.  precision: HEXA_PREC_FP64 or
  * HEXA_PREC_FP32 (factor/x/y then float).  mode: 0 y = Ax, 1 y = Ax with
- * x.Ax, 2 y = b - Ax, 4 y = x + omega (b - Ax)/diag (damped Jacobi). */
+ * x.Ax, 2 y = b - Ax, 4 y = x + omega (b - Ax)/diag (damped Jacobi), 5 one
+ * Chebyshev step written over its previous iterate (y). */
 int hexa_time_operator(hexa_ctx* ctx, const hexa_grid* g, const hexa_bc* bc, double nu, int32_t precision,
                        int32_t mode, const void* factor, const void* x, const void* b, void* y, int32_t reps,
                        double* avg_ms);

@@ -18,7 +18,7 @@ def test_filter_matches_exact(ctx, oracle, rng, dims, quirk):
     R = 0.6
     ref = oracle.helmholtz_direct(g, rho, R, quirk=quirk)
     out, st = filter_density(_lib.make_grid(*dims), rho, R, tol=1e-14, max_iter=5000, quirk=quirk, ctx=ctx)
-    assert np.abs(out - ref).max() <= 1e-11 * np.abs(ref).max()
+    assert np.abs(out - ref).max() <= 1e-10 * np.abs(ref).max()
 
 
 def test_filter_follows_reference_loop(ctx, oracle, rng):

@@ -138,8 +138,8 @@ void hexa_default_params(hexa_solve_params* p) {
   p->mg_levels = 0;
   p->pre_smooth = 2;
   p->post_smooth = 2;
-  p->smoother = HEXA_SMOOTH_JACOBI;
-  p->jacobi_omega = 0.6;
+  p->smoother = HEXA_SMOOTH_CHEBYSHEV;
+  p->jacobi_omega = 0.0;        // 0: 1.2 / (element bound on lambda_max(D^-1 A))
   p->cheb_degree = 2;
   p->coarse_iters = 30;
   p->inner_tol = 1e-4;
@@ -271,6 +271,8 @@ static int apply_operator_t(hexa_ctx* h, const hexa_grid* g, const hexa_bc* bc, 
   if (nch > G.NZ) nch = G.NZ;
   a.kchunk = (int)std::max<long long>(2, (G.NZ + nch - 1) / nch);
   a.diag_quirk = 0;
+  a.xin = nullptr;
+  a.c1 = a.c2 = T(0);
   a.red.partials = c.partials;
   a.red.ticket = c.ticket;
   a.red.dst = nullptr;
@@ -314,7 +316,7 @@ static int time_operator_t(hexa_ctx* h, const hexa_grid* g, const hexa_bc* bc, d
   if (!build_modal(g->dx, g->dy, g->dz, nu, &K64, &e)) return set_err(h, HEXA_ERR_ARG, e);
   if (!is_device_ptr(factor) || !is_device_ptr(x) || !is_device_ptr(y) || (b && !is_device_ptr(b)))
     return set_err(h, HEXA_ERR_ARG, "hexa_time_operator takes device arrays");
-  if ((mode == OP_RESID || mode == OP_JACOBI) && !b) return set_err(h, HEXA_ERR_ARG, "mode needs b");
+  if ((mode == OP_RESID || mode == OP_JACOBI || mode == OP_CHEB2) && !b) return set_err(h, HEXA_ERR_ARG, "mode needs b");
   const Grid G = make_grid(g->nx, g->ny, g->nz);
   Mask m;
   m.faces = bc ? bc->clamp_faces : 0u;
@@ -330,12 +332,19 @@ static int time_operator_t(hexa_ctx* h, const hexa_grid* g, const hexa_bc* bc, d
   else a.K = modal_to_f32(K64);
   a.sigma = T(0);
   a.omega = T(0.6);
+  if (mode == OP_CHEB2) {  // in place over the previous iterate, as in the V-cycle
+    a.xin = y;
+    a.c1 = T(0.5);
+    a.c2 = T(0.3);
+  }
   const int tyw = sizeof(T) == 8 ? 8 : 16;
   const long long bxy = (long long)((G.NX + 30) / 31) * ((G.NY + tyw - 2) / (tyw - 1));
   long long nch = ((sizeof(T) == 8 ? 456 : 304) + bxy - 1) / bxy;
   if (nch > G.NZ) nch = G.NZ;
   a.kchunk = (int)std::max<long long>(2, (G.NZ + nch - 1) / nch);
   a.diag_quirk = 1;
+  a.xin = nullptr;
+  a.c1 = a.c2 = T(0);
   const long long nb = op_num_blocks<T>(G, a.kchunk);
   if (!c.ensure_partials((size_t)nb * 2 + 64)) return HEXA_ERR_NOMEM;
   a.red.partials = c.partials;
@@ -363,7 +372,7 @@ extern "C" {
 int hexa_time_operator(hexa_ctx* h, const hexa_grid* g, const hexa_bc* bc, double nu, int32_t precision, int32_t mode,
                        const void* factor, const void* x, const void* b, void* y, int32_t reps, double* avg_ms) {
   if (!h) return HEXA_ERR_ARG;
-  if (!valid_grid(g) || !factor || !x || !y || !avg_ms || reps < 1 || mode < 0 || mode > 4)
+  if (!valid_grid(g) || !factor || !x || !y || !avg_ms || reps < 1 || mode < 0 || mode > 5)
     return set_err(h, HEXA_ERR_ARG, "invalid arguments");
   h->c.err.clear();
   cudaSetDevice(h->c.device);

@@ -176,7 +176,7 @@ int modal_blocks(const double* ke, ModalK<double>* out, double* max_dropped) {
       H[m][cc] = v;
     }
   // M'[(m,c),(m2,c2)] = sum_{n,n2} H[m][n] K[(n,c),(n2,c2)] H[m2][n2] / 64
-  static double M[24][24];
+  double M[24][24];
   double kmax = 0.0;
   for (int i = 0; i < 576; ++i) kmax = std::fmax(kmax, std::fabs(ke[i]));
   for (int m = 0; m < 8; ++m)
@@ -211,6 +211,37 @@ int modal_blocks(const double* ke, ModalK<double>* out, double* max_dropped) {
   for (int c = 0; c < 3; ++c) out->dd[c] = ke[c + 24 * c];
   if (max_dropped) *max_dropped = dropped / (kmax > 0 ? kmax : 1.0);
   return (dropped <= 1e-12 * kmax) ? 0 : -3;
+}
+
+double smoother_bound(const double* ke, int quirk) {
+  double S[24][24];
+  for (int r = 0; r < 24; ++r)
+    for (int c = 0; c < 24; ++c) {
+      const double dr = quirk ? ke[(3 * (r / 3)) * 25] : ke[r * 25];
+      const double dc = quirk ? ke[(3 * (c / 3)) * 25] : ke[c * 25];
+      S[r][c] = ke[r + 24 * c] / std::sqrt(dr * dc);
+    }
+  // power iteration on the symmetric positive semidefinite S
+  double v[24], w[24], lam = 0.0;
+  for (int i = 0; i < 24; ++i) v[i] = 1.0 + 0.01 * i * ((i & 1) ? -1 : 1);
+  for (int it = 0; it < 500; ++it) {
+    double nrm = 0.0;
+    for (int i = 0; i < 24; ++i) {
+      double t = 0.0;
+      for (int j = 0; j < 24; ++j) t += S[i][j] * v[j];
+      w[i] = t;
+      nrm += t * t;
+    }
+    nrm = std::sqrt(nrm);
+    if (nrm == 0.0) break;
+    double num = 0.0;
+    for (int i = 0; i < 24; ++i) num += v[i] * w[i];
+    double vv = 0.0;
+    for (int i = 0; i < 24; ++i) vv += v[i] * v[i];
+    lam = num / vv;
+    for (int i = 0; i < 24; ++i) v[i] = w[i] / nrm;
+  }
+  return lam;
 }
 
 void helm_corner_matrix(const double* Ke, const double* Me, double R, double A[8][8]) {

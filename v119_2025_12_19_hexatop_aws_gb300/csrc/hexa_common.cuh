@@ -117,7 +117,10 @@ __device__ __forceinline__ void finalize_scalars(const RedArgs& r, const double*
       break;
     case FIN_PCG_ALPHA: {
       s->pAp = tot[0];
-      if (fabs(tot[0]) < 1e-20) {  // GPUSolver.jl:374 `abs(denom) < 1e-20; break`
+      // GPUSolver.jl:374 stops on the absolute test |p.Ap| < 1e-20, which ends
+      // tight solves of unit-load problems early; for the SPD (K + sigma I)
+      // only non-positive (or NaN) curvature is a breakdown here.
+      if (!(tot[0] > 0.0)) {
         s->status = 4;
         s->halt = 1;
         s->alpha = 0.0;

@@ -8,7 +8,14 @@
 namespace hexa {
 
 // ---------------------------------------------------------------- operator
-enum OpMode { OP_APPLY = 0, OP_APPLY_DOT = 1, OP_RESID = 2, OP_RESID_NORM = 3, OP_JACOBI = 4 };
+enum OpMode {
+  OP_APPLY = 0,       // y = Ax
+  OP_APPLY_DOT = 1,   // y = Ax, sum x.Ax
+  OP_RESID = 2,       // y = b - Ax
+  OP_RESID_NORM = 3,  // y = b - Ax, sum y.y
+  OP_JACOBI = 4,      // y = x + omega D^-1 (b - Ax)
+  OP_CHEB2 = 5,       // y = x + c1 (x - xin) + c2 D^-1 (b - Ax)   (xin null: 0; y may alias xin)
+};
 
 template <typename T>
 struct OpArgs {
@@ -18,6 +25,8 @@ struct OpArgs {
   const T* fac;   // element factors (nelem)
   const T* b;     // right-hand side (RESID*, JACOBI)
   T* y;           // output (must not alias x)
+  const T* xin;   // Chebyshev: previous iterate (nullable = 0)
+  T c1, c2;       // Chebyshev step coefficients
   ModalK<T> K;
   T sigma;        // diagonal shift
   T omega;        // Jacobi damping

@@ -12,7 +12,8 @@
 // four columns around a node are summed with one warp shuffle (x) and one
 // shared-memory exchange (y); no atomics anywhere, so y is bitwise
 // reproducible.  Fixed DOFs are masked in-kernel (no free-DOF map), and the
-// epilogue fuses the PCG dot, the residual b - Ax, or a damped-Jacobi step.
+// epilogue fuses the PCG dot, the residual b - Ax, a damped-Jacobi step or a
+// Chebyshev step.
 #include "hexa_common.cuh"
 #include "hexa_kernels.h"
 
@@ -114,7 +115,7 @@ template <typename T, int MODE, int TYW>
 __global__ void __launch_bounds__(32 * TYW) op_kernel(const OpArgs<T> a) {
   if (a.halt && *((volatile const int*)a.halt)) return;
   constexpr int NX_OWN = 31, NY_OWN = TYW - 1;
-  constexpr bool NEED_F = (MODE == OP_JACOBI);
+  constexpr bool NEED_F = (MODE == OP_JACOBI || MODE == OP_CHEB2);
   __shared__ T xch[2][TYW][32][NEED_F ? 4 : 3];
 
   const Grid g = a.g;
@@ -220,9 +221,14 @@ __global__ void __launch_bounds__(32 * TYW) op_kernel(const OpArgs<T> a) {
         } else if (MODE == OP_RESID || MODE == OP_RESID_NORM) {
           out = fixd ? T(0) : (ldx(a.b + 3 * n + c) - Ax);
           if (MODE == OP_RESID_NORM) acc0 += (double)out * (double)out;
-        } else {  // OP_JACOBI: x + omega (b - Ax) / D
+        } else if (MODE == OP_JACOBI) {  // x + omega (b - Ax) / D
           const T d = fma(a.K.dd[a.diag_quirk ? 0 : c], fsum, a.sigma);
           out = fixd ? T(0) : fma(a.omega, (ldx(a.b + 3 * n + c) - Ax) / d, xown[c]);
+        } else {  // OP_CHEB2: x + c1 (x - x_prev) + c2 D^-1 (b - Ax)
+          const T d = fma(a.K.dd[a.diag_quirk ? 0 : c], fsum, a.sigma);
+          const T xp = a.xin ? a.xin[3 * n + c] : T(0);  // plain load: y may alias xin
+          const T t = fma(a.c1, xown[c] - xp, xown[c]);
+          out = fixd ? T(0) : fma(a.c2, (ldx(a.b + 3 * n + c) - Ax) / d, t);
         }
         a.y[3 * n + c] = out;
       }
@@ -273,6 +279,7 @@ void launch_op(int mode, const OpArgs<T>& a, cudaStream_t st) {
     case OP_RESID: op_kernel<T, OP_RESID, TYW><<<grid, block, 0, st>>>(a); break;
     case OP_RESID_NORM: op_kernel<T, OP_RESID_NORM, TYW><<<grid, block, 0, st>>>(a); break;
     case OP_JACOBI: op_kernel<T, OP_JACOBI, TYW><<<grid, block, 0, st>>>(a); break;
+    case OP_CHEB2: op_kernel<T, OP_CHEB2, TYW><<<grid, block, 0, st>>>(a); break;
     default: break;
   }
 }

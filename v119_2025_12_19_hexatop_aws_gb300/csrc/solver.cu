@@ -141,6 +141,25 @@ struct MG {
   int quirk = 0;
   T omega = T(0.6);
   int nu1 = 2, nu2 = 2, citers = 30;
+  int smoother = HEXA_SMOOTH_CHEBYSHEV;
+  // Chebyshev on [lmax/30, lmax] of D^-1 A: d_0 = D^-1 r / theta,
+  // d_s = c1[s] d_{s-1} + c2[s] D^-1 r_s
+  T inv_theta = T(0);
+  std::vector<T> c1, c2;
+
+  void set_chebyshev(double lmax, int nmax) {
+    const double lmin = lmax / 30.0, th = 0.5 * (lmax + lmin), de = 0.5 * (lmax - lmin), sg = th / de;
+    double rho = 1.0 / sg;
+    inv_theta = (T)(1.0 / th);
+    c1.assign(nmax + 1, T(0));
+    c2.assign(nmax + 1, T(0));
+    for (int s = 1; s <= nmax; ++s) {
+      const double rn = 1.0 / (2.0 * sg - rho);
+      c1[s] = (T)(rn * rho);
+      c2[s] = (T)(2.0 * rn / de);
+      rho = rn;
+    }
+  }
 };
 
 template <typename T>
@@ -160,6 +179,9 @@ OpArgs<T> opargs(const Lev<T>& L, const ModalK<T>& K, int quirk, const T* x, con
   a.diag_quirk = quirk;
   a.red = r;
   a.halt = halt;
+  a.xin = nullptr;
+  a.c1 = T(0);
+  a.c2 = T(0);
   return a;
 }
 
@@ -195,6 +217,7 @@ bool build_mg(Ctx& c, MG<T>& mg, const Grid& g0, const Mask& m0, const T* fac0, 
   L0.xb = c.vec<T>(tag + "xb0", n0);
   L0.r = c.vec<T>(tag + "r0", n0);
   if (!L0.xb || !L0.r) return false;
+
   mg.L.push_back(L0);
   for (int l = 1; l < nlev; ++l) {
     const Lev<T>& F = mg.L[l - 1];
@@ -276,17 +299,37 @@ void vcycle(Ctx& c, MG<T>& mg, int l, const T* b, T* xout, const int* halt) {
     coarse_solve<T>(c, mg, b, xout, halt);
     return;
   }
+  // x buffers alternate between xout and V.xb so that the last write lands in xout
   const int nw = mg.nu1 + mg.nu2;
   auto bufw = [&](int w) -> T* { return ((nw - 1 - w) % 2 == 0) ? xout : V.xb; };
   int w = 0;
   T* cur = bufw(w++);
-  launch_jacobi0<T>(V.g, V.m, V.fac, mg.K, mg.quirk, V.sigma, mg.omega, b, cur, halt, c.st);
-  c.launches++;
   RedArgs none = red(c, FIN_NONE, 1, nullptr);
-  for (int s = 1; s < mg.nu1; ++s) {
+  const bool cheb = mg.smoother == HEXA_SMOOTH_CHEBYSHEV;
+  // Chebyshev step s >= 1: x_{s+1} = x_s + c1 (x_s - x_{s-1}) + c2 D^-1 (b - A x_s),
+  // written over x_{s-1} (the buffer bufw() hands out next)
+  const T* prev = nullptr;
+  auto cheb_step = [&](int s) {
     T* nx = bufw(w++);
-    op<T>(c, OP_JACOBI, opargs<T>(V, mg.K, mg.quirk, cur, b, nx, mg.omega, halt, none));
+    OpArgs<T> a = opargs<T>(V, mg.K, mg.quirk, cur, b, nx, T(0), halt, none);
+    a.xin = prev;
+    a.c1 = mg.c1[s];
+    a.c2 = mg.c2[s];
+    op<T>(c, OP_CHEB2, a);
+    prev = cur;
     cur = nx;
+  };
+  // the first sweep from zero is D^-1 b scaled by omega (damped Jacobi) or 1/theta (Chebyshev)
+  launch_jacobi0<T>(V.g, V.m, V.fac, mg.K, mg.quirk, V.sigma, cheb ? mg.inv_theta : mg.omega, b, cur, halt, c.st);
+  c.launches++;
+  for (int s = 1; s < mg.nu1; ++s) {
+    if (cheb) {
+      cheb_step(s);
+    } else {
+      T* nx = bufw(w++);
+      op<T>(c, OP_JACOBI, opargs<T>(V, mg.K, mg.quirk, cur, b, nx, mg.omega, halt, none));
+      cur = nx;
+    }
   }
   op<T>(c, OP_RESID, opargs<T>(V, mg.K, mg.quirk, cur, b, V.r, mg.omega, halt, none));
   Lev<T>& C = mg.L[l + 1];
@@ -296,9 +339,14 @@ void vcycle(Ctx& c, MG<T>& mg, int l, const T* b, T* xout, const int* halt) {
   launch_prolong_add<T>(C.g, C.xa, V.g, V.m, cur, halt, c.st);
   c.launches++;
   for (int s = 0; s < mg.nu2; ++s) {
-    T* nx = bufw(w++);
-    op<T>(c, OP_JACOBI, opargs<T>(V, mg.K, mg.quirk, cur, b, nx, mg.omega, halt, none));
-    cur = nx;
+    if (cheb && s > 0) {
+      cheb_step(s);
+    } else {  // damped Jacobi, or the first Chebyshev step (omega = 1/theta)
+      T* nx = bufw(w++);
+      op<T>(c, OP_JACOBI, opargs<T>(V, mg.K, mg.quirk, cur, b, nx, cheb ? mg.inv_theta : mg.omega, halt, none));
+      prev = cur;
+      cur = nx;
+    }
   }
 }
 
@@ -514,6 +562,25 @@ double device_dot(Ctx& c, const double* a, const double* b, long long n, int slo
   return c.hscal[slot];
 }
 
+// Element bound on lambda_max(D^-1 A) for the smoothers (see smoother_bound).
+double smoother_lmax(const Problem& P, int quirk) {
+  double ke[576];
+  canonical_stiffness(P.dx, P.dy, P.dz, P.nu, ke);
+  return smoother_bound(ke, quirk);
+}
+
+template <typename T>
+void configure_mg(MG<T>& mg, const Problem& P, const hexa_solve_params& prm) {
+  mg.quirk = prm.diag_quirk;
+  const double lmax = smoother_lmax(P, prm.diag_quirk);
+  mg.smoother = prm.smoother;
+  mg.omega = (T)(prm.jacobi_omega > 0 ? prm.jacobi_omega : 1.2 / lmax);
+  mg.nu1 = prm.pre_smooth > 0 ? prm.pre_smooth : 1;
+  mg.nu2 = prm.post_smooth >= 0 ? prm.post_smooth : 2;
+  mg.citers = prm.coarse_iters >= 0 ? prm.coarse_iters : 30;
+  mg.set_chebyshev(lmax, std::max(mg.nu1, mg.nu2) + 1);
+}
+
 bool setup_common(Ctx& c, const Problem& P, const hexa_solve_params& prm, ModalK<double>* K64, double* max_diag,
                   double* bnorm) {
   std::string e;
@@ -602,11 +669,7 @@ int solve_plain(Ctx& c, const Problem& P, const hexa_solve_params& prm, const do
   if (want_mg) {
     nlev = plan_levels(P.g, prm.mg_levels);
     mg.K = K;
-    mg.quirk = prm.diag_quirk;
-    mg.omega = (T)(prm.jacobi_omega > 0 ? prm.jacobi_omega : 0.6);
-    mg.nu1 = prm.pre_smooth > 0 ? prm.pre_smooth : 1;
-    mg.nu2 = prm.post_smooth >= 0 ? prm.post_smooth : 2;
-    mg.citers = prm.coarse_iters >= 0 ? prm.coarse_iters : 30;
+    configure_mg<T>(mg, P, prm);
     if (!build_mg<T>(c, mg, P.g, P.m, fac, nlev, std::string(Is64<T>::v ? "mg64_" : "mg32_"))) return HEXA_ERR_NOMEM;
     mg.L[0].kchunk = L0.kchunk;
   }
@@ -778,11 +841,7 @@ int solve_mixed(Ctx& c, const Problem& P, const hexa_solve_params& prm, const do
   if (use_mg) {
     const int nlev = plan_levels(P.g, prm.mg_levels);
     mg.K = K32;
-    mg.quirk = prm.diag_quirk;
-    mg.omega = (float)(prm.jacobi_omega > 0 ? prm.jacobi_omega : 0.6);
-    mg.nu1 = prm.pre_smooth > 0 ? prm.pre_smooth : 1;
-    mg.nu2 = prm.post_smooth >= 0 ? prm.post_smooth : 2;
-    mg.citers = prm.coarse_iters >= 0 ? prm.coarse_iters : 30;
+    configure_mg<float>(mg, P, prm);
     if (!build_mg<float>(c, mg, P.g, P.m, fac32, nlev, "mg32_")) return HEXA_ERR_NOMEM;
     mg.L[0].kchunk = L0.kchunk;
     mg_set_shift<float>(c, mg, sigma);
@@ -823,7 +882,7 @@ int solve_mixed(Ctx& c, const Problem& P, const hexa_solve_params& prm, const do
       return HEXA_ERR_CUDA;
     inner_total += o.iters;
     applies32 += o.fine_applies;
-    if (o.status == 2 || o.iters == 0) {
+    if (o.status == 2 || o.status == 3 || o.iters == 0) {
       status = HEXA_NOT_CONVERGED;
       break;
     }
