@@ -265,11 +265,7 @@ static int apply_operator_t(hexa_ctx* h, const hexa_grid* g, const hexa_bc* bc, 
   else a.K = modal_to_f32(K64);
   a.sigma = sigma;
   a.omega = T(0);
-  const int tyw = sizeof(T) == 8 ? 8 : 16;
-  const long long bxy = (long long)((G.NX + 30) / 31) * ((G.NY + tyw - 2) / (tyw - 1));
-  long long nch = (456 + bxy - 1) / bxy;
-  if (nch > G.NZ) nch = G.NZ;
-  a.kchunk = (int)std::max<long long>(2, (G.NZ + nch - 1) / nch);
+  a.kchunk = op_pick_kchunk<T>(G);
   a.diag_quirk = 0;
   a.xin = nullptr;
   a.c1 = a.c2 = T(0);
@@ -337,11 +333,7 @@ static int time_operator_t(hexa_ctx* h, const hexa_grid* g, const hexa_bc* bc, d
     a.c1 = T(0.5);
     a.c2 = T(0.3);
   }
-  const int tyw = sizeof(T) == 8 ? 8 : 16;
-  const long long bxy = (long long)((G.NX + 30) / 31) * ((G.NY + tyw - 2) / (tyw - 1));
-  long long nch = ((sizeof(T) == 8 ? 456 : 304) + bxy - 1) / bxy;
-  if (nch > G.NZ) nch = G.NZ;
-  a.kchunk = (int)std::max<long long>(2, (G.NZ + nch - 1) / nch);
+  a.kchunk = op_pick_kchunk<T>(G);
   a.diag_quirk = 1;
   a.xin = nullptr;
   a.c1 = a.c2 = T(0);

@@ -30,7 +30,8 @@ struct OpArgs {
   ModalK<T> K;
   T sigma;        // diagonal shift
   T omega;        // Jacobi damping
-  int kchunk;     // node layers per CTA
+  int kchunk;     // node layers per work item
+  int tiles_x, tiles_y, nchunks;  // filled by launch_op
   int diag_quirk;
   RedArgs red;
   const int* halt;  // nullable: PcgScalars::halt
@@ -40,6 +41,9 @@ template <typename T>
 void launch_op(int mode, const OpArgs<T>& a, cudaStream_t st);
 template <typename T>
 long long op_num_blocks(const Grid& g, int kchunk);
+// node layers per work item so that every resident CTA gets ~8 items
+template <typename T>
+int op_pick_kchunk(const Grid& g);
 ModalK<float> modal_to_f32(const ModalK<double>& K);
 
 // ------------------------------------------------------------ vector passes

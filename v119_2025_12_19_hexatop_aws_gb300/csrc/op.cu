@@ -14,6 +14,8 @@
 // reproducible.  Fixed DOFs are masked in-kernel (no free-DOF map), and the
 // epilogue fuses the PCG dot, the residual b - Ax, a damped-Jacobi step or a
 // Chebyshev step.
+#include <algorithm>
+
 #include "hexa_common.cuh"
 #include "hexa_kernels.h"
 
@@ -33,19 +35,53 @@ __host__ __device__ constexpr bool modal_nz(int q, int c, int c2) {
 template <typename T>
 __device__ __forceinline__ T ldx(const T* p) { return __ldg(p); }
 
-// Corner cc = dx + 2*dy of the column (ie, je) at node layer kk; zeros outside.
-template <typename T>
-__device__ __forceinline__ void load_corners(const Grid& g, const T* __restrict__ x, int ie, int je,
-                                             int kk, T (&v)[4][3]) {
-  const bool kok = (kk >= 0) && (kk < g.NZ);
+// Addressing of one element column's four corner nodes (cc = dx + 2*dy):
+// x/y validity is fixed per thread, each node layer adds one plane offset.
+template <typename IX>
+struct ColumnAddr {
+  IX base;   // 3 * node index of corner 0 at layer 0
+  IX row3;   // 3 * NX: corner 2 is one node row up
+  IX plane3; // 3 * NX * NY
+  bool ok[4];
+};
+
+template <typename IX>
+__device__ __forceinline__ ColumnAddr<IX> column_addr(const Grid& g, int ie, int je) {
+  ColumnAddr<IX> a;
+  a.base = (IX)3 * ((IX)ie + (IX)g.NX * je);
+  a.row3 = (IX)3 * g.NX;
+  a.plane3 = (IX)3 * g.NX * g.NY;
 #pragma unroll
   for (int cc = 0; cc < 4; ++cc) {
     const int i = ie + (cc & 1), j = je + (cc >> 1);
-    const bool ok = kok && (i >= 0) && (i < g.NX) && (j >= 0) && (j < g.NY);
-    const long long n = ok ? ((long long)i + (long long)g.NX * ((long long)j + (long long)g.NY * kk)) : 0;
-#pragma unroll
-    for (int c = 0; c < 3; ++c) v[cc][c] = ok ? ldx(x + 3 * n + c) : T(0);
+    a.ok[cc] = (i >= 0) && (i < g.NX) && (j >= 0) && (j < g.NY);
   }
+  return a;
+}
+
+// Corner values of the column at node layer kk; zeros outside the grid.
+template <typename T, typename IX>
+__device__ __forceinline__ void load_corners(const Grid& g, const ColumnAddr<IX>& ca, const T* __restrict__ x, int kk,
+                                             T (&v)[4][3]) {
+  const bool kok = (kk >= 0) && (kk < g.NZ);
+  const IX lb = ca.base + ca.plane3 * (IX)kk;
+#pragma unroll
+  for (int cc = 0; cc < 4; ++cc) {
+    const bool ok = kok && ca.ok[cc];
+    const IX o = lb + ((cc & 1) ? 3 : 0) + ((cc >> 1) ? ca.row3 : (IX)0);
+#pragma unroll
+    for (int c = 0; c < 3; ++c) v[cc][c] = ok ? ldx(x + o + c) : T(0);
+  }
+}
+
+// 1/d for the smoothers: correctly rounded in FP32; in FP64 a float seed and
+// two Newton steps (relative error far below 1e-15, deterministic).
+__device__ __forceinline__ float recip(float d) { return __frcp_rn(d); }
+__device__ __forceinline__ double recip(double d) {
+  double r = (double)__frcp_rn((float)d);
+  r = r * fma(-d, r, 2.0);
+  r = r * fma(-d, r, 2.0);
+  return r;
 }
 
 // xy part of the Hadamard transform: corners (dx,dy) -> modes (mx,my), both
@@ -82,13 +118,15 @@ __device__ __forceinline__ void xy_inverse(const T (&m)[4][3], T (&v)[4][3]) {
 template <typename T>
 __device__ __forceinline__ void element_modal(const ModalK<T>& K, const T (&L)[4][3],
                                               const T (&U)[4][3], T f, T (&lo)[4][3], T (&hi)[4][3]) {
+  // z stage with the element factor folded in: f(L+U), f(U-L)
   T uh[8][3];
 #pragma unroll
   for (int mxy = 0; mxy < 4; ++mxy)
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
-      uh[mxy][c] = L[mxy][c] + U[mxy][c];
-      uh[mxy + 4][c] = U[mxy][c] - L[mxy][c];
+      const T fu = f * U[mxy][c];
+      uh[mxy][c] = fma(f, L[mxy][c], fu);
+      uh[mxy + 4][c] = fma(-f, L[mxy][c], fu);
     }
   T wh[8][3];
 #pragma unroll
@@ -100,7 +138,7 @@ __device__ __forceinline__ void element_modal(const ModalK<T>& K, const T (&L)[4
 #pragma unroll
       for (int c2 = 0; c2 < 3; ++c2)
         if (modal_nz(q, c, c2)) s = fma(K.B[q][c][c2], uh[q ^ (1 << c2)][c2], s);
-      wh[m][c] = s * f;
+      wh[m][c] = s;
     }
 #pragma unroll
   for (int mxy = 0; mxy < 4; ++mxy)
@@ -111,39 +149,48 @@ __device__ __forceinline__ void element_modal(const ModalK<T>& K, const T (&L)[4
     }
 }
 
-template <typename T, int MODE, int TYW>
-__global__ void __launch_bounds__(32 * TYW) op_kernel(const OpArgs<T> a) {
-  if (a.halt && *((volatile const int*)a.halt)) return;
+// One work item: the node columns of tile (tx, ty) for node layers [k0, k1).
+// IX is the index type: int whenever 3 * nNodes fits, which halves the
+// integer work of the address arithmetic.
+template <typename T, int MODE, int TYW, typename IX>
+__device__ __forceinline__ void op_item(const OpArgs<T>& a, int tx, int ty, int chunk,
+                                        T (&xch)[2][TYW][32][(MODE == OP_JACOBI || MODE == OP_CHEB2) ? 4 : 3],
+                                        double& acc0) {
   constexpr int NX_OWN = 31, NY_OWN = TYW - 1;
   constexpr bool NEED_F = (MODE == OP_JACOBI || MODE == OP_CHEB2);
-  __shared__ T xch[2][TYW][32][NEED_F ? 4 : 3];
-
-  const Grid g = a.g;
+  const Grid& g = a.g;
   const int lane = threadIdx.x, wy = threadIdx.y;
-  const int i0 = blockIdx.x * NX_OWN, j0 = blockIdx.y * NY_OWN;
-  const int k0 = blockIdx.z * a.kchunk;
+  const int i0 = tx * NX_OWN, j0 = ty * NY_OWN;
+  const int k0 = chunk * a.kchunk;
   const int k1 = min(k0 + a.kchunk, g.NZ);
   const int ie = i0 - 1 + lane, je = j0 - 1 + wy;
   const bool colv = (ie >= 0) && (ie < g.nx) && (je >= 0) && (je < g.ny);
-  const long long ecol = colv ? ((long long)ie + (long long)g.nx * je) : 0;
-  const long long eplane = (long long)g.nx * g.ny;
+  const IX ecol = colv ? ((IX)ie + (IX)g.nx * je) : (IX)0;
+  const IX eplane = (IX)g.nx * g.ny;
   const int in = i0 + lane, jn = j0 + wy;
   const bool own = (lane < NX_OWN) && (wy < NY_OWN) && (in < g.NX) && (jn < g.NY);
   const T* __restrict__ x = a.x;
   const T* __restrict__ fac = a.fac;
+  const ColumnAddr<IX> ca = column_addr<IX>(g, ie, je);
+  // Dirichlet bits of this thread's node column: the x/y faces are fixed per
+  // column, the z faces and the optional node mask are tested per layer
+  const uint32_t F = a.m.faces;
+  const unsigned colfix = (((F & 1u) && in == 0) || ((F & 2u) && in == g.NX - 1) || ((F & 4u) && jn == 0) ||
+                           ((F & 8u) && jn == g.NY - 1)) ? 7u : 0u;
+  const IX nplane = (IX)g.NX * g.NY;
+  const IX ncol = (IX)in + (IX)g.NX * jn;
 
   auto facload = [&](int k) -> T {
     return (colv && k >= 0 && k < g.nz) ? ldx(fac + ecol + eplane * k) : T(0);
   };
-
   T Lm[4][3], carry[4][3], xown[3];
   T fprev;
   {
     T raw[4][3];
-    load_corners<T>(g, x, ie, je, k0 - 1, raw);
+    load_corners<T, IX>(g, ca, x, k0 - 1, raw);
     T Lprev[4][3];
     xy_forward<T>(raw, Lprev);
-    load_corners<T>(g, x, ie, je, k0, raw);
+    load_corners<T, IX>(g, ca, x, k0, raw);
 #pragma unroll
     for (int c = 0; c < 3; ++c) xown[c] = raw[3][c];
     xy_forward<T>(raw, Lm);
@@ -152,11 +199,15 @@ __global__ void __launch_bounds__(32 * TYW) op_kernel(const OpArgs<T> a) {
     element_modal<T>(a.K, Lprev, Lm, fprev, lo, carry);
   }
 
-  double acc0 = 0.0;
+  // sums of this item in the kernel's own precision (one item is at most a
+  // few dozen layers per thread), folded into the FP64 accumulator at the end:
+  // FP64 arithmetic in the FP32 kernels would run at GB300's FP64 rate
+  T accT = T(0);
   T nraw[4][3];
-  load_corners<T>(g, x, ie, je, k0 + 1, nraw);
+  load_corners<T, IX>(g, ca, x, k0 + 1, nraw);
   T fnext = facload(k0);
 
+#pragma unroll 2
   for (int k = k0; k < k1; ++k) {
     T raw[4][3];
 #pragma unroll
@@ -165,7 +216,7 @@ __global__ void __launch_bounds__(32 * TYW) op_kernel(const OpArgs<T> a) {
       for (int c = 0; c < 3; ++c) raw[cc][c] = nraw[cc][c];
     const T f = fnext;
     if (k + 1 < k1) {  // prefetch the next layer
-      load_corners<T>(g, x, ie, je, k + 2, nraw);
+      load_corners<T, IX>(g, ca, x, k + 2, nraw);
       fnext = facload(k + 1);
     }
     T Um[4][3];
@@ -201,13 +252,24 @@ __global__ void __launch_bounds__(32 * TYW) op_kernel(const OpArgs<T> a) {
     if (NEED_F) xch[buf][wy][lane][NEED_F ? 3 : 0] = F1;
     __syncthreads();
     if (own) {
-      const long long n = (long long)in + (long long)g.NX * ((long long)jn + (long long)g.NY * k);
-      const unsigned fx = fixed_bits(g, a.m, in, jn, k, n);
+      const IX n = ncol + nplane * (IX)k;
+      unsigned fx = colfix;
+      if (((F & 16u) && k == 0) || ((F & 32u) && k == g.NZ - 1)) fx = 7u;
+      if (a.m.node) fx |= (unsigned)__ldg(a.m.node + n);
       T Kx[3];
 #pragma unroll
       for (int c = 0; c < 3; ++c) Kx[c] = T1[c] + xch[buf][wy + 1][lane][c];
-      T fsum = T(0);
-      if (NEED_F) fsum = F1 + xch[buf][wy + 1][lane][NEED_F ? 3 : 0];
+      T dinv[3] = {T(0), T(0), T(0)};
+      if (NEED_F) {
+        const T fsum = F1 + xch[buf][wy + 1][lane][NEED_F ? 3 : 0];
+        if (a.diag_quirk) {
+          const T r = recip(fma(a.K.dd[0], fsum, a.sigma));
+          dinv[0] = dinv[1] = dinv[2] = r;
+        } else {
+#pragma unroll
+          for (int c = 0; c < 3; ++c) dinv[c] = recip(fma(a.K.dd[c], fsum, a.sigma));
+        }
+      }
 #pragma unroll
       for (int c = 0; c < 3; ++c) {
         const bool fixd = (fx >> c) & 1u;
@@ -217,18 +279,16 @@ __global__ void __launch_bounds__(32 * TYW) op_kernel(const OpArgs<T> a) {
           out = fixd ? T(0) : Ax;
         } else if (MODE == OP_APPLY_DOT) {
           out = fixd ? T(0) : Ax;
-          acc0 += (double)xown[c] * (double)out;
+          accT = fma(xown[c], out, accT);
         } else if (MODE == OP_RESID || MODE == OP_RESID_NORM) {
           out = fixd ? T(0) : (ldx(a.b + 3 * n + c) - Ax);
-          if (MODE == OP_RESID_NORM) acc0 += (double)out * (double)out;
+          if (MODE == OP_RESID_NORM) accT = fma(out, out, accT);
         } else if (MODE == OP_JACOBI) {  // x + omega (b - Ax) / D
-          const T d = fma(a.K.dd[a.diag_quirk ? 0 : c], fsum, a.sigma);
-          out = fixd ? T(0) : fma(a.omega, (ldx(a.b + 3 * n + c) - Ax) / d, xown[c]);
+          out = fixd ? T(0) : fma(a.omega * dinv[c], ldx(a.b + 3 * n + c) - Ax, xown[c]);
         } else {  // OP_CHEB2: x + c1 (x - x_prev) + c2 D^-1 (b - Ax)
-          const T d = fma(a.K.dd[a.diag_quirk ? 0 : c], fsum, a.sigma);
           const T xp = a.xin ? a.xin[3 * n + c] : T(0);  // plain load: y may alias xin
           const T t = fma(a.c1, xown[c] - xp, xown[c]);
-          out = fixd ? T(0) : fma(a.c2, (ldx(a.b + 3 * n + c) - Ax) / d, t);
+          out = fixd ? T(0) : fma(a.c2 * dinv[c], ldx(a.b + 3 * n + c) - Ax, t);
         }
         a.y[3 * n + c] = out;
       }
@@ -237,6 +297,24 @@ __global__ void __launch_bounds__(32 * TYW) op_kernel(const OpArgs<T> a) {
     for (int c = 0; c < 3; ++c) xown[c] = raw[3][c];
   }
 
+  acc0 += (double)accT;
+  __syncthreads();  // the next item reuses xch
+}
+
+template <typename T, int MODE, int TYW, typename IX>
+__global__ void __launch_bounds__(32 * TYW) op_kernel(const OpArgs<T> a) {
+  if (a.halt && *((volatile const int*)a.halt)) return;
+  __shared__ T xch[2][TYW][32][(MODE == OP_JACOBI || MODE == OP_CHEB2) ? 4 : 3];
+  double acc0 = 0.0;
+  // static stride over (tile x, tile y, z-chunk) items: deterministic, and
+  // with the grid sized to the resident CTAs no wave is left half empty
+  const int nxy = a.tiles_x * a.tiles_y;
+  const int items = nxy * a.nchunks;
+  for (int item = blockIdx.x; item < items; item += gridDim.x) {
+    const int chunk = item / nxy, t = item - chunk * nxy;
+    const int ty = t / a.tiles_x, tx = t - ty * a.tiles_x;
+    op_item<T, MODE, TYW, IX>(a, tx, ty, chunk, xch, acc0);
+  }
   if (MODE == OP_APPLY_DOT || MODE == OP_RESID_NORM) {
     double v[1] = {acc0};
     block_reduce_finalize<1>(a.red, v);
@@ -256,38 +334,90 @@ static ModalK<T> cast_modal(const ModalK<double>& K) {
 template <typename T>
 constexpr int op_tyw() { return sizeof(T) == 8 ? 8 : 16; }
 
-template <typename T>
-dim3 op_grid(const Grid& g, int kchunk) {
-  constexpr int TYW = op_tyw<T>();
-  return dim3((g.NX + 30) / 31, (g.NY + TYW - 2) / (TYW - 1), (g.NZ + kchunk - 1) / kchunk);
+template <typename T, int MODE>
+static int op_resident_ctas() {
+  static int cached = 0;
+  if (!cached) {
+    int dev = 0, sms = 0, occ = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, op_kernel<T, MODE, op_tyw<T>(), long long>, 32 * op_tyw<T>(), 0);
+    cached = std::max(1, sms) * std::max(1, occ);
+  }
+  return cached;
 }
 
+template <typename T>
+static int resident_ctas(int mode) {
+  switch (mode) {
+    case OP_APPLY: return op_resident_ctas<T, OP_APPLY>();
+    case OP_APPLY_DOT: return op_resident_ctas<T, OP_APPLY_DOT>();
+    case OP_RESID: return op_resident_ctas<T, OP_RESID>();
+    case OP_RESID_NORM: return op_resident_ctas<T, OP_RESID_NORM>();
+    case OP_JACOBI: return op_resident_ctas<T, OP_JACOBI>();
+    default: return op_resident_ctas<T, OP_CHEB2>();
+  }
+}
+
+template <typename T>
+void op_tiles(const Grid& g, int kchunk, int* tx, int* ty, int* nch) {
+  constexpr int TYW = op_tyw<T>();
+  *tx = (g.NX + 30) / 31;
+  *ty = (g.NY + TYW - 2) / (TYW - 1);
+  *nch = (g.NZ + kchunk - 1) / kchunk;
+}
+
+// Largest CTA count any mode launches for this grid (sizes reduction partials).
 template <typename T>
 long long op_num_blocks(const Grid& g, int kchunk) {
-  dim3 d = op_grid<T>(g, kchunk);
-  return (long long)d.x * d.y * d.z;
+  int tx, ty, nch;
+  op_tiles<T>(g, kchunk, &tx, &ty, &nch);
+  return (long long)tx * ty * nch;
 }
 
 template <typename T>
-void launch_op(int mode, const OpArgs<T>& a, cudaStream_t st) {
+int op_pick_kchunk(const Grid& g) {
+  int tx, ty, nch;
+  op_tiles<T>(g, 1, &tx, &ty, &nch);
+  const long long tiles = (long long)tx * ty;
+  const long long want = 8LL * resident_ctas<T>(OP_CHEB2);  // ~8 items per CTA
+  long long chunks = (want + tiles - 1) / tiles;
+  chunks = std::max<long long>(1, std::min<long long>(chunks, (g.NZ + 15) / 16));  // chunks of >= 16 layers
+  return (int)((g.NZ + chunks - 1) / chunks);
+}
+
+template <typename T>
+void launch_op(int mode, const OpArgs<T>& a0, cudaStream_t st) {
   constexpr int TYW = op_tyw<T>();
-  const dim3 grid = op_grid<T>(a.g, a.kchunk);
+  OpArgs<T> a = a0;
+  op_tiles<T>(a.g, a.kchunk, &a.tiles_x, &a.tiles_y, &a.nchunks);
+  const long long items = (long long)a.tiles_x * a.tiles_y * a.nchunks;
+  const int grid = (int)std::min<long long>(items, resident_ctas<T>(mode));
   const dim3 block(32, TYW);
+  const bool i32 = a.g.ndof() < (1LL << 30) && a.g.nelem() < (1LL << 30);
+#define HEXA_OP_CASE(M)                                                              \
+  case M:                                                                           \
+    if (i32) op_kernel<T, M, TYW, int><<<grid, block, 0, st>>>(a);                  \
+    else op_kernel<T, M, TYW, long long><<<grid, block, 0, st>>>(a);                \
+    break;
   switch (mode) {
-    case OP_APPLY: op_kernel<T, OP_APPLY, TYW><<<grid, block, 0, st>>>(a); break;
-    case OP_APPLY_DOT: op_kernel<T, OP_APPLY_DOT, TYW><<<grid, block, 0, st>>>(a); break;
-    case OP_RESID: op_kernel<T, OP_RESID, TYW><<<grid, block, 0, st>>>(a); break;
-    case OP_RESID_NORM: op_kernel<T, OP_RESID_NORM, TYW><<<grid, block, 0, st>>>(a); break;
-    case OP_JACOBI: op_kernel<T, OP_JACOBI, TYW><<<grid, block, 0, st>>>(a); break;
-    case OP_CHEB2: op_kernel<T, OP_CHEB2, TYW><<<grid, block, 0, st>>>(a); break;
+    HEXA_OP_CASE(OP_APPLY)
+    HEXA_OP_CASE(OP_APPLY_DOT)
+    HEXA_OP_CASE(OP_RESID)
+    HEXA_OP_CASE(OP_RESID_NORM)
+    HEXA_OP_CASE(OP_JACOBI)
+    HEXA_OP_CASE(OP_CHEB2)
     default: break;
   }
+#undef HEXA_OP_CASE
 }
 
 template void launch_op<double>(int, const OpArgs<double>&, cudaStream_t);
 template void launch_op<float>(int, const OpArgs<float>&, cudaStream_t);
 template long long op_num_blocks<double>(const Grid&, int);
 template long long op_num_blocks<float>(const Grid&, int);
+template int op_pick_kchunk<double>(const Grid&);
+template int op_pick_kchunk<float>(const Grid&);
 template ModalK<float> cast_modal<float>(const ModalK<double>&);
 template ModalK<double> cast_modal<double>(const ModalK<double>&);
 

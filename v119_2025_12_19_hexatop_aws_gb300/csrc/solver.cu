@@ -98,15 +98,7 @@ struct Is64 { static constexpr bool v = sizeof(T) == 8; };
 
 template <typename T>
 int pick_kchunk(const Grid& g) {
-  const int tyw = Is64<T>::v ? 8 : 16;
-  const long long bxy = (long long)((g.NX + 30) / 31) * ((g.NY + tyw - 2) / (tyw - 1));
-  const long long target = Is64<T>::v ? 152LL * 3 : 152LL * 2;
-  long long nchunks = (target + bxy - 1) / bxy;
-  if (nchunks < 1) nchunks = 1;
-  if (nchunks > g.NZ) nchunks = g.NZ;
-  int kc = (int)((g.NZ + nchunks - 1) / nchunks);
-  if (kc < 2) kc = 2;
-  return kc;
+  return op_pick_kchunk<T>(g);
 }
 
 RedArgs red(Ctx& c, int op, int nsum, PcgScalars* s, double* dst = nullptr) {

@@ -20,6 +20,20 @@ static inline int vec_blocks(long long n, int threads = 256, int maxb = 152 * 8)
   return (int)b;
 }
 
+// Per-thread partial sums run in the vector's precision for kChunk terms and
+// are then folded into FP64: FP64 arithmetic per element would make the FP32
+// passes FP64-bound on GB300.
+constexpr int kChunk = 32;
+template <typename T, int NS>
+__device__ __forceinline__ void flush_parts(double (&acc)[NS], T (&part)[NS], int& cnt) {
+#pragma unroll
+  for (int q = 0; q < NS; ++q) {
+    acc[q] += (double)part[q];
+    part[q] = T(0);
+  }
+  cnt = 0;
+}
+
 template <typename T>
 __global__ void fill_kernel(T* v, T val, long long n) {
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
@@ -160,13 +174,17 @@ __global__ void dot_kernel(const T* __restrict__ a, const T* __restrict__ b, con
                            const T* __restrict__ d, long long n, RedArgs red, const int* halt) {
   if (halt && *((volatile const int*)halt)) return;
   double acc[NS];
+  T part[NS];
 #pragma unroll
-  for (int q = 0; q < NS; ++q) acc[q] = 0.0;
+  for (int q = 0; q < NS; ++q) acc[q] = 0.0, part[q] = T(0);
+  int cnt = 0;
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
        i += (long long)gridDim.x * blockDim.x) {
-    acc[0] += (double)a[i] * (double)b[i];
-    if (NS > 1) acc[NS - 1] += (double)c[i] * (double)d[i];
+    part[0] = fma(a[i], b[i], part[0]);
+    if (NS > 1) part[NS - 1] = fma(c[i], d[i], part[NS - 1]);
+    if (++cnt == kChunk) flush_parts<T, NS>(acc, part, cnt);
   }
+  flush_parts<T, NS>(acc, part, cnt);
   block_reduce_finalize<NS>(red, acc);
 }
 template <typename T>
@@ -183,22 +201,27 @@ __global__ void pcg_update_kernel(T* __restrict__ x, T* __restrict__ r, T* __res
                                   const PcgScalars* s) {
   if (*((volatile const int*)&s->halt)) return;
   const T alpha = (T)s->alpha;
-  double acc[JAC ? 2 : 1];
-  acc[0] = 0.0;
-  if (JAC) acc[JAC ? 1 : 0] = 0.0;
+  constexpr int NS = JAC ? 2 : 1;
+  double acc[NS];
+  T part[NS];
+#pragma unroll
+  for (int q2 = 0; q2 < NS; ++q2) acc[q2] = 0.0, part[q2] = T(0);
+  int cnt = 0;
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
        i += (long long)gridDim.x * blockDim.x) {
     x[i] = fma(alpha, p[i], x[i]);
     const T ri = fma(-alpha, q[i], r[i]);
     r[i] = ri;
-    acc[0] += (double)ri * (double)ri;
+    part[0] = fma(ri, ri, part[0]);
     if (JAC) {
       const T zi = ri * dinv[i];
       z[i] = zi;
-      acc[JAC ? 1 : 0] += (double)ri * (double)zi;
+      part[NS - 1] = fma(ri, zi, part[NS - 1]);
     }
+    if (++cnt == kChunk) flush_parts<T, NS>(acc, part, cnt);
   }
-  block_reduce_finalize<JAC ? 2 : 1>(red, acc);
+  flush_parts<T, NS>(acc, part, cnt);
+  block_reduce_finalize<NS>(red, acc);
 }
 template <typename T>
 void launch_pcg_update(T* x, T* r, T* z, const T* p, const T* q, const T* dinv, long long n,
@@ -227,12 +250,16 @@ __global__ void jacobi_precond_kernel(T* __restrict__ z, const T* __restrict__ r
                                       const int* halt) {
   if (halt && *((volatile const int*)halt)) return;
   double acc[1] = {0.0};
+  T part[1] = {T(0)};
+  int cnt = 0;
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
        i += (long long)gridDim.x * blockDim.x) {
     const T zi = r[i] * dinv[i];
     z[i] = zi;
-    acc[0] += (double)r[i] * (double)zi;
+    part[0] = fma(r[i], zi, part[0]);
+    if (++cnt == kChunk) flush_parts<T, 1>(acc, part, cnt);
   }
+  flush_parts<T, 1>(acc, part, cnt);
   block_reduce_finalize<1>(red, acc);
 }
 template <typename T>
