@@ -88,6 +88,7 @@ typedef struct hexa_solve_params {
   int32_t use_graphs;         /* capture PCG iterations / V-cycles in CUDA graphs */
   int32_t graph_iters;        /* iterations per graph launch (host reads status between launches) */
   int32_t true_residual;      /* 1: recompute ||f-(K+sI)u||/||f|| in FP64 and iterate until <= tol */
+  int32_t divergence_check;   /* 1: stop when rel > 10 or (k > 500 and rel > 100 best), GPUSolver.jl:397 */
 } hexa_solve_params;
 
 typedef struct hexa_solve_stats {

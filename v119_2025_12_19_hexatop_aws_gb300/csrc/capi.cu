@@ -147,6 +147,7 @@ void hexa_default_params(hexa_solve_params* p) {
   p->use_graphs = 1;
   p->graph_iters = 10;
   p->true_residual = 1;
+  p->divergence_check = 1;
 }
 
 int hexa_create(int32_t device, hexa_ctx** out) {

@@ -105,6 +105,11 @@ void launch_restrict(const Grid& gf, const T* rf, const Grid& gc, const Mask& mc
 template <typename T>
 void launch_prolong_add(const Grid& gc, const T* xc, const Grid& gf, const Mask& mf, T* xf,
                         const int* halt, cudaStream_t st);
+// `iters` Jacobi-PCG iterations on a small grid in one single-CTA launch
+// (w: 24 * nelem scratch for the element products)
+template <typename T>
+void launch_coarse_pcg(const Grid& g, const Mask& m, const T* fac, const ModalK<T>& K, T sigma, const T* dinv,
+                       const T* b, T* x, T* r, T* z, T* p, T* q, T* w, int iters, const int* halt, cudaStream_t st);
 // x = omega * b / D (first damped-Jacobi sweep from a zero guess)
 template <typename T>
 void launch_jacobi0(const Grid& g, const Mask& m, const T* fac, const ModalK<T>& K, int quirk,

@@ -176,6 +176,170 @@ void launch_jacobi0(const Grid& g, const Mask& m, const T* fac, const ModalK<T>&
   jacobi0_kernel<T><<<mg_blocks(g.nnode()), 256, 0, st>>>(g, m, fac, K, quirk, sigma, omega, b, x, halt);
 }
 
+// ---------------------------------------------------------------------------
+// Coarsest-level solve in one launch: a single CTA runs `iters` Jacobi-PCG
+// iterations on a small grid (element products into a scratch array, then a
+// node gather), with block reductions in a fixed order.  Replaces the
+// 3 launches per iteration of the general path when the coarse grid is small.
+template <typename T>
+__device__ __forceinline__ double cta_sum(double v, double* red) {
+  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5, nw = blockDim.x >> 5;
+  v = warp_sum(v);
+  __syncthreads();
+  if (lane == 0) red[wid] = v;
+  __syncthreads();
+  double t = 0.0;
+  for (int w = 0; w < nw; ++w) t += red[w];  // every thread sums in the same order
+  return t;
+}
+
+__device__ __forceinline__ bool modal_nz_mg(int q, int c, int c2) {
+  if (q == 1 || q == 2 || q == 4) {
+    const int c0 = (q == 1) ? 0 : (q == 2 ? 1 : 2);
+    return c != c0 && c2 != c0;
+  }
+  if (q == 3 || q == 5 || q == 6) {
+    const int cf = (q == 3) ? 2 : (q == 5 ? 1 : 0);
+    return (c == cf) == (c2 == cf);
+  }
+  return true;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(1024) coarse_pcg_kernel(Grid g, Mask m, const T* __restrict__ fac, ModalK<T> K,
+                                                          T sigma, const T* __restrict__ dinv, const T* __restrict__ b,
+                                                          T* x, T* r, T* z, T* p, T* q, T* w, int iters,
+                                                          const int* halt) {
+  if (halt && *((volatile const int*)halt)) return;
+  __shared__ double red[32];
+  const int tid = threadIdx.x, nthr = blockDim.x;
+  const long long n3 = g.ndof(), ne = g.nelem(), nn = g.nnode();
+  double part = 0.0;
+  for (long long i = tid; i < n3; i += nthr) {
+    const T ri = b[i], zi = dinv[i] * ri;
+    x[i] = T(0);
+    r[i] = ri;
+    z[i] = zi;
+    p[i] = zi;
+    part += (double)ri * (double)zi;
+  }
+  double rz = cta_sum<T>(part, red);
+  for (int it = 0; it < iters; ++it) {
+    // element products w_e = f_e K0 p_e (Hadamard basis), corner order dx + 2dy + 4dz
+    for (long long e = tid; e < ne; e += nthr) {
+      const int i = (int)(e % g.nx);
+      const long long t = e / g.nx;
+      const int j = (int)(t % g.ny), k = (int)(t / g.ny);
+      T h[8][3];
+#pragma unroll
+      for (int cc = 0; cc < 8; ++cc) {
+        const long long nd = (long long)(i + (cc & 1)) + (long long)g.NX * ((long long)(j + ((cc >> 1) & 1)) + (long long)g.NY * (k + (cc >> 2)));
+#pragma unroll
+        for (int c = 0; c < 3; ++c) h[cc][c] = p[3 * nd + c];
+      }
+#pragma unroll
+      for (int c = 0; c < 3; ++c)
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+          const int sft = 1 << d;
+          T tmp[8];
+#pragma unroll
+          for (int cc = 0; cc < 8; ++cc) {
+            const int lo = cc & ~sft;
+            tmp[cc] = (cc & sft) ? (h[lo | sft][c] - h[lo][c]) : (h[lo][c] + h[lo | sft][c]);
+          }
+#pragma unroll
+          for (int cc = 0; cc < 8; ++cc) h[cc][c] = tmp[cc];
+        }
+      const T f = fac[e];
+      T wh[8][3];
+#pragma unroll
+      for (int mm = 0; mm < 8; ++mm)
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+          const int qq = mm ^ (1 << c);
+          T s = T(0);
+#pragma unroll
+          for (int c2 = 0; c2 < 3; ++c2)
+            if (modal_nz_mg(qq, c, c2)) s = fma(K.B[qq][c][c2], h[qq ^ (1 << c2)][c2], s);
+          wh[mm][c] = s * f;
+        }
+      // inverse transform (the forward butterflies transposed)
+#pragma unroll
+      for (int c = 0; c < 3; ++c)
+#pragma unroll
+        for (int d = 2; d >= 0; --d) {
+          const int sft = 1 << d;
+          T tmp[8];
+#pragma unroll
+          for (int cc = 0; cc < 8; ++cc) {
+            const int lo = cc & ~sft;
+            tmp[cc] = (cc & sft) ? (wh[lo][c] + wh[lo | sft][c]) : (wh[lo][c] - wh[lo | sft][c]);
+          }
+#pragma unroll
+          for (int cc = 0; cc < 8; ++cc) wh[cc][c] = tmp[cc];
+        }
+#pragma unroll
+      for (int cc = 0; cc < 8; ++cc)
+#pragma unroll
+        for (int c = 0; c < 3; ++c) w[e * 24 + 3 * cc + c] = wh[cc][c];
+    }
+    __syncthreads();
+    part = 0.0;
+    for (long long nd = tid; nd < nn; nd += nthr) {
+      const int i = (int)(nd % g.NX);
+      const long long t = nd / g.NX;
+      const int j = (int)(t % g.NY), k = (int)(t / g.NY);
+      const unsigned fx = fixed_bits(g, m, i, j, k, nd);
+      T s0 = T(0), s1 = T(0), s2 = T(0);
+#pragma unroll
+      for (int oz = 0; oz < 2; ++oz)
+#pragma unroll
+        for (int oy = 0; oy < 2; ++oy)
+#pragma unroll
+          for (int ox = 0; ox < 2; ++ox) {
+            const int ei = i - 1 + ox, ej = j - 1 + oy, ek = k - 1 + oz;
+            if (ei < 0 || ei >= g.nx || ej < 0 || ej >= g.ny || ek < 0 || ek >= g.nz) continue;
+            const long long e = (long long)ei + (long long)g.nx * ((long long)ej + (long long)g.ny * ek);
+            const int ln = (1 - ox) + 2 * (1 - oy) + 4 * (1 - oz);
+            s0 += w[e * 24 + 3 * ln];
+            s1 += w[e * 24 + 3 * ln + 1];
+            s2 += w[e * 24 + 3 * ln + 2];
+          }
+      const T sv[3] = {s0, s1, s2};
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        const T pv = p[3 * nd + c];
+        const T qv = ((fx >> c) & 1u) ? T(0) : fma(sigma, pv, sv[c]);
+        q[3 * nd + c] = qv;
+        part += (double)pv * (double)qv;
+      }
+    }
+    const double pAp = cta_sum<T>(part, red);
+    if (!(pAp > 0.0)) break;  // converged to rounding or no curvature left
+    const T alpha = (T)(rz / pAp);
+    part = 0.0;
+    for (long long i = tid; i < n3; i += nthr) {
+      x[i] = fma(alpha, p[i], x[i]);
+      const T ri = fma(-alpha, q[i], r[i]);
+      r[i] = ri;
+      const T zi = dinv[i] * ri;
+      z[i] = zi;
+      part += (double)ri * (double)zi;
+    }
+    const double rz_new = cta_sum<T>(part, red);
+    const T beta = (T)(rz != 0.0 ? rz_new / rz : 0.0);
+    rz = rz_new;
+    for (long long i = tid; i < n3; i += nthr) p[i] = fma(beta, p[i], z[i]);
+    __syncthreads();
+  }
+}
+template <typename T>
+void launch_coarse_pcg(const Grid& g, const Mask& m, const T* fac, const ModalK<T>& K, T sigma, const T* dinv,
+                       const T* b, T* x, T* r, T* z, T* p, T* q, T* w, int iters, const int* halt, cudaStream_t st) {
+  coarse_pcg_kernel<T><<<1, 1024, 0, st>>>(g, m, fac, K, sigma, dinv, b, x, r, z, p, q, w, iters, halt);
+}
+
 #define INST(T)                                                                                     \
   template void launch_coarsen_factors<T>(const Grid&, const T*, const Grid&, T*, cudaStream_t);    \
   template void launch_restrict<T>(const Grid&, const T*, const Grid&, const Mask&, T*, const int*, \
@@ -183,7 +347,9 @@ void launch_jacobi0(const Grid& g, const Mask& m, const T* fac, const ModalK<T>&
   template void launch_prolong_add<T>(const Grid&, const T*, const Grid&, const Mask&, T*,          \
                                       const int*, cudaStream_t);                                    \
   template void launch_jacobi0<T>(const Grid&, const Mask&, const T*, const ModalK<T>&, int, T, T,  \
-                                  const T*, T*, const int*, cudaStream_t);
+                                  const T*, T*, const int*, cudaStream_t);                          \
+  template void launch_coarse_pcg<T>(const Grid&, const Mask&, const T*, const ModalK<T>&, T, const T*, \
+                                     const T*, T*, T*, T*, T*, T*, T*, int, const int*, cudaStream_t);
 INST(double)
 INST(float)
 #undef INST

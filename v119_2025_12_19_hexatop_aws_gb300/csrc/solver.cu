@@ -92,6 +92,8 @@ bool build_modal(double dx, double dy, double dz, double nu, ModalK<double>* K, 
 namespace {
 
 constexpr int kRedBlocks = 152 * 4;  // grid of reducing vector passes
+// Coarsest grids up to this many elements are solved by the single-CTA kernel.
+constexpr long long kCoarseOneCta = 4096;
 
 template <typename T>
 struct Is64 { static constexpr bool v = sizeof(T) == 8; };
@@ -122,6 +124,7 @@ struct Lev {
   T* b = nullptr;   // level right-hand side (coarse levels)
   T* r = nullptr;   // level residual
   T* dinv = nullptr, *p = nullptr, *q = nullptr, *z = nullptr;  // coarsest-level PCG
+  T* w = nullptr;  // element-product scratch of the single-CTA coarse solve
   T sigma = 0;
   int kchunk = 4;
 };
@@ -244,6 +247,10 @@ bool build_mg(Ctx& c, MG<T>& mg, const Grid& g0, const Mask& m0, const T* fac0, 
   Lc.p = c.vec<T>(s + "p", nc);
   Lc.q = c.vec<T>(s + "q", nc);
   Lc.z = c.vec<T>(s + "z", nc);
+  if (Lc.g.nelem() <= kCoarseOneCta) {
+    Lc.w = c.vec<T>(s + "w", 24 * Lc.g.nelem());
+    if (!Lc.w) return false;
+  }
   if (!Lc.xa) {  // single-level hierarchy
     Lc.xa = c.vec<T>(s + "xa", nc);
     Lc.b = c.vec<T>(s + "b", nc);
@@ -267,6 +274,12 @@ template <typename T>
 void coarse_solve(Ctx& c, MG<T>& mg, const T* b, T* x, const int* halt_main) {
   Lev<T>& V = mg.L.back();
   const long long n = V.g.ndof();
+  if (V.w) {
+    launch_coarse_pcg<T>(V.g, V.m, V.fac, mg.K, V.sigma, V.dinv, b, x, V.r, V.z, V.p, V.q, V.w, mg.citers, halt_main,
+                         c.st);
+    c.launches++;
+    return;
+  }
   launch_scalars_init(c.s2, c.s, mg.citers, c.st);
   launch_fill<T>(x, T(0), n, c.st);
   launch_copy<T>(V.r, b, n, c.st);
@@ -443,10 +456,43 @@ double applies_per_iteration(const PcgEnv<T>& E) {
   return 1.0 + per;
 }
 
+// Replays groups of PCG iterations (a CUDA graph captured on first use, or
+// direct launches) until the device-side halt flag is set; *h receives the
+// final scalars.  Iterations continue from whatever state E and c.s hold.
+template <typename T>
+bool pcg_drive(Ctx& c, PcgEnv<T>& E, Graph& graph, PcgScalars* h) {
+  int G = E.graph_iters < 2 ? 2 : E.graph_iters;
+  if (G & 1) ++G;  // even: each group starts with the same z / z_old buffer parity
+  if (E.use_graphs && !graph.exec) {
+    if (!capture(c, graph, [&]() {
+          for (int i = 0; i < G; ++i) pcg_iteration<T>(c, E, i & 1);
+        }))
+      return false;
+  }
+  double host_best = INFINITY;
+  while (true) {
+    if (E.use_graphs) {
+      if (!replay(c, graph)) return false;
+    } else {
+      for (int i = 0; i < G; ++i) pcg_iteration<T>(c, E, i & 1);
+      if (!c.cuda_ok("pcg iteration")) return false;
+    }
+    cudaMemcpyAsync(c.hs, c.s, sizeof(PcgScalars), cudaMemcpyDeviceToHost, c.st);
+    if (cudaStreamSynchronize(c.st) != cudaSuccess) return c.cuda_ok("pcg sync");
+    *h = *c.hs;
+    if (E.bestx && h->best_rel < host_best) {
+      host_best = h->best_rel;
+      cudaMemcpyAsync(E.bestx, E.x, sizeof(T) * E.n, cudaMemcpyDeviceToDevice, c.st);
+    }
+    if (h->halt) break;
+  }
+  return true;
+}
+
 // Runs PCG from the current E.x.  host_scalars carries tol/max_iter/cadence.
 template <typename T>
 bool run_pcg(Ctx& c, PcgEnv<T>& E, double tol, int max_iter, int cadence, bool x_is_zero, double bnorm,
-             PcgOut* out) {
+             bool div_check, PcgOut* out) {
   PcgScalars h;
   std::memset(&h, 0, sizeof(h));
   h.tol = tol;
@@ -454,6 +500,7 @@ bool run_pcg(Ctx& c, PcgEnv<T>& E, double tol, int max_iter, int cadence, bool x
   h.cadence = cadence;
   h.bnorm = bnorm;
   h.best_rel = INFINITY;
+  h.no_div = div_check ? 0 : 1;
   *c.hs = h;
   cudaMemcpyAsync(c.s, c.hs, sizeof(PcgScalars), cudaMemcpyHostToDevice, c.st);
   Lev<T>& L = *E.L0;
@@ -477,40 +524,14 @@ bool run_pcg(Ctx& c, PcgEnv<T>& E, double tol, int max_iter, int cadence, bool x
   c.launches++;
   if (!c.cuda_ok("pcg setup")) return false;
 
-  int G = E.graph_iters < 2 ? 2 : E.graph_iters;
-  if (G & 1) ++G;
   Graph graph;
-  if (E.use_graphs) {
-    if (!capture(c, graph, [&]() {
-          for (int i = 0; i < G; ++i) pcg_iteration<T>(c, E, i & 1);
-        }))
-      return false;
-  }
-  double host_best = INFINITY;
-  int done_iters = 0;
-  const double per = applies_per_iteration(E);
-  while (true) {
-    if (E.use_graphs) {
-      if (!replay(c, graph)) return false;
-    } else {
-      for (int i = 0; i < G; ++i) pcg_iteration<T>(c, E, i & 1);
-      if (!c.cuda_ok("pcg iteration")) return false;
-    }
-    cudaMemcpyAsync(c.hs, c.s, sizeof(PcgScalars), cudaMemcpyDeviceToHost, c.st);
-    if (cudaStreamSynchronize(c.st) != cudaSuccess) return c.cuda_ok("pcg sync");
-    h = *c.hs;
-    done_iters = h.iter;
-    if (E.bestx && h.best_rel < host_best) {
-      host_best = h.best_rel;
-      cudaMemcpyAsync(E.bestx, E.x, sizeof(T) * E.n, cudaMemcpyDeviceToDevice, c.st);
-    }
-    if (h.halt) break;
-  }
+  const int iter0 = 0;
+  if (!pcg_drive<T>(c, E, graph, &h)) return false;
   out->status = h.status;
-  out->iters = done_iters;
+  out->iters = h.iter - iter0;
   out->relres = h.relres;
   out->best_rel = h.best_rel;
-  out->fine_applies += per * done_iters + (x_is_zero ? 0.0 : 1.0);
+  out->fine_applies += applies_per_iteration(E) * out->iters + (x_is_zero ? 0.0 : 1.0);
   return true;
 }
 
@@ -698,7 +719,8 @@ int solve_plain(Ctx& c, const Problem& P, const hexa_solve_params& prm, const do
         c.launches++;
       }
       PcgOut o;
-      if (!run_pcg<T>(c, E, prm.tol, prm.max_iter, prm.check_cadence, x_zero, bnorm, &o)) return HEXA_ERR_CUDA;
+      if (!run_pcg<T>(c, E, prm.tol, prm.max_iter, prm.check_cadence, x_zero, bnorm, prm.divergence_check != 0, &o))
+        return HEXA_ERR_CUDA;
       // FP64 true-residual restarts (plain FP64 only)
       if (o.status == 1 && prm.true_residual && Is64<T>::v) {
         double* r64 = c.vec<double>("rtrue", n);
@@ -709,7 +731,8 @@ int solve_plain(Ctx& c, const Problem& P, const hexa_solve_params& prm, const do
           PcgOut o2;
           const int left = prm.max_iter - o.iters;
           if (left <= 0) break;
-          if (!run_pcg<T>(c, E, prm.tol, left, prm.check_cadence, false, bnorm, &o2)) return HEXA_ERR_CUDA;
+          if (!run_pcg<T>(c, E, prm.tol, left, prm.check_cadence, false, bnorm, prm.divergence_check != 0, &o2))
+            return HEXA_ERR_CUDA;
           o.iters += o2.iters;
           o.fine_applies += o2.fine_applies;
           o.status = o2.status;
@@ -852,38 +875,104 @@ int solve_mixed(Ctx& c, const Problem& P, const hexa_solve_params& prm, const do
   c.launches++;
   if (!c.cuda_ok("mixed setup")) return HEXA_ERR_CUDA;
   cudaEventRecord(c.ev[1], c.st);
+  // One FP32 PCG carried across "reliable updates": the correction x32 is
+  // accumulated into the FP64 iterate whenever the FP32 recursive residual has
+  // dropped by inner_tol, the FP64 true residual f - (K + sigma I) u replaces
+  // the FP32 residual (rescaled to unit norm, so void-contrast magnitudes never
+  // meet FP32's range limits) and the search direction is kept, rescaled --
+  // no restart, so the FP32 solve keeps its Krylov progress.
   double rn = true_residual_norm(c, P, K64, prm.diag_quirk, sigma, u, r64);
   double rel = rn / bnorm;
   double applies64 = 1.0, applies32 = 0.0;
-  int outer = 0, inner_total = 0, status = HEXA_OK;
+  int outer = 0, status = HEXA_OK;
   const int max_outer = prm.max_outer > 0 ? prm.max_outer : 20;
   const double inner_tol = prm.inner_tol > 0 ? prm.inner_tol : 1e-4;
-  while (rel > prm.tol) {
-    if (outer >= max_outer || inner_total >= prm.max_iter || !(rel == rel)) {
-      status = HEXA_NOT_CONVERGED;
-      break;
-    }
-    ++outer;
-    c.hscal[10] = 1.0 / rn;
+  double scale = 1.0 / rn;  // r32 = scale * r_true
+  PcgScalars h;
+  std::memset(&h, 0, sizeof(h));
+  Graph graph;
+  if (rel > prm.tol) {
+    c.hscal[10] = scale;
     cudaMemcpyAsync(c.dscal + 10, c.hscal + 10, sizeof(double), cudaMemcpyHostToDevice, c.st);
     launch_scale_to_f32(b32, r64, c.dscal + 10, n, c.st);
     launch_fill<float>(E.x, 0.0f, n, c.st);
     c.launches += 2;
-    PcgOut o;
-    if (!run_pcg<float>(c, E, inner_tol, prm.max_iter - inner_total, prm.check_cadence, true, 1.0, &o))
-      return HEXA_ERR_CUDA;
-    inner_total += o.iters;
-    applies32 += o.fine_applies;
-    if (o.status == 2 || o.status == 3 || o.iters == 0) {
+    h.tol = inner_tol;
+    h.max_iter = prm.max_iter;
+    h.cadence = prm.check_cadence;
+    h.bnorm = 1.0;
+    h.best_rel = INFINITY;
+    h.no_div = 1;
+    *c.hs = h;
+    cudaMemcpyAsync(c.s, c.hs, sizeof(PcgScalars), cudaMemcpyHostToDevice, c.st);
+    const int* halt = &c.s->halt;
+    launch_copy<float>(E.r, b32, n, c.st);
+    c.launches++;
+    if (E.mg) {
+      vcycle<float>(c, *E.mg, 0, E.r, E.zA, halt);
+      launch_dot<float>(E.r, E.zA, (const float*)nullptr, (const float*)nullptr, n, red(c, FIN_INIT_RZ, 1, c.s),
+                        kRedBlocks, halt, c.st);
+    } else {
+      launch_jacobi_precond<float>(E.zA, E.r, E.dinv, n, red(c, FIN_INIT_RZ, 1, c.s), kRedBlocks, halt, c.st);
+    }
+    launch_copy<float>(E.p, E.zA, n, c.st);
+    c.launches += 2;
+    if (!c.cuda_ok("mixed setup")) return HEXA_ERR_CUDA;
+  }
+  while (rel > prm.tol) {
+    if (!pcg_drive<float>(c, E, graph, &h)) return HEXA_ERR_CUDA;
+    ++outer;
+    if (h.status == 2) {  // NaN in the FP32 recursion
       status = HEXA_NOT_CONVERGED;
       break;
     }
+    // accumulate the FP32 correction and recompute the true residual in FP64
     launch_add_scaled_f32(u, E.x, c.dscal + 10, n, c.st);
     c.launches++;
     rn = true_residual_norm(c, P, K64, prm.diag_quirk, sigma, u, r64);
     applies64 += 1.0;
     rel = rn / bnorm;
+    if (rel <= prm.tol) break;
+    if (h.iter >= prm.max_iter || outer >= max_outer || !(rel == rel)) {
+      status = HEXA_NOT_CONVERGED;
+      break;
+    }
+    // replace the residual, keep the direction: p <- z_new + beta * (scale_new/scale) p
+    const double scale_new = 1.0 / rn, ratio = scale_new / scale;
+    const double rz_old = h.rz * ratio * ratio;
+    c.hscal[10] = scale_new;
+    cudaMemcpyAsync(c.dscal + 10, c.hscal + 10, sizeof(double), cudaMemcpyHostToDevice, c.st);
+    launch_scale_to_f32(E.r, r64, c.dscal + 10, n, c.st);
+    launch_fill<float>(E.x, 0.0f, n, c.st);
+    c.launches += 2;
+    h.halt = 0;
+    h.status = 0;
+    h.best_rel = INFINITY;
+    *c.hs = h;
+    cudaMemcpyAsync(c.s, c.hs, sizeof(PcgScalars), cudaMemcpyHostToDevice, c.st);
+    const int* halt = &c.s->halt;
+    if (E.mg) {
+      vcycle<float>(c, *E.mg, 0, E.r, E.zA, halt);
+      launch_dot<float>(E.r, E.zA, (const float*)nullptr, (const float*)nullptr, n, red(c, FIN_INIT_RZ, 1, c.s),
+                        kRedBlocks, halt, c.st);
+    } else {
+      launch_jacobi_precond<float>(E.zA, E.r, E.dinv, n, red(c, FIN_INIT_RZ, 1, c.s), kRedBlocks, halt, c.st);
+    }
+    c.launches++;
+    double rz_new = 0.0;
+    cudaMemcpyAsync(c.hscal + 11, &c.s->rz, sizeof(double), cudaMemcpyDeviceToHost, c.st);
+    if (cudaStreamSynchronize(c.st) != cudaSuccess) {
+      c.cuda_ok("reliable update");
+      return HEXA_ERR_CUDA;
+    }
+    rz_new = c.hscal[11];
+    const double beta = (rz_old > 0.0) ? rz_new / rz_old : 0.0;
+    launch_axpby<float>(E.p, (float)(beta * ratio), E.zA, 1.0f, n, c.st);
+    c.launches++;
+    scale = scale_new;
   }
+  applies32 = applies_per_iteration(E) * h.iter;
+  const int inner_total = h.iter;
   cudaEventRecord(c.ev[2], c.st);
   st->compliance = device_dot(c, P.f64, u, n, 9);
   cudaEventSynchronize(c.ev[2]);

@@ -99,7 +99,8 @@ def run_simp(S: SimpSetup, x0: np.ndarray, n_iter: int = 10, keep=True, ctx=None
     for _ in range(n_iter):
         xphys, _ = filter_density(S.grid, x, S.filter_radius, tol=S.filter_tol, quirk=False, max_iter=10000, ctx=ctx)
         fac = simp_factors(xphys, S.Emin, S.E0, S.penal, ctx=ctx)
-        u, st = solve(S.grid, fac, S.f, clamp_faces=S.clamp_faces, fixed_dof=S.fixed_dof, params=S.params, ctx=ctx)
+        params = S.params or _lib.default_params(divergence_check=0)
+        u, st = solve(S.grid, fac, S.f, clamp_faces=S.clamp_faces, fixed_dof=S.fixed_dof, params=params, ctx=ctx)
         dc, c = sensitivities(S.grid, xphys, u, nu=S.nu, Emin=S.Emin, E0=S.E0, penal=S.penal, ctx=ctx)
         dcx, _ = filter_density(S.grid, dc, S.filter_radius, tol=S.filter_tol, quirk=False, max_iter=10000, ctx=ctx)
         hist.append(SimpRecord(c, float(xphys.mean()), int(st["iterations"]), float(st["true_relres"]),
