@@ -39,6 +39,7 @@ extern "C" {
 #define HEXA_ERR_NOMEM (-3)
 #define HEXA_ERR_CORRUPT_INPUT (-4) /* NaN/Inf in the stiffness diagonal: GPUSolver.jl:310-315 */
 #define HEXA_ERR_NO_DEVICE (-5)     /* "CUDA not functional!": GPUSolver.jl:470-472 */
+#define HEXA_ERR_TOO_LARGE (-6)     /* grid beyond HEXA_NOALLOC_MAX_NODES (hexa_filter_noalloc) */
 
 typedef struct hexa_ctx hexa_ctx;
 
@@ -196,6 +197,24 @@ int hexa_solve_multi_rhs(hexa_ctx* ctx, const hexa_grid* g, const hexa_bc* bc, c
 int hexa_filter(hexa_ctx* ctx, const hexa_grid* g, const double* rho_in, double radius, double tol,
                 int32_t max_iter, int32_t quirk, int32_t precision, double* rho_out,
                 hexa_filter_stats* stats);
+
+/* The filter of hexa_filter without any device allocation (this entry point
+ * has no counterpart in the reference).  For callers that cannot allocate
+ * device memory where they filter -- code running while its application
+ * captures a CUDA stream, or hosts whose own pool owns the device-memory
+ * budget.  All scratch lives in one fixed device array inside the library
+ * (about 15 MB, held by every GPU that loads the library until exit), so the
+ * grid may have at most HEXA_NOALLOC_MAX_NODES nodes; larger grids return
+ * HEXA_ERR_TOO_LARGE.  rho_in and rho_out must be device pointers (host
+ * arrays would need a staging allocation: HEXA_ERR_ARG); FP64 arithmetic,
+ * same algorithm and results as hexa_filter with HEXA_PREC_FP64.  stream may
+ * be NULL (default stream); the call returns when its work is done.  Every
+ * call reuses the array: calls that overlap on the GPU race and must be
+ * serialised by the caller.  The first call on a device resolves the array's
+ * device address; make it before any stream capture begins. */
+#define HEXA_NOALLOC_MAX_NODES 262144
+int hexa_filter_noalloc(const hexa_grid* g, const double* rho_in, double radius, double tol, int32_t max_iter,
+                        int32_t quirk, double* rho_out, void* stream, hexa_filter_stats* stats);
 
 /* ---- (e) SIMP sensitivities and OC update ------------------------------ */
 /* dc_e = -penal * rho_e^(penal-1) * (E0 - Emin) * u_e^T K0 u_e and

@@ -21,6 +21,8 @@ HEXA_ERR_CUDA = -2
 HEXA_ERR_NOMEM = -3
 HEXA_ERR_CORRUPT_INPUT = -4
 HEXA_ERR_NO_DEVICE = -5
+HEXA_ERR_TOO_LARGE = -6
+NOALLOC_MAX_NODES = 262144
 
 PRECOND = {"jacobi": 0, "multigrid": 1}
 PRECISION = {"fp64": 0, "mixed": 1, "fp32": 2}
@@ -93,6 +95,7 @@ SIGNATURES = {
     "hexa_solve_multi_rhs": (I32, [P, C.POINTER(Grid), C.POINTER(BC), P, I32, P, C.POINTER(SolveParams), P,
                                    C.POINTER(SolveStats)]),
     "hexa_filter": (I32, [P, C.POINTER(Grid), P, D, D, I32, I32, I32, P, C.POINTER(FilterStats)]),
+    "hexa_filter_noalloc": (I32, [C.POINTER(Grid), P, D, D, I32, I32, P, P, C.POINTER(FilterStats)]),
     "hexa_sensitivities": (I32, [P, C.POINTER(Grid), D, P, P, D, D, D, P, C.POINTER(D)]),
     "hexa_simp_factors": (I32, [P, I64, P, D, D, D, P]),
     "hexa_oc_update": (I32, [P, I64, P, P, P, D, D, P, C.POINTER(D)]),
