@@ -49,6 +49,14 @@ def parse():
     ap.add_argument("--no-plain", action="store_true", help="skip the plain FP64 comparison solve")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--cpu-seconds", type=float, default=20.0)
+    ap.add_argument("--profile", action="store_true",
+                    help="profiling run: the warm-up and timed mixed steps only (no plain FP64, e2e, roofline or "
+                         "CPU legs), the timed steps bracketed by cudaProfilerStart/Stop for "
+                         "ncu --profile-from-start off; used for the launch lists under profiles/")
+    ap.add_argument("--kernel", default=None, choices=["apply", "apply_dot", "residual", "jacobi", "chebyshev",
+                                                       "apply_fp64"],
+                    help="time one operator mode alone on the config grid (--steps launches after --warmup) and "
+                         "print its GB/s; the small case for ncu --set full captures")
     return ap.parse_args()
 
 
@@ -156,12 +164,15 @@ def make_inputs(name, ctx):
 
 
 def solver_params(name, precision):
+    """The plain FP64 form uses the configuration's multigrid (4 levels at c2,
+    5 at c3, V(2,2)); the mixed form is the autotuned one (level count and
+    Chebyshev steps picked by trial solves on the first call, then cached)."""
     from v119_2025_12_19_hexatop_aws_gb300 import _lib, workloads as W
     # the reference's rel > 10 divergence stop (GPUSolver.jl:397) is off: CG residuals of these
     # high-contrast systems oscillate above it on the way to convergence
-    return _lib.default_params(precision=precision, precond="multigrid", tol=1e-9, max_iter=30000,
+    return _lib.default_params(precision=precision, precond="multigrid", tol=1e-9, max_iter=60000,
                                mg_levels=W.MG_LEVELS.get(name, 0), pre_smooth=2, post_smooth=2,
-                               divergence_check=0)
+                               divergence_check=0, autotune=1 if precision == "mixed" else 0)
 
 
 def peaks():
@@ -230,6 +241,10 @@ def run_ours(a):
         ctx.check(rc, allow=(_lib.HEXA_OK,))
         return st.as_dict()
 
+    if a.kernel:
+        run_kernel(a, ctx, grid, bc, fac_d, f_d, ndof, nelem, dist)
+        return
+
     for _ in range(a.warmup):
         step(pm, fac_d.data_ptr(), f_d.data_ptr(), u_d.data_ptr())
     torch.cuda.synchronize()
@@ -239,12 +254,16 @@ def run_ours(a):
     l0 = ctx.kernel_launches
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     torch.cuda.synchronize()
+    if a.profile:
+        torch.cuda.profiler.start()
     ev0.record()
     stats = []
     for _ in range(a.steps):
         stats.append(step(pm, fac_d.data_ptr(), f_d.data_ptr(), u_d.data_ptr()))
     ev1.record()
     torch.cuda.synchronize()
+    if a.profile:
+        torch.cuda.profiler.stop()
     ck = clocks.stop()
     dist.barrier()
     launches = ctx.kernel_launches - l0
@@ -252,6 +271,16 @@ def run_ours(a):
     ms = dist.max(ms)
     s_last = stats[-1]
     comp_mixed = s_last["compliance"]
+
+    if a.profile:
+        if dist.rank == 0:
+            print(json.dumps({"metric": METRIC, "value": round(ms / 1e3, 6), "unit": "s", "profile_run": True,
+                              "steps": a.steps, "warmup": a.warmup, "iterations": s_last["iterations"],
+                              "mg_levels": s_last["mg_levels"], "smooth_steps": s_last["smooth_steps"],
+                              "gpu_launches": int(launches)}))
+        ctx.close()
+        dist.close()
+        return
 
     # plain FP64 GMG-PCG on the same system (second call timed: the first allocates)
     plain = None
@@ -327,8 +356,9 @@ def run_ours(a):
         "warmup": a.warmup, "ms_per_step": round(ms, 3), "higher_is_better": False, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic (seeded cantilever, Helmholtz-smoothed density)",
         "config": {"workload": f"{a.config} cantilever {nx}x{ny}x{nz} hex8, {ndof} DOF, SIMP p=3 Emin=1e-9, "
-                               f"mixed FP32 GMG-PCG ({s_last['mg_levels']} levels, V(2,2) Jacobi) in FP64 "
-                               f"refinement to 1e-9",
+                               f"mixed: FP32 GMG-PCG (autotuned: {s_last['mg_levels']} levels, Chebyshev) with "
+                               f"FP64 reliable updates to true residual 1e-9; plain: FP64 GMG-PCG "
+                               f"({solver_params(a.config, 'fp64').mg_levels} levels, V(2,2))",
                    "parallelism": f"replicas{dist.ws}", "l2": "inputs larger than L2 (no flush)"},
         "e2e": {"value": round(e2e_ms / 1e3, 6), "unit": "s", "h2d_bytes_per_step": 8 * (nelem + ndof),
                 "d2h_bytes_per_step": 8 * ndof},
@@ -337,6 +367,7 @@ def run_ours(a):
         "gpu_launches": int(launches),
         "clocks": ck,
         "solve": {"iterations": s_last["iterations"], "outer_iterations": s_last["outer_iterations"],
+                  "mg_levels": s_last["mg_levels"], "smooth_steps": s_last["smooth_steps"],
                   "true_relres": s_last["true_relres"], "compliance": comp_mixed,
                   "fine_applies": s_last["fine_applies"], "dof_iterations_per_s": dofit,
                   "setup_ms": s_last["setup_ms"], "solve_ms": s_last["solve_ms"]},
@@ -345,6 +376,38 @@ def run_ours(a):
     }
     if dist.rank == 0:
         print(json.dumps(out))
+    ctx.close()
+    dist.close()
+
+
+OP_MODES = {"apply": (0, 2, 8, 4), "apply_dot": (1, 2, 8, 4), "residual": (2, 2, 12, 4), "jacobi": (4, 2, 12, 4),
+            "chebyshev": (5, 2, 16, 4), "apply_fp64": (0, 0, 16, 8)}  # mode, precision, B/DOF, B/element
+
+
+def run_kernel(a, ctx, grid, bc, fac_d, f_d, ndof, nelem, dist):
+    """One operator mode alone: --warmup launches, then --steps launches timed
+    by the library with CUDA events on its stream (algorithmic bytes: B/DOF * nDOF
+    + B/element * nElem per launch)."""
+    import ctypes as C
+    import torch
+    from v119_2025_12_19_hexatop_aws_gb300 import _lib
+
+    mode, prec, bdof, belem = OP_MODES[a.kernel]
+    cast = (lambda t: t.to(torch.float32).contiguous()) if prec == 2 else (lambda t: t)
+    fac, x, b = cast(fac_d), cast(torch.rand_like(f_d)), cast(f_d)
+    y = torch.empty_like(x)
+    t = C.c_double()
+    for reps in (max(1, a.warmup), max(1, a.steps)):
+        ctx.check(ctx.lib.hexa_time_operator(ctx.h, C.byref(grid), C.byref(bc), 0.3, prec, mode, fac.data_ptr(),
+                                             x.data_ptr(), b.data_ptr(), y.data_ptr(), reps, C.byref(t)),
+                  allow=(_lib.HEXA_OK,))
+    nbytes = bdof * ndof + belem * nelem
+    peak, kind = peaks()
+    if dist.rank == 0:
+        print(json.dumps({"kernel": a.kernel, "config": a.config, "ms_per_launch": t.value,
+                          "algorithmic_bytes": nbytes, "gbs": nbytes / (t.value * 1e-3) / 1e9,
+                          "frac": nbytes / (t.value * 1e-3) / 1e9 / peak, "peak": peak, "peak_source": kind,
+                          "launches": max(1, a.warmup) + max(1, a.steps)}))
     ctx.close()
     dist.close()
 

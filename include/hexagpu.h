@@ -90,6 +90,8 @@ typedef struct hexa_solve_params {
   int32_t graph_iters;        /* iterations per graph launch (host reads status between launches) */
   int32_t true_residual;      /* 1: recompute ||f-(K+sI)u||/||f|| in FP64 and iterate until <= tol */
   int32_t divergence_check;   /* 1: stop when rel > 10 or (k > 500 and rel > 100 best), GPUSolver.jl:397 */
+  int32_t autotune;           /* mixed + multigrid: pick levels and smoother degree by short trial solves,
+                                 cached per grid in the context (0: use mg_levels / pre_smooth / post_smooth) */
 } hexa_solve_params;
 
 typedef struct hexa_solve_stats {
@@ -99,6 +101,7 @@ typedef struct hexa_solve_stats {
   int32_t attempts;         /* shift attempts used */
   int32_t precond_used;     /* HEXA_PRECOND_USED_*: "GMG_GPU" / "Jacobi_GPU" (GPUSolver.jl:463) */
   int32_t mg_levels;
+  int32_t smooth_steps;     /* smoothing steps per side of the V-cycle that was used */
   double relres;            /* recursive ||r||/||f_free|| as GPUSolver.jl:380-382 reports */
   double true_relres;       /* ||f - (K+sigma I) u|| / ||f|| recomputed in FP64 */
   double shift;             /* sigma = shift_factor * max(diag K_ff) (GPUSolver.jl:343) */

@@ -182,3 +182,22 @@ def test_void_contrast_mixed_reaches_fp64_residual(ctx, oracle, rng):
     um, sm = solve(grid, fac, f, clamp_faces=1, params=_lib.default_params(precision="mixed"), ctx=ctx)
     assert s64["true_relres"] <= 1e-9 and sm["true_relres"] <= 1e-9
     assert abs(sm["compliance"] - s64["compliance"]) <= 1e-8 * abs(s64["compliance"])
+
+
+def test_autotuned_mixed_matches_fp64_and_caches(ctx, oracle, rng):
+    dims = (32, 16, 16)
+    g = oracle.Grid(*dims)
+    rho = np.clip(0.3 + 0.3 * rng.standard_normal(g.nelem), 0.001, 1.0)
+    fac = 1e-9 + rho ** 3 * (1 - 1e-9)
+    f = workloads.edge_load(*dims)
+    grid = _lib.make_grid(*dims)
+    u64, s64 = solve(grid, fac, f, clamp_faces=1, params=_lib.default_params(divergence_check=0), ctx=ctx)
+    p = _lib.default_params(precision="mixed", autotune=1, divergence_check=0)
+    um, s1 = solve(grid, fac, f, clamp_faces=1, params=p, ctx=ctx)
+    um2, s2 = solve(grid, fac, f, clamp_faces=1, params=p, ctx=ctx)
+    assert s1["status"] == 0 and s1["true_relres"] <= 1e-9
+    assert s1["smooth_steps"] in (2, 3, 4, 5) and s1["mg_levels"] >= 2
+    assert (s2["mg_levels"], s2["smooth_steps"]) == (s1["mg_levels"], s1["smooth_steps"])
+    assert s2["setup_ms"] < s1["setup_ms"]  # the second call reuses the tuned settings
+    assert np.array_equal(um, um2)
+    assert abs(s1["compliance"] - s64["compliance"]) <= 1e-8 * abs(s64["compliance"])

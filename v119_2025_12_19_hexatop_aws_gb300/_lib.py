@@ -47,14 +47,15 @@ class SolveParams(C.Structure):
         ("smoother", C.c_int32), ("jacobi_omega", C.c_double), ("cheb_degree", C.c_int32),
         ("coarse_iters", C.c_int32), ("inner_tol", C.c_double), ("max_outer", C.c_int32),
         ("use_graphs", C.c_int32), ("graph_iters", C.c_int32), ("true_residual", C.c_int32),
-        ("divergence_check", C.c_int32),
+        ("divergence_check", C.c_int32), ("autotune", C.c_int32),
     ]
 
 
 class SolveStats(C.Structure):
     _fields_ = [
         ("status", C.c_int32), ("iterations", C.c_int32), ("outer_iterations", C.c_int32), ("attempts", C.c_int32),
-        ("precond_used", C.c_int32), ("mg_levels", C.c_int32), ("relres", C.c_double), ("true_relres", C.c_double),
+        ("precond_used", C.c_int32), ("mg_levels", C.c_int32), ("smooth_steps", C.c_int32), ("relres", C.c_double),
+        ("true_relres", C.c_double),
         ("shift", C.c_double), ("max_diag", C.c_double), ("compliance", C.c_double), ("setup_ms", C.c_double),
         ("solve_ms", C.c_double), ("total_ms", C.c_double), ("fine_applies", C.c_double),
         ("fine_applies_fp64", C.c_double),

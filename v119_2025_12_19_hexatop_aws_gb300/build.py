@@ -19,7 +19,7 @@ CSRC = PKG / "csrc"
 BUILD = PKG / "_build"
 LIB = PKG / "libhexagpu.so"
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
-SOURCES = ["op.cu", "vec.cu", "mg.cu", "helm.cu", "topo.cu", "solver.cu", "capi.cu", "noalloc.cu", "element.cpp"]
+SOURCES = ["op.cu", "vec.cu", "mg.cu", "helm.cu", "topo.cu", "block.cu", "solver.cu", "capi.cu", "noalloc.cu", "element.cpp"]
 
 
 def nvcc() -> str:
@@ -71,7 +71,8 @@ def build(force: bool = False, verbose: bool = False, ptxas_verbose: bool = Fals
             if log.strip():
                 print(log, file=sys.stderr)
     tmp = LIB.with_suffix(".so.tmp")
-    cmd = [nvcc(), "-shared", "-o", str(tmp), *[o for o, _ in results], ARCH, "-cudart", "static", "-lrt", "-lpthread", "-ldl"]
+    cmd = [nvcc(), "-shared", "-o", str(tmp), *[o for o, _ in results], ARCH, "-cudart", "static", "-lrt", "-lpthread", "-ldl",
+           "-Xlinker", "--no-undefined"]  # a missing definition fails the build, not the first call
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{' '.join(cmd)}\n{r.stdout}\n{r.stderr}")

@@ -1,0 +1,383 @@
+// Block PCG kernels: k right-hand sides held as k consecutive columns of
+// length n (column j of X starts at X + j*n).
+//
+// One block iteration (O'Leary's block CG in its flexible form) is
+//   Z = M R                      (preconditioner, column by column)
+//   D = Q^T Z,  beta = -G^+ D    (gram + k x k solve; G = P^T A P of the last step)
+//   P = Z + P beta               (block_p_update)
+//   Q = A P                      (the multi-column operator)
+//   G = P^T Q, C = P^T R         (gram with two right operands)
+//   alpha = G^+ C                (k x k solve)
+//   X += P alpha, R -= Q alpha   (block_update, with the column norms of R)
+// G^+ is a pseudo-inverse through a Cholesky factorisation that drops a
+// direction whose pivot is below eps * G_jj (a search direction dependent on
+// the others), so converged or dependent columns cannot break the iteration.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+
+#include "hexa_common.cuh"
+#include "hexa_kernels.h"
+
+namespace hexa {
+
+namespace {
+
+constexpr int kThreads = 256;
+
+template <typename T>
+constexpr int gram_td() { return sizeof(T) == 8 ? 64 : 128; }
+
+template <int KC, int NB>
+struct GramShape {
+  static constexpr int NBC = NB * KC;            // right operand columns
+  static constexpr int RI = KC >= 2 ? 2 : 1;     // register block of a thread
+  static constexpr int RJ = NBC >= 4 ? 4 : NBC;
+  static constexpr int GI = KC / RI, GJ = NBC / RJ, GROUPS = GI * GJ;
+  static constexpr int SLICES = kThreads / GROUPS;  // DOF slices of a tile
+  static constexpr int NPAIR = KC * NBC;
+};
+
+__device__ __forceinline__ bool halt_set(const int* h) { return h && *((volatile const int*)h); }
+
+// out[i * NBC + j] = sum_d a_i[d] * b_j[d] for i < KC, j < NBC, where
+// b_j = b1_j for j < KC and b2_{j-KC} otherwise; columns >= k read as zero.
+// Tiles of TD DOFs are staged in shared memory; each thread accumulates an
+// RI x RJ block of pairs over one DOF slice in T, folded to FP64 per tile.
+// Per-block partials are summed in block order by the last block (ticket):
+// the result is bitwise reproducible.
+template <typename T, int KC, int NB>
+__global__ void __launch_bounds__(kThreads) gram_kernel(const T* __restrict__ a, const T* __restrict__ b1,
+                                                         const T* __restrict__ b2, int k, long long n,
+                                                         double* partials, unsigned* ticket, double* out,
+                                                         const int* halt) {
+  if (halt_set(halt)) return;
+  using S = GramShape<KC, NB>;
+  constexpr int TD = gram_td<T>();
+  __shared__ T sA[KC][TD + 1];
+  __shared__ T sB[S::NBC][TD + 1];
+  __shared__ double sred[S::SLICES][S::NPAIR];
+  __shared__ bool am_last;
+  const int tid = threadIdx.x;
+  const int grp = tid % S::GROUPS, slice = tid / S::GROUPS;
+  const int gi = grp / S::GJ, gj = grp % S::GJ;
+  double acc[S::RI][S::RJ];
+#pragma unroll
+  for (int i = 0; i < S::RI; ++i)
+#pragma unroll
+    for (int j = 0; j < S::RJ; ++j) acc[i][j] = 0.0;
+  const long long ntiles = (n + TD - 1) / TD;
+  for (long long t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    const long long d0 = t * TD;
+    for (int e = tid; e < (KC + S::NBC) * TD; e += kThreads) {
+      const int col = e / TD, d = e - col * TD;
+      const long long gd = d0 + d;
+      if (col < KC) {
+        sA[col][d] = (col < k && gd < n) ? a[(long long)col * n + gd] : T(0);
+      } else {
+        const int cb = col - KC, j = cb % KC;
+        const T* src = cb < KC ? b1 : b2;
+        sB[cb][d] = (j < k && gd < n) ? src[(long long)j * n + gd] : T(0);
+      }
+    }
+    __syncthreads();
+    T part[S::RI][S::RJ];
+#pragma unroll
+    for (int i = 0; i < S::RI; ++i)
+#pragma unroll
+      for (int j = 0; j < S::RJ; ++j) part[i][j] = T(0);
+    for (int d = slice; d < TD; d += S::SLICES) {
+      T av[S::RI], bv[S::RJ];
+#pragma unroll
+      for (int i = 0; i < S::RI; ++i) av[i] = sA[gi * S::RI + i][d];
+#pragma unroll
+      for (int j = 0; j < S::RJ; ++j) bv[j] = sB[gj * S::RJ + j][d];
+#pragma unroll
+      for (int i = 0; i < S::RI; ++i)
+#pragma unroll
+        for (int j = 0; j < S::RJ; ++j) part[i][j] = fma(av[i], bv[j], part[i][j]);
+    }
+#pragma unroll
+    for (int i = 0; i < S::RI; ++i)
+#pragma unroll
+      for (int j = 0; j < S::RJ; ++j) acc[i][j] += (double)part[i][j];
+    __syncthreads();
+  }
+#pragma unroll
+  for (int i = 0; i < S::RI; ++i)
+#pragma unroll
+    for (int j = 0; j < S::RJ; ++j) sred[slice][(gi * S::RI + i) * S::NBC + gj * S::RJ + j] = acc[i][j];
+  __syncthreads();
+  for (int p = tid; p < S::NPAIR; p += kThreads) {
+    double s = 0.0;
+    for (int sl = 0; sl < S::SLICES; ++sl) s += sred[sl][p];
+    partials[(long long)blockIdx.x * S::NPAIR + p] = s;
+  }
+  __threadfence();
+  __syncthreads();
+  if (tid == 0) am_last = (atomicAdd(ticket, 1u) == gridDim.x - 1);
+  __syncthreads();
+  if (!am_last) return;
+  __threadfence();
+  for (int p = tid; p < S::NPAIR; p += kThreads) {
+    double s = 0.0;
+    for (unsigned b = 0; b < gridDim.x; ++b) s += ((volatile double*)partials)[(long long)b * S::NPAIR + p];
+    out[p] = s;
+  }
+  if (tid == 0) *ticket = 0u;
+}
+
+// out (k x k, row = direction, column = right-hand side) = sign * G^+ rhs with
+// G_ij = (g[i*ldg+j] + g[j*ldg+i]) / 2 and rhs_ij = r[i*ldr + roff + j].
+__global__ void block_solve_kernel(const double* g, int ldg, const double* r, int ldr, int roff, int k, double sign,
+                                   double eps, double* out, const int* halt) {
+  if (halt_set(halt)) return;
+  __shared__ double L[kMaxBlockCols][kMaxBlockCols];
+  __shared__ int drop[kMaxBlockCols];
+  const int t = threadIdx.x;
+  if (t == 0) {
+    for (int j = 0; j < k; ++j) {
+      const double gjj = g[j * ldg + j];
+      double d = gjj;
+      for (int m = 0; m < j; ++m) d -= L[j][m] * L[j][m];
+      const bool ok = (gjj > 0.0) && (d > eps * gjj) && (d == d);
+      drop[j] = ok ? 0 : 1;
+      const double ljj = ok ? sqrt(d) : 0.0;
+      L[j][j] = ljj;
+      for (int i = j + 1; i < k; ++i) {
+        double v = 0.5 * (g[i * ldg + j] + g[j * ldg + i]);
+        for (int m = 0; m < j; ++m) v -= L[i][m] * L[j][m];
+        L[i][j] = ok ? v / ljj : 0.0;
+      }
+      for (int i = 0; i < j; ++i) L[i][j] = 0.0;
+    }
+  }
+  __syncthreads();
+  if (t < k) {
+    double y[kMaxBlockCols];
+    for (int i = 0; i < k; ++i) {  // L y = rhs(:, t)
+      double v = r[i * ldr + roff + t];
+      for (int m = 0; m < i; ++m) v -= L[i][m] * y[m];
+      y[i] = drop[i] ? 0.0 : v / L[i][i];
+    }
+    for (int i = k - 1; i >= 0; --i) {  // L^T x = y
+      double v = y[i];
+      for (int m = i + 1; m < k; ++m) v -= L[m][i] * y[m];
+      y[i] = drop[i] ? 0.0 : v / L[i][i];
+    }
+    for (int i = 0; i < k; ++i) out[i * k + t] = sign * y[i];
+  }
+}
+
+// X_j += sum_i P_i alpha_ij ; R_j -= sum_i Q_i alpha_ij ; sums ||R_j||^2.
+template <typename T, int KC>
+__global__ void __launch_bounds__(kThreads) block_update_kernel(T* __restrict__ X, T* __restrict__ R,
+                                                                 const T* __restrict__ P, const T* __restrict__ Q,
+                                                                 const double* alpha, int k, long long n,
+                                                                 RedArgs red) {
+  if (halt_set(red.s ? &red.s->halt : nullptr)) return;
+  __shared__ T sa[KC][KC];
+  for (int e = threadIdx.x; e < KC * KC; e += blockDim.x) {
+    const int i = e / KC, j = e % KC;
+    sa[i][j] = (i < k && j < k) ? (T)alpha[i * k + j] : T(0);
+  }
+  __syncthreads();
+  double acc[KC];
+  T part[KC];
+#pragma unroll
+  for (int j = 0; j < KC; ++j) acc[j] = 0.0, part[j] = T(0);
+  int cnt = 0;
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long d = (long long)blockIdx.x * blockDim.x + threadIdx.x; d < n; d += stride) {
+    T pv[KC], qv[KC];
+#pragma unroll
+    for (int i = 0; i < KC; ++i) {
+      pv[i] = i < k ? P[(long long)i * n + d] : T(0);
+      qv[i] = i < k ? Q[(long long)i * n + d] : T(0);
+    }
+#pragma unroll
+    for (int j = 0; j < KC; ++j) {
+      if (j < k) {
+        T x = X[(long long)j * n + d], r = R[(long long)j * n + d];
+#pragma unroll
+        for (int i = 0; i < KC; ++i) {
+          x = fma(pv[i], sa[i][j], x);
+          r = fma(-qv[i], sa[i][j], r);
+        }
+        X[(long long)j * n + d] = x;
+        R[(long long)j * n + d] = r;
+        part[j] = fma(r, r, part[j]);
+      }
+    }
+    if (++cnt == 32) {
+#pragma unroll
+      for (int j = 0; j < KC; ++j) acc[j] += (double)part[j], part[j] = T(0);
+      cnt = 0;
+    }
+  }
+#pragma unroll
+  for (int j = 0; j < KC; ++j) acc[j] += (double)part[j];
+  block_reduce_finalize<KC>(red, acc);
+}
+
+// P_j = Z_j + sum_i P_i beta_ij
+template <typename T, int KC>
+__global__ void __launch_bounds__(kThreads) block_p_update_kernel(T* __restrict__ P, const T* __restrict__ Z,
+                                                                   const double* beta, int k, long long n,
+                                                                   const int* halt) {
+  if (halt_set(halt)) return;
+  __shared__ T sb[KC][KC];
+  for (int e = threadIdx.x; e < KC * KC; e += blockDim.x) {
+    const int i = e / KC, j = e % KC;
+    sb[i][j] = (i < k && j < k) ? (T)beta[i * k + j] : T(0);
+  }
+  __syncthreads();
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long d = (long long)blockIdx.x * blockDim.x + threadIdx.x; d < n; d += stride) {
+    T pv[KC];
+#pragma unroll
+    for (int i = 0; i < KC; ++i) pv[i] = i < k ? P[(long long)i * n + d] : T(0);
+#pragma unroll
+    for (int j = 0; j < KC; ++j) {
+      if (j < k) {
+        T v = Z[(long long)j * n + d];
+#pragma unroll
+        for (int i = 0; i < KC; ++i) v = fma(pv[i], sb[i][j], v);
+        P[(long long)j * n + d] = v;
+      }
+    }
+  }
+}
+
+// Column kernels: blockIdx.y is the column.
+template <typename T>
+__global__ void cols_jacobi_kernel(T* __restrict__ z, const T* __restrict__ r, const T* __restrict__ dinv,
+                                   long long n, const int* halt) {
+  if (halt_set(halt)) return;
+  const long long off = (long long)blockIdx.y * n;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    z[off + i] = r[off + i] * dinv[i];
+}
+
+template <typename T>
+__global__ void cols_from64_kernel(T* __restrict__ d, const double* __restrict__ s, const double* scale, long long n) {
+  const long long off = (long long)blockIdx.y * n;
+  const double sc = scale[blockIdx.y];
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    d[off + i] = (T)(s[off + i] * sc);
+}
+
+template <typename T>
+__global__ void cols_accum_kernel(double* __restrict__ u, const T* __restrict__ d, const double* scale, long long n) {
+  const long long off = (long long)blockIdx.y * n;
+  const double sc = scale[blockIdx.y];
+  if (sc == 0.0) return;  // frozen column: no correction
+  const double inv = 1.0 / sc;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    u[off + i] = fma((double)d[off + i], inv, u[off + i]);
+}
+
+int col_grid_x(long long n, int k) {
+  const long long want = std::max<long long>(1, 152LL * 8 / std::max(1, k));
+  return (int)std::max<long long>(1, std::min<long long>((n + kThreads - 1) / kThreads, want));
+}
+
+}  // namespace
+
+long long block_partials_needed(int k) {
+  const int kc = k <= 1 ? 1 : k <= 2 ? 2 : k <= 4 ? 4 : k <= 8 ? 8 : 16;
+  return (long long)kBlockRedBlocks * kc * 2 * kc + (long long)kBlockRedBlocks * kc;
+}
+
+int block_kc(int k) { return k <= 1 ? 1 : k <= 2 ? 2 : k <= 4 ? 4 : k <= 8 ? 8 : 16; }
+
+template <typename T>
+void launch_gram(const T* a, const T* b1, const T* b2, int k, long long n, double* partials, unsigned* ticket,
+                 double* out, const int* halt, cudaStream_t st) {
+  constexpr int TD = gram_td<T>();
+  const int g = (int)std::max<long long>(1, std::min<long long>((n + TD - 1) / TD, kBlockRedBlocks));
+  const int kc = block_kc(k);
+#define HEXA_GRAM(KCV)                                                                                   \
+  case KCV:                                                                                             \
+    if (b2) gram_kernel<T, KCV, 2><<<g, kThreads, 0, st>>>(a, b1, b2, k, n, partials, ticket, out, halt); \
+    else gram_kernel<T, KCV, 1><<<g, kThreads, 0, st>>>(a, b1, b2, k, n, partials, ticket, out, halt);    \
+    break;
+  switch (kc) {
+    HEXA_GRAM(1)
+    HEXA_GRAM(2)
+    HEXA_GRAM(4)
+    HEXA_GRAM(8)
+    HEXA_GRAM(16)
+    default: break;
+  }
+#undef HEXA_GRAM
+}
+
+void launch_block_solve(const double* g, int ldg, const double* r, int ldr, int roff, int k, double sign, double eps,
+                        double* out, const int* halt, cudaStream_t st) {
+  block_solve_kernel<<<1, 32, 0, st>>>(g, ldg, r, ldr, roff, k, sign, eps, out, halt);
+}
+
+template <typename T>
+void launch_block_update(T* X, T* R, const T* P, const T* Q, const double* alpha, int k, long long n,
+                         const RedArgs& red, cudaStream_t st) {
+  const int g = (int)std::max<long long>(1, std::min<long long>((n + kThreads - 1) / kThreads, kBlockRedBlocks));
+#define HEXA_BU(KCV) \
+  case KCV: block_update_kernel<T, KCV><<<g, kThreads, 0, st>>>(X, R, P, Q, alpha, k, n, red); break;
+  switch (block_kc(k)) {
+    HEXA_BU(1)
+    HEXA_BU(2)
+    HEXA_BU(4)
+    HEXA_BU(8)
+    HEXA_BU(16)
+    default: break;
+  }
+#undef HEXA_BU
+}
+
+template <typename T>
+void launch_block_p_update(T* P, const T* Z, const double* beta, int k, long long n, const int* halt,
+                           cudaStream_t st) {
+  const int g = (int)std::max<long long>(1, std::min<long long>((n + kThreads - 1) / kThreads, 152LL * 8));
+#define HEXA_BP(KCV) \
+  case KCV: block_p_update_kernel<T, KCV><<<g, kThreads, 0, st>>>(P, Z, beta, k, n, halt); break;
+  switch (block_kc(k)) {
+    HEXA_BP(1)
+    HEXA_BP(2)
+    HEXA_BP(4)
+    HEXA_BP(8)
+    HEXA_BP(16)
+    default: break;
+  }
+#undef HEXA_BP
+}
+
+template <typename T>
+void launch_cols_jacobi(T* z, const T* r, const T* dinv, long long n, int k, const int* halt, cudaStream_t st) {
+  cols_jacobi_kernel<T><<<dim3(col_grid_x(n, k), k), kThreads, 0, st>>>(z, r, dinv, n, halt);
+}
+
+template <typename T>
+void launch_cols_from64(T* dst, const double* src, const double* scale, long long n, int k, cudaStream_t st) {
+  cols_from64_kernel<T><<<dim3(col_grid_x(n, k), k), kThreads, 0, st>>>(dst, src, scale, n);
+}
+
+template <typename T>
+void launch_cols_accum(double* u, const T* d, const double* scale, long long n, int k, cudaStream_t st) {
+  cols_accum_kernel<T><<<dim3(col_grid_x(n, k), k), kThreads, 0, st>>>(u, d, scale, n);
+}
+
+#define HEXA_BLOCK_INST(T)                                                                                    \
+  template void launch_gram<T>(const T*, const T*, const T*, int, long long, double*, unsigned*, double*,    \
+                               const int*, cudaStream_t);                                                    \
+  template void launch_block_update<T>(T*, T*, const T*, const T*, const double*, int, long long,            \
+                                       const RedArgs&, cudaStream_t);                                         \
+  template void launch_block_p_update<T>(T*, const T*, const double*, int, long long, const int*, cudaStream_t); \
+  template void launch_cols_jacobi<T>(T*, const T*, const T*, long long, int, const int*, cudaStream_t);     \
+  template void launch_cols_from64<T>(T*, const double*, const double*, long long, int, cudaStream_t);       \
+  template void launch_cols_accum<T>(double*, const T*, const double*, long long, int, cudaStream_t);
+HEXA_BLOCK_INST(float)
+HEXA_BLOCK_INST(double)
+#undef HEXA_BLOCK_INST
+
+}  // namespace hexa

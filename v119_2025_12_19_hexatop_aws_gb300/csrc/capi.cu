@@ -148,6 +148,7 @@ void hexa_default_params(hexa_solve_params* p) {
   p->graph_iters = 10;
   p->true_residual = 1;
   p->divergence_check = 1;
+  p->autotune = 0;
 }
 
 int hexa_create(int32_t device, hexa_ctx** out) {
@@ -174,7 +175,7 @@ int hexa_create(int32_t device, hexa_ctx** out) {
     uint64_t thr = ~0ULL;
     cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
   }
-  c.ticket = c.vec<unsigned>("ticket", 16);
+  c.ticket = c.vec<unsigned>("ticket", 64);  // [0, 16): per-column reductions, 32: gram
   c.s = c.vec<PcgScalars>("scalars", 1);
   c.s2 = c.vec<PcgScalars>("scalars2", 1);
   c.dscal = c.vec<double>("dscal", 64);
@@ -182,7 +183,7 @@ int hexa_create(int32_t device, hexa_ctx** out) {
     hexa_destroy(h);
     return HEXA_ERR_NOMEM;
   }
-  cudaMemsetAsync(c.ticket, 0, 16 * sizeof(unsigned), c.st);
+  cudaMemsetAsync(c.ticket, 0, 64 * sizeof(unsigned), c.st);
   cudaMemsetAsync(c.s, 0, sizeof(PcgScalars), c.st);
   cudaMemsetAsync(c.s2, 0, sizeof(PcgScalars), c.st);
   if (cudaMallocHost(&c.hs, sizeof(PcgScalars)) != cudaSuccess || cudaMallocHost(&c.hscal, 64 * sizeof(double)) != cudaSuccess) {
@@ -483,33 +484,38 @@ int hexa_solve_system_gpu(hexa_ctx* h, const hexa_grid* g, float E, const float*
 
 int hexa_solve_multi_rhs(hexa_ctx* h, const hexa_grid* g, const hexa_bc* bc, const double* factor, int32_t k,
                          const double* F, const hexa_solve_params* p, double* U, hexa_solve_stats* stats) {
+  const auto t0 = std::chrono::steady_clock::now();
   if (!h) return HEXA_ERR_ARG;
   if (!valid_grid(g) || !factor || !F || !U || k < 1) return set_err(h, HEXA_ERR_ARG, "invalid arguments");
   if (!valid_params(p)) return set_err(h, HEXA_ERR_ARG, "invalid solver parameters");
-  // Column-by-column until the block kernels land: each column is a full solve.
+  Ctx& c = h->c;
+  c.err.clear();
+  cudaSetDevice(c.device);
   const long long ndof = 3LL * (g->nx + 1) * (g->ny + 1) * (g->nz + 1);
-  hexa_solve_stats acc;
-  std::memset(&acc, 0, sizeof(acc));
-  int worst = HEXA_OK;
-  for (int j = 0; j < k; ++j) {
-    hexa_solve_stats st;
-    int rc = hexa_solve(h, g, bc, factor, F + j * ndof, p, nullptr, U + j * ndof, &st);
-    if (rc < 0) return rc;
-    if (rc > worst) worst = rc;
-    acc.iterations += st.iterations;
-    acc.solve_ms += st.solve_ms;
-    acc.setup_ms += st.setup_ms;
-    acc.total_ms += st.total_ms;
-    acc.compliance += st.compliance / k;
-    acc.true_relres = std::fmax(acc.true_relres, st.true_relres);
-    acc.relres = std::fmax(acc.relres, st.relres);
-    acc.fine_applies += st.fine_applies;
-    acc.precond_used = st.precond_used;
-    acc.mg_levels = st.mg_levels;
+  hexa_solve_stats st;
+  std::memset(&st, 0, sizeof(st));
+  Problem P;
+  // prepare_problem stages the factor and the first column; all k columns are staged here
+  if (!prepare_problem(h, g, bc, p->nu, factor, F, &P)) return set_err(h, HEXA_ERR_NOMEM, c.err.empty() ? "staging failed" : c.err);
+  const double* Fr = stage_in<double>(c, F, ndof * k, "in_F_raw");
+  double* Fd = c.vec<double>("in_F", ndof * k);
+  double* Ud = out_buf<double>(c, U, ndof * k, "out_U");
+  if (!Fr || !Fd || !Ud) return set_err(h, HEXA_ERR_NOMEM, c.err);
+  for (int j = 0; j < k; ++j) {  // loads at fixed DOFs are dropped, as in hexa_solve
+    launch_mask_copy<double, double>(P.g, P.m, Fd + j * ndof, Fr + j * ndof, c.st);
+    c.launches++;
   }
-  acc.status = worst;
-  if (stats) *stats = acc;
-  return worst;
+  int rc = multi_rhs_problem(c, P, k, Fd, *p, Ud, &st);
+  stage_out<double>(c, U, Ud, ndof * k);
+  if (cudaStreamSynchronize(c.st) != cudaSuccess) {
+    c.cuda_ok("multi-rhs solve");
+    rc = HEXA_ERR_CUDA;
+  }
+  st.status = rc;
+  st.total_ms = wall_ms(t0);
+  c.last_ms = st.setup_ms + st.solve_ms;
+  if (stats) *stats = st;
+  return rc;
 }
 
 }  // extern "C"

@@ -90,18 +90,30 @@ enum FinalizeOp {
   FIN_PCG_BETA = 4,     // rz_new = sum0 [, rz_old_mix = sum1]; beta
   FIN_INIT_RES = 5,     // rr = sum0 ; relres
   FIN_INIT_RZ = 6,      // rz = sum0
+  FIN_BLOCK_RES = 7,    // nsum column norms ||R_j||^2 (to dst when given); rr = max; test, iter++
 };
 
 // Reduction plumbing of one reducing launch: per-block partials, a ticket
 // counter and what the last block does with the total.
+// With ncol > 1 the launch solves ncol independent columns (right-hand
+// sides): block b belongs to column b % ncol, each column has its own ticket,
+// scalars (s + col) and destination (dst + col * nsum), and the grid size is a
+// multiple of ncol.
 struct RedArgs {
   double* partials;     // [nblocks * nsum]
-  unsigned* ticket;     // zero before the launch, reset by the last block
-  double* dst;          // FIN_STORE destination (nsum values)
-  PcgScalars* s;        // scalars for FIN_PCG_*
+  unsigned* ticket;     // [ncol], zero before the launch, reset by the column's last block
+  double* dst;          // FIN_STORE destination (nsum values per column)
+  PcgScalars* s;        // scalars for FIN_PCG_* (one per column)
   int op;
   int nsum;             // 1 or 2 sums per thread
+  int ncol = 1;         // columns of a batched pass (block b works on column b % ncol)
 };
+
+// Halt flag of column col given the flag of column 0 (flags live in an array
+// of PcgScalars).
+__device__ __forceinline__ bool halted(const int* halt0, int col) {
+  return halt0 && *((volatile const int*)((const char*)halt0 + (size_t)col * sizeof(PcgScalars)));
+}
 
 __device__ __forceinline__ double warp_sum(double v) {
 #pragma unroll
@@ -109,11 +121,11 @@ __device__ __forceinline__ double warp_sum(double v) {
   return v;
 }
 
-__device__ __forceinline__ void finalize_scalars(const RedArgs& r, const double* tot) {
-  PcgScalars* s = r.s;
+__device__ __forceinline__ void finalize_scalars(const RedArgs& r, const double* tot, int col) {
+  PcgScalars* s = r.s ? r.s + col : nullptr;
   switch (r.op) {
     case FIN_STORE:
-      for (int q = 0; q < r.nsum; ++q) r.dst[q] = tot[q];
+      for (int q = 0; q < r.nsum; ++q) r.dst[col * r.nsum + q] = tot[q];
       break;
     case FIN_PCG_ALPHA: {
       s->pAp = tot[0];
@@ -175,6 +187,27 @@ __device__ __forceinline__ void finalize_scalars(const RedArgs& r, const double*
     case FIN_INIT_RZ:
       s->rz = tot[0];
       break;
+    case FIN_BLOCK_RES: {
+      double mx = 0.0;
+      bool bad = false;
+      for (int q = 0; q < r.nsum; ++q) {
+        if (r.dst) r.dst[q] = tot[q];
+        if (!(tot[q] == tot[q]) || isinf(tot[q])) bad = true;
+        mx = fmax(mx, tot[q]);
+      }
+      s->rr = mx;
+      s->iter += 1;
+      const double rel = sqrt(mx) / s->bnorm;
+      s->relres = rel;
+      if (bad) {
+        s->status = 2; s->halt = 1;
+      } else if (rel < s->tol) {
+        s->status = 1; s->halt = 1;
+      }
+      if (rel < s->best_rel) s->best_rel = rel;
+      if (!s->halt && s->iter >= s->max_iter) s->halt = 1;
+      break;
+    }
     default:
       break;
   }
@@ -191,7 +224,10 @@ __device__ __forceinline__ void block_reduce_finalize(const RedArgs& r, double (
   const int nthr = blockDim.x * blockDim.y * blockDim.z;
   const int lane = tid & 31, wid = tid >> 5, nw = (nthr + 31) >> 5;
   const long long bid = blockIdx.x + (long long)gridDim.x * (blockIdx.y + (long long)gridDim.y * blockIdx.z);
-  const long long nb = (long long)gridDim.x * gridDim.y * gridDim.z;
+  const long long nball = (long long)gridDim.x * gridDim.y * gridDim.z;
+  const int ncol = r.ncol > 1 ? r.ncol : 1;
+  const int col = (int)(bid % ncol);
+  const long long nb = nball / ncol;  // blocks of this column
 #pragma unroll
   for (int q = 0; q < NSUM; ++q) {
     double t = warp_sum(v[q]);
@@ -207,7 +243,7 @@ __device__ __forceinline__ void block_reduce_finalize(const RedArgs& r, double (
     }
     if (lane == 0) {
       __threadfence();
-      unsigned tk = atomicAdd(r.ticket, 1u);
+      unsigned tk = atomicAdd(r.ticket + col, 1u);
       am_last = (tk == (unsigned)(nb - 1));
     }
   }
@@ -220,7 +256,7 @@ __device__ __forceinline__ void block_reduce_finalize(const RedArgs& r, double (
   for (int q = 0; q < NSUM; ++q) acc[q] = 0.0;
   for (long long b = tid; b < nb; b += nthr) {
 #pragma unroll
-    for (int q = 0; q < NSUM; ++q) acc[q] += ((volatile double*)r.partials)[b * NSUM + q];
+    for (int q = 0; q < NSUM; ++q) acc[q] += ((volatile double*)r.partials)[(b * ncol + col) * NSUM + q];
   }
   __syncthreads();
 #pragma unroll
@@ -237,8 +273,8 @@ __device__ __forceinline__ void block_reduce_finalize(const RedArgs& r, double (
       for (int w = 0; w < nw; ++w) t += sred[q][w];
       tot[q] = t;
     }
-    finalize_scalars(r, tot);
-    *r.ticket = 0u;
+    finalize_scalars(r, tot, col);
+    r.ticket[col] = 0u;
   }
 }
 

@@ -35,6 +35,8 @@ struct OpArgs {
   int diag_quirk;
   RedArgs red;
   const int* halt;  // nullable: PcgScalars::halt
+  int ncol = 1;     // columns (x, b, y, xin advance by ndof per column); the dot
+                    // modes sum over all columns
 };
 
 template <typename T>
@@ -47,7 +49,10 @@ int op_pick_kchunk(const Grid& g);
 ModalK<float> modal_to_f32(const ModalK<double>& K);
 
 // ------------------------------------------------------------ vector passes
-// All vectors are full-length AoS (3*nNodes) and zero at fixed DOFs.
+// All vectors are full-length AoS (3*nNodes) and zero at fixed DOFs.  The
+// PCG passes take n = the length of one column; with RedArgs::ncol > 1 they
+// work on ncol consecutive columns (per-column scalars and reductions; a
+// diagonal is shared by the columns).
 template <typename T>
 void launch_fill(T* v, T val, long long n, cudaStream_t st);
 void launch_fill_u32(unsigned* v, unsigned val, long long n, cudaStream_t st);
@@ -73,17 +78,20 @@ void launch_pcg_update(T* x, T* r, T* z, const T* p, const T* q, const T* dinv, 
                        const RedArgs& red, int nblocks, const PcgScalars* s, cudaStream_t st);
 // p = z + beta p
 template <typename T>
-void launch_p_update(T* p, const T* z, long long n, const PcgScalars* s, cudaStream_t st);
+void launch_p_update(T* p, const T* z, long long n, const PcgScalars* s, cudaStream_t st, int ncol = 1);
+// x = a[c] x + y per column c (a: ncol device doubles)
+template <typename T>
+void launch_scale_add_cols(T* x, const double* a, const T* y, long long n, int ncol, cudaStream_t st);
 // z = dinv * r (Jacobi) ; rz = r.z
 template <typename T>
 void launch_jacobi_precond(T* z, const T* r, const T* dinv, long long n, const RedArgs& red,
                            int nblocks, const int* halt, cudaStream_t st);
 // dst32 = (T32)(src64 * scale)
 void launch_scale_to_f32(float* dst, const double* src, const double* scale, long long n,
-                         cudaStream_t st);
+                         cudaStream_t st, int ncol = 1);
 // u64 += (double)d32 / scale
 void launch_add_scaled_f32(double* u, const float* d, const double* scale, long long n,
-                           cudaStream_t st);
+                           cudaStream_t st, int ncol = 1);
 // x = a*x + b*y with host scalars
 template <typename T>
 void launch_axpby(T* x, T a, const T* y, T b, long long n, cudaStream_t st);
@@ -141,5 +149,35 @@ void launch_oc_volumes(const double* x, const double* dc, const double* dv, long
                        cudaStream_t st);
 void launch_oc_apply(const double* x, const double* dc, const double* dv, long long n, double lam,
                      double move, double* xout, cudaStream_t st);
+
+
+// ---- block PCG over k <= kMaxBlockCols columns (block.cu) ----------------
+constexpr int kMaxBlockCols = 16;
+constexpr int kBlockRedBlocks = 608;  // grid of the reducing block passes
+int block_kc(int k);                  // compiled column count (1, 2, 4, 8, 16) for k
+long long block_partials_needed(int k);
+// out[i * NBC + j] = a_i . b_j over the columns (NBC = kc or 2 kc; b_j = b1_j,
+// then b2_j when b2 is given); the last block writes out in a fixed order
+template <typename T>
+void launch_gram(const T* a, const T* b1, const T* b2, int k, long long n, double* partials, unsigned* ticket,
+                 double* out, const int* halt, cudaStream_t st);
+// out = sign * G^+ rhs (k x k, G symmetrised from g, pivots below eps * G_jj dropped)
+void launch_block_solve(const double* g, int ldg, const double* r, int ldr, int roff, int k, double sign, double eps,
+                        double* out, const int* halt, cudaStream_t st);
+// X += P alpha, R -= Q alpha, column norms of R reduced with red (FIN_BLOCK_RES)
+template <typename T>
+void launch_block_update(T* X, T* R, const T* P, const T* Q, const double* alpha, int k, long long n,
+                         const RedArgs& red, cudaStream_t st);
+template <typename T>
+void launch_block_p_update(T* P, const T* Z, const double* beta, int k, long long n, const int* halt,
+                           cudaStream_t st);
+template <typename T>
+void launch_cols_jacobi(T* z, const T* r, const T* dinv, long long n, int k, const int* halt, cudaStream_t st);
+// dst_j = (T)(src_j * scale[j])
+template <typename T>
+void launch_cols_from64(T* dst, const double* src, const double* scale, long long n, int k, cudaStream_t st);
+// u_j += d_j / scale[j] (columns with scale 0 are left alone)
+template <typename T>
+void launch_cols_accum(double* u, const T* d, const double* scale, long long n, int k, cudaStream_t st);
 
 }  // namespace hexa

@@ -155,7 +155,7 @@ __device__ __forceinline__ void element_modal(const ModalK<T>& K, const T (&L)[4
 template <typename T, int MODE, int TYW, typename IX>
 __device__ __forceinline__ void op_item(const OpArgs<T>& a, int tx, int ty, int chunk,
                                         T (&xch)[2][TYW][32][(MODE == OP_JACOBI || MODE == OP_CHEB2) ? 4 : 3],
-                                        double& acc0) {
+                                        double& acc0, long long co) {
   constexpr int NX_OWN = 31, NY_OWN = TYW - 1;
   constexpr bool NEED_F = (MODE == OP_JACOBI || MODE == OP_CHEB2);
   const Grid& g = a.g;
@@ -169,7 +169,11 @@ __device__ __forceinline__ void op_item(const OpArgs<T>& a, int tx, int ty, int 
   const IX eplane = (IX)g.nx * g.ny;
   const int in = i0 + lane, jn = j0 + wy;
   const bool own = (lane < NX_OWN) && (wy < NY_OWN) && (in < g.NX) && (jn < g.NY);
-  const T* __restrict__ x = a.x;
+  // column co / ndof of a multi-column apply (the factors are shared)
+  const T* __restrict__ x = a.x + co;
+  const T* __restrict__ bv = a.b ? a.b + co : a.b;
+  T* yv = a.y + co;  // not restrict: CHEB2 runs in place (xin == y)
+  const T* xinv = a.xin ? a.xin + co : a.xin;
   const T* __restrict__ fac = a.fac;
   const ColumnAddr<IX> ca = column_addr<IX>(g, ie, je);
   // Dirichlet bits of this thread's node column: the x/y faces are fixed per
@@ -281,16 +285,16 @@ __device__ __forceinline__ void op_item(const OpArgs<T>& a, int tx, int ty, int 
           out = fixd ? T(0) : Ax;
           accT = fma(xown[c], out, accT);
         } else if (MODE == OP_RESID || MODE == OP_RESID_NORM) {
-          out = fixd ? T(0) : (ldx(a.b + 3 * n + c) - Ax);
+          out = fixd ? T(0) : (ldx(bv + 3 * n + c) - Ax);
           if (MODE == OP_RESID_NORM) accT = fma(out, out, accT);
         } else if (MODE == OP_JACOBI) {  // x + omega (b - Ax) / D
-          out = fixd ? T(0) : fma(a.omega * dinv[c], ldx(a.b + 3 * n + c) - Ax, xown[c]);
+          out = fixd ? T(0) : fma(a.omega * dinv[c], ldx(bv + 3 * n + c) - Ax, xown[c]);
         } else {  // OP_CHEB2: x + c1 (x - x_prev) + c2 D^-1 (b - Ax)
-          const T xp = a.xin ? a.xin[3 * n + c] : T(0);  // plain load: y may alias xin
+          const T xp = xinv ? xinv[3 * n + c] : T(0);  // plain load: y may alias xin
           const T t = fma(a.c1, xown[c] - xp, xown[c]);
-          out = fixd ? T(0) : fma(a.c2 * dinv[c], ldx(a.b + 3 * n + c) - Ax, t);
+          out = fixd ? T(0) : fma(a.c2 * dinv[c], ldx(bv + 3 * n + c) - Ax, t);
         }
-        a.y[3 * n + c] = out;
+        yv[3 * n + c] = out;
       }
     }
 #pragma unroll
@@ -313,7 +317,8 @@ __global__ void __launch_bounds__(32 * TYW) op_kernel(const OpArgs<T> a) {
   for (int item = blockIdx.x; item < items; item += gridDim.x) {
     const int chunk = item / nxy, t = item - chunk * nxy;
     const int ty = t / a.tiles_x, tx = t - ty * a.tiles_x;
-    op_item<T, MODE, TYW, IX>(a, tx, ty, chunk, xch, acc0);
+    // every column of a multi-column apply reuses the item's factors from L1
+    for (int col = 0; col < a.ncol; ++col) op_item<T, MODE, TYW, IX>(a, tx, ty, chunk, xch, acc0, col * a.g.ndof());
   }
   if (MODE == OP_APPLY_DOT || MODE == OP_RESID_NORM) {
     double v[1] = {acc0};

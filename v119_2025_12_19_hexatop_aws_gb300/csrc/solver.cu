@@ -16,7 +16,9 @@
 // convergence and the iteration continues until it meets the tolerance.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <chrono>
+#include <cstdio>
 #include <cmath>
 #include <cstring>
 #include <vector>
@@ -27,7 +29,7 @@
 
 namespace hexa {
 
-void launch_scalars_init(PcgScalars* s, const PcgScalars* parent, int max_iter, cudaStream_t st);
+void launch_scalars_init(PcgScalars* s, const PcgScalars* parent, int max_iter, cudaStream_t st, int ncol = 1);
 
 // ------------------------------------------------------------------ context
 void* Ctx::get(const std::string& name, size_t bytes) {
@@ -456,11 +458,18 @@ double applies_per_iteration(const PcgEnv<T>& E) {
   return 1.0 + per;
 }
 
+template <typename T>
+double applies_per_iteration_mg(const MG<T>* mg) {
+  PcgEnv<T> E;
+  E.mg = const_cast<MG<T>*>(mg);
+  return applies_per_iteration(E);
+}
+
 // Replays groups of PCG iterations (a CUDA graph captured on first use, or
 // direct launches) until the device-side halt flag is set; *h receives the
 // final scalars.  Iterations continue from whatever state E and c.s hold.
 template <typename T>
-bool pcg_drive(Ctx& c, PcgEnv<T>& E, Graph& graph, PcgScalars* h) {
+bool pcg_drive(Ctx& c, PcgEnv<T>& E, Graph& graph, PcgScalars* h, double* ms = nullptr) {
   int G = E.graph_iters < 2 ? 2 : E.graph_iters;
   if (G & 1) ++G;  // even: each group starts with the same z / z_old buffer parity
   if (E.use_graphs && !graph.exec) {
@@ -470,6 +479,7 @@ bool pcg_drive(Ctx& c, PcgEnv<T>& E, Graph& graph, PcgScalars* h) {
       return false;
   }
   double host_best = INFINITY;
+  if (ms) cudaEventRecord(c.ev[2], c.st);
   while (true) {
     if (E.use_graphs) {
       if (!replay(c, graph)) return false;
@@ -486,13 +496,20 @@ bool pcg_drive(Ctx& c, PcgEnv<T>& E, Graph& graph, PcgScalars* h) {
     }
     if (h->halt) break;
   }
+  if (ms) {
+    cudaEventRecord(c.ev[3], c.st);
+    cudaEventSynchronize(c.ev[3]);
+    float t = 0.f;
+    cudaEventElapsedTime(&t, c.ev[2], c.ev[3]);
+    *ms += t;
+  }
   return true;
 }
 
 // Runs PCG from the current E.x.  host_scalars carries tol/max_iter/cadence.
 template <typename T>
 bool run_pcg(Ctx& c, PcgEnv<T>& E, double tol, int max_iter, int cadence, bool x_is_zero, double bnorm,
-             bool div_check, PcgOut* out) {
+             bool div_check, PcgOut* out, double* ms = nullptr) {
   PcgScalars h;
   std::memset(&h, 0, sizeof(h));
   h.tol = tol;
@@ -526,7 +543,7 @@ bool run_pcg(Ctx& c, PcgEnv<T>& E, double tol, int max_iter, int cadence, bool x
 
   Graph graph;
   const int iter0 = 0;
-  if (!pcg_drive<T>(c, E, graph, &h)) return false;
+  if (!pcg_drive<T>(c, E, graph, &h, ms)) return false;
   out->status = h.status;
   out->iters = h.iter - iter0;
   out->relres = h.relres;
@@ -793,11 +810,67 @@ int solve_plain(Ctx& c, const Problem& P, const hexa_solve_params& prm, const do
   st->shift = sigma;
   st->precond_used = use_mg ? HEXA_PRECOND_USED_MULTIGRID : HEXA_PRECOND_USED_JACOBI;
   st->mg_levels = use_mg ? (int)mg.L.size() : 1;
+  st->smooth_steps = use_mg ? mg.nu2 : 0;
   st->fine_applies = applies;
   st->fine_applies_fp64 = Is64<T>::v ? applies : 1.0;
   if (!c.cuda_ok("solve")) return HEXA_ERR_CUDA;
   (void)last;
   return success ? HEXA_OK : HEXA_NOT_CONVERGED;
+}
+
+// Autotuner of the mixed form's multigrid: short FP32 GMG-PCG trials on
+// b = f/||f|| pick the level count (stage 1) and the Chebyshev smoothing steps
+// per side (stage 2) that minimise the estimated time to the tolerance,
+// (log10(1/tol) / digits gained per iteration) * device time per iteration.
+// The choice is cached in the context per grid.
+std::pair<int, int> autotune_mixed(Ctx& c, const Problem& P, const hexa_solve_params& prm, float* fac32,
+                                   const ModalK<float>& K32, double sigma, PcgEnv<float>& E, float* b32,
+                                   double bnorm, MG<float>& mg) {
+  char key[96];
+  std::snprintf(key, sizeof(key), "%d,%d,%d,%d,%g,%g", P.g.nx, P.g.ny, P.g.nz, prm.diag_quirk, P.nu, prm.tol);
+  auto it = c.tuned.find(key);
+  if (it != c.tuned.end()) return it->second;
+  const long long n = P.g.ndof();
+  c.hscal[12] = 1.0 / bnorm;
+  cudaMemcpyAsync(c.dscal + 12, c.hscal + 12, sizeof(double), cudaMemcpyHostToDevice, c.st);
+  launch_scale_to_f32(b32, P.f64, c.dscal + 12, n, c.st);
+  c.launches++;
+  const double digits = std::log10(1.0 / prm.tol);
+  const int lmax = plan_levels(P.g, 16);
+  const int trial_iters = 60;
+  auto trial = [&](int levels, int nu) -> double {
+    hexa_solve_params q = prm;
+    q.pre_smooth = q.post_smooth = nu;
+    mg = MG<float>();
+    mg.K = K32;
+    configure_mg<float>(mg, P, q);
+    if (!build_mg<float>(c, mg, P.g, P.m, fac32, levels, "mg32_")) return INFINITY;
+    mg_set_shift<float>(c, mg, sigma);
+    E.L0 = &mg.L[0];
+    E.mg = &mg;
+    E.b = b32;
+    launch_fill<float>(E.x, 0.0f, n, c.st);
+    c.launches++;
+    PcgOut o;
+    double ms = 0.0;
+    if (!run_pcg<float>(c, E, 1e-30, trial_iters, 1, true, 1.0, false, &o, &ms) || o.iters < 2) return INFINITY;
+    const double rel = o.relres;
+    if (!(rel > 0.0) || !(rel < 1.0)) return INFINITY;
+    const double per_digit = o.iters / (-std::log10(rel));
+    return digits * per_digit * (ms / o.iters);
+  };
+  int best_l = std::max(2, lmax), best_nu = 3;
+  double best = INFINITY;
+  for (int l = std::max(2, lmax - 2); l <= lmax; ++l) {
+    const double t = trial(l, 3);
+    if (t < best) best = t, best_l = l;
+  }
+  for (int nu : {2, 4, 5}) {
+    const double t = trial(best_l, nu);
+    if (t < best) best = t, best_nu = nu;
+  }
+  c.tuned[key] = {best_l, best_nu};
+  return {best_l, best_nu};
 }
 
 // Mixed precision: FP64 iterative refinement around FP32 GMG-PCG correction
@@ -853,10 +926,17 @@ int solve_mixed(Ctx& c, const Problem& P, const hexa_solve_params& prm, const do
   if (!E.x || !E.r || !E.zA || !E.zB || !E.p || !E.q || !E.dinv || !b32 || !r64) return HEXA_ERR_NOMEM;
   MG<float> mg;
   const bool use_mg = prm.precond == HEXA_PRECOND_MULTIGRID;
+  hexa_solve_params prm2 = prm;
+  if (use_mg && prm.autotune) {
+    const std::pair<int, int> t = autotune_mixed(c, P, prm, fac32, K32, sigma, E, b32, bnorm, mg);
+    prm2.mg_levels = t.first;
+    prm2.pre_smooth = prm2.post_smooth = t.second;
+  }
   if (use_mg) {
-    const int nlev = plan_levels(P.g, prm.mg_levels);
+    const int nlev = plan_levels(P.g, prm2.mg_levels);
+    mg = MG<float>();
     mg.K = K32;
-    configure_mg<float>(mg, P, prm);
+    configure_mg<float>(mg, P, prm2);
     if (!build_mg<float>(c, mg, P.g, P.m, fac32, nlev, "mg32_")) return HEXA_ERR_NOMEM;
     mg.L[0].kchunk = L0.kchunk;
     mg_set_shift<float>(c, mg, sigma);
@@ -989,9 +1069,256 @@ int solve_mixed(Ctx& c, const Problem& P, const hexa_solve_params& prm, const do
   st->shift = sigma;
   st->precond_used = use_mg ? HEXA_PRECOND_USED_MULTIGRID : HEXA_PRECOND_USED_JACOBI;
   st->mg_levels = use_mg ? (int)mg.L.size() : 1;
+  st->smooth_steps = use_mg ? mg.nu2 : 0;
   st->fine_applies = applies32 + applies64;
   st->fine_applies_fp64 = applies64;
   if (!c.cuda_ok("mixed solve")) return HEXA_ERR_CUDA;
+  return status;
+}
+
+// k load cases as one block PCG (block.cu) on the columns of F (k <= 16).
+// T = float: FP32 operator, V-cycles and block recursion, carried across
+// reliable updates -- whenever every active column's recursive residual has
+// dropped by inner_tol, the FP32 corrections are added to the FP64 iterate
+// U, the FP64 true residuals F - (K + sigma I) U replace the FP32 residuals
+// (each rescaled to unit norm) and the iteration continues with its search
+// directions, which the block A-orthogonalisation keeps valid.  A column
+// whose true relative residual meets tol is frozen (its scale set to 0: zero
+// residual, no further correction).  T = double: the same loop in FP64.
+template <typename T>
+int solve_block(Ctx& c, const Problem& P, int k, const hexa_solve_params& prm, double* U, hexa_solve_stats* st) {
+  const long long n = P.g.ndof();
+  ModalK<double> K64;
+  double max_diag = 0, f0norm = 0;
+  cudaEventRecord(c.ev[0], c.st);
+  if (!setup_common(c, P, prm, &K64, &max_diag, &f0norm)) return c.err.empty() ? HEXA_ERR_CUDA : HEXA_ERR_NOMEM;
+  st->max_diag = max_diag;
+  if (std::isnan(max_diag) || std::isinf(max_diag)) {
+    c.err = "Stiffness Matrix Diagonal contains NaN/Inf";
+    cudaMemsetAsync(U, 0, sizeof(double) * n * k, c.st);
+    st->relres = NAN;
+    return HEXA_ERR_CORRUPT_INPUT;
+  }
+  const double sigma = prm.shift_factor * max_diag;
+  const int kc = block_kc(k);
+  if (!c.ensure_partials((size_t)block_partials_needed(k) + 4096)) return HEXA_ERR_NOMEM;
+  ModalK<T> K;
+  if (Is64<T>::v) std::memcpy(&K, &K64, sizeof(K));
+  else {
+    ModalK<float> kf = modal_to_f32(K64);
+    std::memcpy(&K, &kf, sizeof(K));
+  }
+  const T* fac = Host<T>::fac(c, P);
+  T* X = c.vec<T>("blk_X", n * k);
+  T* R = c.vec<T>("blk_R", n * k);
+  T* Z = c.vec<T>("blk_Z", n * k);
+  T* Pd = c.vec<T>("blk_P", n * k);
+  T* Q = c.vec<T>("blk_Q", n * k);
+  T* dinv = c.vec<T>("blk_dinv", n);
+  double* R64 = c.vec<double>("blk_R64", n * k);
+  // small arrays: gram1 (kc x 2kc), gram2 (kc x kc), alpha, beta (k x k),
+  // column norms, scales
+  double* sm = c.vec<double>("blk_small", 4096);
+  if (!fac || !X || !R || !Z || !Pd || !Q || !dinv || !R64 || !sm) return HEXA_ERR_NOMEM;
+  double *gram1 = sm, *gram2 = sm + 1024, *alpha = sm + 1536, *beta = sm + 1792, *rr = sm + 2048,
+         *fn2 = sm + 2080, *rn2 = sm + 2112, *scale = sm + 2144, *comp = sm + 2176;
+  double* hsm = c.hscal;  // 64 pinned doubles: [0,k) norms, [16, 16+k) scales
+  unsigned* gticket = c.ticket + 32;
+  cudaMemsetAsync(gticket, 0, sizeof(unsigned), c.st);
+  // column norms of F
+  {
+    RedArgs r = red(c, FIN_STORE, 1, nullptr, fn2);
+    r.ncol = k;
+    launch_dot<double>(P.f64, P.f64, (const double*)nullptr, (const double*)nullptr, n, r, kRedBlocks * k, nullptr,
+                       c.st);
+    c.launches++;
+  }
+  cudaMemcpyAsync(hsm, fn2, sizeof(double) * k, cudaMemcpyDeviceToHost, c.st);
+  if (cudaStreamSynchronize(c.st) != cudaSuccess) return c.cuda_ok("block setup") ? HEXA_ERR_CUDA : HEXA_ERR_CUDA;
+  std::vector<double> fnorm(k);
+  for (int j = 0; j < k; ++j) fnorm[j] = std::sqrt(std::fmax(hsm[j], 0.0));
+
+  Lev<T> L0;
+  L0.g = P.g;
+  L0.m = P.m;
+  L0.fac = const_cast<T*>(fac);
+  L0.kchunk = pick_kchunk<T>(P.g);
+  L0.sigma = (T)sigma;
+  MG<T> mg;
+  const bool use_mg = prm.precond == HEXA_PRECOND_MULTIGRID;
+  if (use_mg) {
+    hexa_solve_params prm2 = prm;
+    auto it = c.tuned.find(std::to_string(P.g.nx) + "x" + std::to_string(P.g.ny) + "x" + std::to_string(P.g.nz) +
+                           (Is64<T>::v ? "/64" : "/32"));
+    if (prm.autotune && it != c.tuned.end()) {
+      prm2.mg_levels = it->second.first;
+      prm2.pre_smooth = prm2.post_smooth = it->second.second;
+    }
+    mg.K = K;
+    configure_mg<T>(mg, P, prm2);
+    if (!build_mg<T>(c, mg, P.g, P.m, fac, plan_levels(P.g, prm2.mg_levels),
+                     std::string(Is64<T>::v ? "mg64_" : "mg32_")))
+      return HEXA_ERR_NOMEM;
+    mg.L[0].kchunk = L0.kchunk;
+    mg_set_shift<T>(c, mg, sigma);
+  } else {
+    launch_diag<T>(P.g, P.m, fac, K, prm.diag_quirk, (T)sigma, nullptr, dinv, c.st);
+    c.launches++;
+  }
+  Lev<T>& LA = use_mg ? mg.L[0] : L0;
+  Lev<double> L64;
+  L64.g = P.g;
+  L64.m = P.m;
+  L64.fac = const_cast<double*>(P.fac64);
+  L64.sigma = sigma;
+  L64.kchunk = pick_kchunk<double>(P.g);
+
+  // start: U = 0, P = Q = 0, G = identity (so the first beta is zero)
+  launch_fill<double>(U, 0.0, n * k, c.st);
+  launch_fill<T>(Pd, T(0), n * k, c.st);
+  launch_fill<T>(Q, T(0), n * k, c.st);
+  launch_fill<double>(gram1, 0.0, 1024, c.st);
+  c.launches += 4;
+  {
+    std::vector<double> id((size_t)kc * 2 * kc, 0.0);
+    for (int j = 0; j < kc; ++j) id[(size_t)j * 2 * kc + j] = 1.0;
+    cudaMemcpyAsync(gram1, id.data(), id.size() * sizeof(double), cudaMemcpyHostToDevice, c.st);
+    cudaStreamSynchronize(c.st);
+  }
+  const int* halt = &c.s->halt;
+  const double eps = Is64<T>::v ? 1e-12 : 1e-6;
+  auto iteration = [&]() {
+    if (use_mg) {
+      for (int j = 0; j < k; ++j) vcycle<T>(c, mg, 0, R + (long long)j * n, Z + (long long)j * n, halt);
+    } else {
+      launch_cols_jacobi<T>(Z, R, dinv, n, k, halt, c.st);
+      c.launches++;
+    }
+    launch_gram<T>(Q, Z, (const T*)nullptr, k, n, c.partials, gticket, gram2, halt, c.st);
+    launch_block_solve(gram1, 2 * kc, gram2, kc, 0, k, -1.0, eps, beta, halt, c.st);
+    launch_block_p_update<T>(Pd, Z, beta, k, n, halt, c.st);
+    OpArgs<T> a = opargs<T>(LA, K, prm.diag_quirk, Pd, nullptr, Q, T(0), halt, red(c, FIN_NONE, 1, nullptr));
+    a.ncol = k;
+    op<T>(c, OP_APPLY, a);
+    launch_gram<T>(Pd, Q, R, k, n, c.partials, gticket, gram1, halt, c.st);
+    launch_block_solve(gram1, 2 * kc, gram1, 2 * kc, kc, k, 1.0, eps, alpha, halt, c.st);
+    RedArgs ru = red(c, FIN_BLOCK_RES, k, c.s, rr);
+    launch_block_update<T>(X, R, Pd, Q, alpha, k, n, ru, c.st);
+    c.launches += 6;
+  };
+  auto true_residuals = [&](std::vector<double>& rel) -> bool {
+    OpArgs<double> a = opargs<double>(L64, K64, prm.diag_quirk, U, P.f64, R64, 0.0, nullptr, red(c, FIN_NONE, 1, nullptr));
+    a.ncol = k;
+    op<double>(c, OP_RESID, a);
+    RedArgs r = red(c, FIN_STORE, 1, nullptr, rn2);
+    r.ncol = k;
+    launch_dot<double>(R64, R64, (const double*)nullptr, (const double*)nullptr, n, r, kRedBlocks * k, nullptr, c.st);
+    c.launches++;
+    cudaMemcpyAsync(hsm, rn2, sizeof(double) * k, cudaMemcpyDeviceToHost, c.st);
+    if (cudaStreamSynchronize(c.st) != cudaSuccess) return c.cuda_ok("block residual");
+    for (int j = 0; j < k; ++j) rel[j] = fnorm[j] > 0 ? std::sqrt(std::fmax(hsm[j], 0.0)) / fnorm[j] : 0.0;
+    return true;
+  };
+  if (!c.cuda_ok("block setup")) return HEXA_ERR_CUDA;
+  cudaEventRecord(c.ev[1], c.st);
+
+  std::vector<double> rel(k, 0.0);
+  const double inner_tol = Is64<T>::v ? 0.0 : (prm.inner_tol > 0 ? prm.inner_tol : 1e-4);
+  const int max_outer = prm.max_outer > 0 ? prm.max_outer : 20;
+  int outer = 0, status = HEXA_OK, applies64 = 0;
+  PcgScalars h;
+  std::memset(&h, 0, sizeof(h));
+  h.max_iter = prm.max_iter;
+  h.bnorm = 1.0;
+  h.best_rel = INFINITY;
+  h.no_div = 1;
+  Graph graph;
+  int G = prm.graph_iters > 0 ? prm.graph_iters : 10;
+  const bool graphs = prm.use_graphs != 0;
+  double worst = 0.0;
+  while (true) {
+    if (!true_residuals(rel)) return HEXA_ERR_CUDA;
+    ++applies64;
+    worst = 0.0;
+    for (int j = 0; j < k; ++j) worst = std::fmax(worst, rel[j]);
+    if (!(worst == worst)) {
+      status = HEXA_NOT_CONVERGED;
+      break;
+    }
+    if (worst <= prm.tol) break;
+    if (outer >= max_outer || h.iter >= prm.max_iter || h.status == 2) {
+      status = HEXA_NOT_CONVERGED;
+      break;
+    }
+    // rescale: active columns to unit norm, converged ones frozen
+    double need = 1.0;  // scaled residual that brings every active column to tol
+    for (int j = 0; j < k; ++j) {
+      const double rn = rel[j] * fnorm[j];
+      hsm[16 + j] = (rel[j] <= prm.tol || rn == 0.0) ? 0.0 : 1.0 / rn;
+      if (hsm[16 + j] != 0.0) need = std::fmin(need, prm.tol / rel[j]);
+    }
+    cudaMemcpyAsync(scale, hsm + 16, sizeof(double) * k, cudaMemcpyHostToDevice, c.st);
+    launch_cols_from64<T>(R, R64, scale, n, k, c.st);
+    launch_fill<T>(X, T(0), n * k, c.st);
+    c.launches += 2;
+    // the FP64 recursion runs to the outer tolerance in one pass
+    h.tol = Is64<T>::v ? 0.5 * need : std::fmax(inner_tol, 0.5 * need);
+    h.halt = 0;
+    h.status = 0;
+    h.best_rel = INFINITY;
+    *c.hs = h;
+    cudaMemcpyAsync(c.s, c.hs, sizeof(PcgScalars), cudaMemcpyHostToDevice, c.st);
+    if (graphs && !graph.exec) {
+      if (!capture(c, graph, [&]() {
+            for (int i = 0; i < G; ++i) iteration();
+          }))
+        return HEXA_ERR_CUDA;
+    }
+    while (true) {
+      if (graphs) {
+        if (!replay(c, graph)) return HEXA_ERR_CUDA;
+      } else {
+        for (int i = 0; i < G; ++i) iteration();
+      }
+      cudaMemcpyAsync(c.hs, c.s, sizeof(PcgScalars), cudaMemcpyDeviceToHost, c.st);
+      if (cudaStreamSynchronize(c.st) != cudaSuccess) return c.cuda_ok("block pcg") ? HEXA_ERR_CUDA : HEXA_ERR_CUDA;
+      h = *c.hs;
+      if (h.halt) break;
+    }
+    ++outer;
+    launch_cols_accum<T>(U, X, scale, n, k, c.st);
+    c.launches++;
+  }
+  // compliance: equal-weighted sum over the load cases of f_j . u_j
+  {
+    RedArgs r = red(c, FIN_STORE, 1, nullptr, comp);
+    r.ncol = k;
+    launch_dot<double>(P.f64, U, (const double*)nullptr, (const double*)nullptr, n, r, kRedBlocks * k, nullptr, c.st);
+    c.launches++;
+  }
+  cudaMemcpyAsync(hsm, comp, sizeof(double) * k, cudaMemcpyDeviceToHost, c.st);
+  cudaEventRecord(c.ev[2], c.st);
+  cudaEventSynchronize(c.ev[2]);
+  double compl_sum = 0.0;
+  for (int j = 0; j < k; ++j) compl_sum += hsm[j];
+  float ms1 = 0, ms2 = 0;
+  cudaEventElapsedTime(&ms1, c.ev[0], c.ev[1]);
+  cudaEventElapsedTime(&ms2, c.ev[1], c.ev[2]);
+  st->setup_ms = ms1;
+  st->solve_ms = ms2;
+  st->iterations = h.iter;
+  st->outer_iterations = outer;
+  st->attempts = 1;
+  st->relres = worst;
+  st->true_relres = worst;
+  st->shift = sigma;
+  st->compliance = compl_sum;
+  st->precond_used = use_mg ? HEXA_PRECOND_USED_MULTIGRID : HEXA_PRECOND_USED_JACOBI;
+  st->mg_levels = use_mg ? (int)mg.L.size() : 1;
+  st->smooth_steps = use_mg ? mg.nu2 : 0;
+  st->fine_applies = (applies_per_iteration_mg(use_mg ? &mg : nullptr)) * h.iter * k + applies64 * k;
+  st->fine_applies_fp64 = Is64<T>::v ? st->fine_applies : (double)applies64 * k;
+  if (!c.cuda_ok("block solve")) return HEXA_ERR_CUDA;
   return status;
 }
 
@@ -1005,6 +1332,43 @@ int solve_problem(Ctx& c, const Problem& P, const hexa_solve_params& prm, const 
     case HEXA_PREC_MIXED: return solve_mixed(c, P, prm, u0, u, st);
     default: c.err = "unknown precision"; return HEXA_ERR_ARG;
   }
+}
+
+int multi_rhs_problem(Ctx& c, const Problem& P, int k, const double* F_dev, const hexa_solve_params& prm,
+                      double* U_dev, hexa_solve_stats* st) {
+  // groups of up to 16 columns, each one block PCG
+  const long long n = P.g.ndof();
+  hexa_solve_stats acc;
+  std::memset(&acc, 0, sizeof(acc));
+  int worst = HEXA_OK;
+  for (int j0 = 0; j0 < k; j0 += kMaxBlockCols) {
+    const int kb = std::min(kMaxBlockCols, k - j0);
+    Problem Q = P;
+    Q.f64 = F_dev + (long long)j0 * n;
+    hexa_solve_stats s1;
+    std::memset(&s1, 0, sizeof(s1));
+    int rc = (prm.precision == HEXA_PREC_FP64) ? solve_block<double>(c, Q, kb, prm, U_dev + (long long)j0 * n, &s1)
+                                              : solve_block<float>(c, Q, kb, prm, U_dev + (long long)j0 * n, &s1);
+    if (rc < 0) return rc;
+    if (rc > worst) worst = rc;
+    acc.iterations += s1.iterations;
+    acc.outer_iterations += s1.outer_iterations;
+    acc.attempts = 1;
+    acc.setup_ms += s1.setup_ms;
+    acc.solve_ms += s1.solve_ms;
+    acc.compliance += s1.compliance;
+    acc.relres = std::fmax(acc.relres, s1.relres);
+    acc.true_relres = std::fmax(acc.true_relres, s1.true_relres);
+    acc.fine_applies += s1.fine_applies;
+    acc.fine_applies_fp64 += s1.fine_applies_fp64;
+    acc.precond_used = s1.precond_used;
+    acc.mg_levels = s1.mg_levels;
+    acc.smooth_steps = s1.smooth_steps;
+    acc.shift = s1.shift;
+    acc.max_diag = s1.max_diag;
+  }
+  *st = acc;
+  return worst;
 }
 
 }  // namespace hexa

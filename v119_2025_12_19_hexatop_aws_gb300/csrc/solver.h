@@ -27,6 +27,8 @@ struct Ctx {
   PcgScalars* s2 = nullptr;  // coarse-level PCG
   double* dscal = nullptr;   // 64 device doubles of scratch results
   PcgScalars* hs = nullptr;  // pinned host mirror of s
+  // autotuned multigrid settings per grid and precision: {levels, smoothing steps}
+  std::map<std::string, std::pair<int, int>> tuned;
   double* hscal = nullptr;   // pinned host mirror of dscal
 
   void* get(const std::string& name, size_t bytes);

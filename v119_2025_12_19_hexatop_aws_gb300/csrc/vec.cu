@@ -8,6 +8,8 @@
 // block reductions; the coefficients (alpha, beta) and the convergence test
 // live in device memory, so no scalar ever returns to the host inside an
 // iteration.
+#include <algorithm>
+
 #include "hexa_common.cuh"
 #include "hexa_kernels.h"
 
@@ -169,19 +171,41 @@ void launch_max(const double* v, long long n, const RedArgs& red, int nblocks, c
   max_kernel<<<nblocks, 256, 0, st>>>(v, n, red);
 }
 
+// Column mapping of the batched passes: block b works on column b % ncol as
+// block b / ncol of that column's gridDim.x / ncol blocks.
+struct ColMap {
+  int col;
+  long long first, stride;
+};
+__device__ __forceinline__ ColMap colmap(int ncol) {
+  const int nc = ncol > 1 ? ncol : 1;
+  ColMap m;
+  m.col = (int)(blockIdx.x % nc);
+  const long long j = blockIdx.x / nc, nbc = gridDim.x / nc;
+  m.first = j * blockDim.x + threadIdx.x;
+  m.stride = nbc * blockDim.x;
+  return m;
+}
+static inline int col_blocks(int nblocks, int ncol) {
+  const int nc = ncol > 1 ? ncol : 1;
+  const int per = std::max(1, nblocks / nc);
+  return per * nc;
+}
+
 template <typename T, int NS>
 __global__ void dot_kernel(const T* __restrict__ a, const T* __restrict__ b, const T* __restrict__ c,
                            const T* __restrict__ d, long long n, RedArgs red, const int* halt) {
-  if (halt && *((volatile const int*)halt)) return;
+  const ColMap cm = colmap(red.ncol);
+  if (halted(halt, cm.col)) return;
+  const long long off = (long long)cm.col * n;
   double acc[NS];
   T part[NS];
 #pragma unroll
   for (int q = 0; q < NS; ++q) acc[q] = 0.0, part[q] = T(0);
   int cnt = 0;
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
-       i += (long long)gridDim.x * blockDim.x) {
-    part[0] = fma(a[i], b[i], part[0]);
-    if (NS > 1) part[NS - 1] = fma(c[i], d[i], part[NS - 1]);
+  for (long long i = cm.first; i < n; i += cm.stride) {
+    part[0] = fma(a[off + i], b[off + i], part[0]);
+    if (NS > 1) part[NS - 1] = fma(c[off + i], d[off + i], part[NS - 1]);
     if (++cnt == kChunk) flush_parts<T, NS>(acc, part, cnt);
   }
   flush_parts<T, NS>(acc, part, cnt);
@@ -190,8 +214,9 @@ __global__ void dot_kernel(const T* __restrict__ a, const T* __restrict__ b, con
 template <typename T>
 void launch_dot(const T* a, const T* b, const T* c, const T* d, long long n, const RedArgs& red,
                 int nblocks, const int* halt, cudaStream_t st) {
-  if (c) dot_kernel<T, 2><<<nblocks, 256, 0, st>>>(a, b, c, d, n, red, halt);
-  else dot_kernel<T, 1><<<nblocks, 256, 0, st>>>(a, b, c, d, n, red, halt);
+  const int g = col_blocks(nblocks, red.ncol);
+  if (c) dot_kernel<T, 2><<<g, 256, 0, st>>>(a, b, c, d, n, red, halt);
+  else dot_kernel<T, 1><<<g, 256, 0, st>>>(a, b, c, d, n, red, halt);
 }
 
 template <typename T, bool JAC>
@@ -199,23 +224,25 @@ __global__ void pcg_update_kernel(T* __restrict__ x, T* __restrict__ r, T* __res
                                   const T* __restrict__ p, const T* __restrict__ q,
                                   const T* __restrict__ dinv, long long n, RedArgs red,
                                   const PcgScalars* s) {
-  if (*((volatile const int*)&s->halt)) return;
-  const T alpha = (T)s->alpha;
+  const ColMap cm = colmap(red.ncol);
+  if (*((volatile const int*)&s[cm.col].halt)) return;
+  const T alpha = (T)s[cm.col].alpha;
+  const long long off = (long long)cm.col * n;
   constexpr int NS = JAC ? 2 : 1;
   double acc[NS];
   T part[NS];
 #pragma unroll
   for (int q2 = 0; q2 < NS; ++q2) acc[q2] = 0.0, part[q2] = T(0);
   int cnt = 0;
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
-       i += (long long)gridDim.x * blockDim.x) {
-    x[i] = fma(alpha, p[i], x[i]);
-    const T ri = fma(-alpha, q[i], r[i]);
-    r[i] = ri;
+  for (long long i = cm.first; i < n; i += cm.stride) {
+    const long long k = off + i;
+    x[k] = fma(alpha, p[k], x[k]);
+    const T ri = fma(-alpha, q[k], r[k]);
+    r[k] = ri;
     part[0] = fma(ri, ri, part[0]);
     if (JAC) {
-      const T zi = ri * dinv[i];
-      z[i] = zi;
+      const T zi = ri * dinv[i];  // the diagonal is shared by the columns
+      z[k] = zi;
       part[NS - 1] = fma(ri, zi, part[NS - 1]);
     }
     if (++cnt == kChunk) flush_parts<T, NS>(acc, part, cnt);
@@ -226,37 +253,39 @@ __global__ void pcg_update_kernel(T* __restrict__ x, T* __restrict__ r, T* __res
 template <typename T>
 void launch_pcg_update(T* x, T* r, T* z, const T* p, const T* q, const T* dinv, long long n,
                        const RedArgs& red, int nblocks, const PcgScalars* s, cudaStream_t st) {
-  if (dinv) pcg_update_kernel<T, true><<<nblocks, 256, 0, st>>>(x, r, z, p, q, dinv, n, red, s);
-  else pcg_update_kernel<T, false><<<nblocks, 256, 0, st>>>(x, r, z, p, q, dinv, n, red, s);
+  const int g = col_blocks(nblocks, red.ncol);
+  if (dinv) pcg_update_kernel<T, true><<<g, 256, 0, st>>>(x, r, z, p, q, dinv, n, red, s);
+  else pcg_update_kernel<T, false><<<g, 256, 0, st>>>(x, r, z, p, q, dinv, n, red, s);
 }
 
 template <typename T>
 __global__ void p_update_kernel(T* __restrict__ p, const T* __restrict__ z, long long n,
-                                const PcgScalars* s) {
-  if (*((volatile const int*)&s->halt)) return;
-  const T beta = (T)s->beta;
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
-       i += (long long)gridDim.x * blockDim.x)
-    p[i] = fma(beta, p[i], z[i]);
+                                const PcgScalars* s, int ncol) {
+  const ColMap cm = colmap(ncol);
+  if (*((volatile const int*)&s[cm.col].halt)) return;
+  const T beta = (T)s[cm.col].beta;
+  const long long off = (long long)cm.col * n;
+  for (long long i = cm.first; i < n; i += cm.stride) p[off + i] = fma(beta, p[off + i], z[off + i]);
 }
 template <typename T>
-void launch_p_update(T* p, const T* z, long long n, const PcgScalars* s, cudaStream_t st) {
-  p_update_kernel<T><<<vec_blocks(n), 256, 0, st>>>(p, z, n, s);
+void launch_p_update(T* p, const T* z, long long n, const PcgScalars* s, cudaStream_t st, int ncol) {
+  p_update_kernel<T><<<col_blocks(vec_blocks(n), ncol), 256, 0, st>>>(p, z, n, s, ncol);
 }
 
 template <typename T>
 __global__ void jacobi_precond_kernel(T* __restrict__ z, const T* __restrict__ r,
                                       const T* __restrict__ dinv, long long n, RedArgs red,
                                       const int* halt) {
-  if (halt && *((volatile const int*)halt)) return;
+  const ColMap cm = colmap(red.ncol);
+  if (halted(halt, cm.col)) return;
+  const long long off = (long long)cm.col * n;
   double acc[1] = {0.0};
   T part[1] = {T(0)};
   int cnt = 0;
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
-       i += (long long)gridDim.x * blockDim.x) {
-    const T zi = r[i] * dinv[i];
-    z[i] = zi;
-    part[0] = fma(r[i], zi, part[0]);
+  for (long long i = cm.first; i < n; i += cm.stride) {
+    const T zi = r[off + i] * dinv[i];
+    z[off + i] = zi;
+    part[0] = fma(r[off + i], zi, part[0]);
     if (++cnt == kChunk) flush_parts<T, 1>(acc, part, cnt);
   }
   flush_parts<T, 1>(acc, part, cnt);
@@ -265,31 +294,47 @@ __global__ void jacobi_precond_kernel(T* __restrict__ z, const T* __restrict__ r
 template <typename T>
 void launch_jacobi_precond(T* z, const T* r, const T* dinv, long long n, const RedArgs& red,
                            int nblocks, const int* halt, cudaStream_t st) {
-  jacobi_precond_kernel<T><<<nblocks, 256, 0, st>>>(z, r, dinv, n, red, halt);
+  jacobi_precond_kernel<T><<<col_blocks(nblocks, red.ncol), 256, 0, st>>>(z, r, dinv, n, red, halt);
 }
 
+// Column c of the batched vectors: dst = (T32)(src * scale[c]).
 __global__ void scale_to_f32_kernel(float* __restrict__ d, const double* __restrict__ s,
-                                    const double* scale, long long n) {
-  const double sc = *scale;
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
-       i += (long long)gridDim.x * blockDim.x)
-    d[i] = (float)(s[i] * sc);
+                                    const double* scale, long long n, int ncol) {
+  const ColMap cm = colmap(ncol);
+  const double sc = scale[cm.col];
+  const long long off = (long long)cm.col * n;
+  for (long long i = cm.first; i < n; i += cm.stride) d[off + i] = (float)(s[off + i] * sc);
 }
 void launch_scale_to_f32(float* dst, const double* src, const double* scale, long long n,
-                         cudaStream_t st) {
-  scale_to_f32_kernel<<<vec_blocks(n), 256, 0, st>>>(dst, src, scale, n);
+                         cudaStream_t st, int ncol) {
+  scale_to_f32_kernel<<<col_blocks(vec_blocks(n), ncol), 256, 0, st>>>(dst, src, scale, n, ncol);
 }
 
+// u += d / scale[c] per column
 __global__ void add_scaled_f32_kernel(double* __restrict__ u, const float* __restrict__ d,
-                                      const double* scale, long long n) {
-  const double inv = 1.0 / *scale;
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
-       i += (long long)gridDim.x * blockDim.x)
-    u[i] = fma((double)d[i], inv, u[i]);
+                                      const double* scale, long long n, int ncol) {
+  const ColMap cm = colmap(ncol);
+  const double inv = 1.0 / scale[cm.col];
+  const long long off = (long long)cm.col * n;
+  for (long long i = cm.first; i < n; i += cm.stride) u[off + i] = fma((double)d[off + i], inv, u[off + i]);
 }
 void launch_add_scaled_f32(double* u, const float* d, const double* scale, long long n,
-                           cudaStream_t st) {
-  add_scaled_f32_kernel<<<vec_blocks(n), 256, 0, st>>>(u, d, scale, n);
+                           cudaStream_t st, int ncol) {
+  add_scaled_f32_kernel<<<col_blocks(vec_blocks(n), ncol), 256, 0, st>>>(u, d, scale, n, ncol);
+}
+
+// x = a[c] * x + y per column (a on the device)
+template <typename T>
+__global__ void scale_add_cols_kernel(T* __restrict__ x, const double* a, const T* __restrict__ y, long long n,
+                                      int ncol) {
+  const ColMap cm = colmap(ncol);
+  const T ac = (T)a[cm.col];
+  const long long off = (long long)cm.col * n;
+  for (long long i = cm.first; i < n; i += cm.stride) x[off + i] = fma(ac, x[off + i], y[off + i]);
+}
+template <typename T>
+void launch_scale_add_cols(T* x, const double* a, const T* y, long long n, int ncol, cudaStream_t st) {
+  scale_add_cols_kernel<T><<<col_blocks(vec_blocks(n), ncol), 256, 0, st>>>(x, a, y, n, ncol);
 }
 
 template <typename T>
@@ -317,14 +362,17 @@ void launch_convert(TD* dst, const TS* src, long long n, cudaStream_t st) {
 // Reset the scalars of a nested (coarse-level) PCG: no convergence test,
 // a fixed iteration count, and the parent's halt flag so a halted outer
 // iteration skips the nested one too.
-__global__ void scalars_init_kernel(PcgScalars* s, const PcgScalars* parent, int max_iter) {
+__global__ void scalars_init_kernel(PcgScalars* s0, const PcgScalars* parent, int max_iter, int ncol) {
+  const int c = threadIdx.x;
+  if (c >= ncol) return;
+  PcgScalars* s = s0 + c;
   s->rz = 0.0; s->rz_prev = 0.0; s->pAp = 0.0; s->alpha = 0.0; s->beta = 0.0; s->rr = 0.0;
   s->bnorm = 1.0; s->relres = 0.0; s->best_rel = INFINITY; s->tol = 0.0;
-  s->halt = parent ? *((volatile const int*)&parent->halt) : 0;
+  s->halt = parent ? *((volatile const int*)&parent[c].halt) : 0;
   s->status = 0; s->iter = 0; s->max_iter = max_iter; s->cadence = 0; s->test_now = 0;
 }
-void launch_scalars_init(PcgScalars* s, const PcgScalars* parent, int max_iter, cudaStream_t st) {
-  scalars_init_kernel<<<1, 1, 0, st>>>(s, parent, max_iter);
+void launch_scalars_init(PcgScalars* s, const PcgScalars* parent, int max_iter, cudaStream_t st, int ncol) {
+  scalars_init_kernel<<<1, 64, 0, st>>>(s, parent, max_iter, ncol);
 }
 
 #define INST(T)                                                                                 \
@@ -336,7 +384,8 @@ void launch_scalars_init(PcgScalars* s, const PcgScalars* parent, int max_iter, 
                               int, const int*, cudaStream_t);                                   \
   template void launch_pcg_update<T>(T*, T*, T*, const T*, const T*, const T*, long long,        \
                                      const RedArgs&, int, const PcgScalars*, cudaStream_t);      \
-  template void launch_p_update<T>(T*, const T*, long long, const PcgScalars*, cudaStream_t);    \
+  template void launch_p_update<T>(T*, const T*, long long, const PcgScalars*, cudaStream_t, int); \
+  template void launch_scale_add_cols<T>(T*, const double*, const T*, long long, int, cudaStream_t); \
   template void launch_jacobi_precond<T>(T*, const T*, const T*, long long, const RedArgs&, int, \
                                          const int*, cudaStream_t);                             \
   template void launch_axpby<T>(T*, T, const T*, T, long long, cudaStream_t);

@@ -90,6 +90,30 @@ def solve(grid: _lib.Grid, factor, f, *, clamp_faces: int = 0, fixed_dof=None, p
     return u_out, st.as_dict()
 
 
+def solve_multi_rhs(grid: _lib.Grid, factor, F, *, clamp_faces: int = 0, fixed_dof=None,
+                    params: _lib.SolveParams | None = None, U_out=None, ctx: _lib.Context | None = None):
+    """Solve the k load cases F (k x 3*nNodes, row j = load case j) as one block PCG.
+
+    precision "fp64": block PCG in FP64; "mixed"/"fp32": FP32 block PCG with
+    FP64 reliable updates to params.tol per column.  Returns (U, stats dict);
+    stats["compliance"] is the sum over the load cases of f_j . u_j and
+    stats["true_relres"] the largest per-column FP64 relative residual."""
+    ctx = ctx or context()
+    params = params or _lib.default_params()
+    ndof = 3 * (grid.nx + 1) * (grid.ny + 1) * (grid.nz + 1)
+    k = int(F.shape[0])
+    if tuple(F.shape) != (k, ndof):
+        raise ValueError(f"F must have shape (k, {ndof})")
+    if U_out is None:
+        U_out = np.empty((k, ndof), dtype=np.float64)
+    bc = _lib.make_bc(clamp_faces, fixed_dof)
+    st = _lib.SolveStats()
+    rc = ctx.lib.hexa_solve_multi_rhs(ctx.h, C.byref(grid), C.byref(bc), _lib.ptr(factor), k, _lib.ptr(F),
+                                      C.byref(params), _lib.ptr(U_out), C.byref(st))
+    ctx.check(rc)
+    return U_out, st.as_dict()
+
+
 def solve_system_gpu(nodes, elements, E, nu, bc, f, density, *, max_iter=40000, tol=1e-6, method="native",
                      solver="cg", use_precond=True, shift_factor=1.0e-4, min_stiffness_threshold=1.0e-3,
                      u_guess=None, config=None):
