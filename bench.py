@@ -45,7 +45,9 @@ def parse():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--config", default="c3", choices=["c1", "c2", "c3"])
+    ap.add_argument("--config", default="c3", choices=["c1", "c2", "c3", "c4", "c5"],
+                    help="c1-c3: one cantilever solve; c4: 8 load cases on the c2 grid as one block PCG; "
+                         "c5: 64 uneven cantilevers (filter + solve) as one batch")
     ap.add_argument("--no-plain", action="store_true", help="skip the plain FP64 comparison solve")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--cpu-seconds", type=float, default=20.0)
@@ -449,9 +451,132 @@ def run_reference(a):
     print(json.dumps(out))
 
 
+# ------------------------------------------------------------- batching
+def _timed(fn, warmup, steps):
+    import torch
+    for _ in range(warmup):
+        fn()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    out = None
+    for _ in range(steps):
+        out = fn()
+    torch.cuda.synchronize()
+    return (time.perf_counter() - t0) / steps, out
+
+
+def run_c4(a):
+    """k = 8 load cases on the c2 cantilever: one block PCG (FP32 inner, FP64
+    reliable updates to 1e-9 per column) against 8 separate mixed solves."""
+    import ctypes as C
+    import torch
+    from v119_2025_12_19_hexatop_aws_gb300 import _lib, workloads as W
+    from v119_2025_12_19_hexatop_aws_gb300 import build as libbuild
+    libbuild.build()
+    ctx = _lib.Context(0)
+    grid, rho, fac, _ = make_inputs("c2", ctx)
+    nx, ny, nz = grid.nx, grid.ny, grid.nz
+    F = W.point_loads(nx, ny, nz, 8)
+    k, ndof = F.shape
+    fac_d = torch.from_numpy(fac).cuda()
+    F_d = torch.from_numpy(F).cuda()
+    U_d = torch.empty_like(F_d)
+    u_d = torch.empty(ndof, dtype=torch.float64, device="cuda")
+    bc = _lib.make_bc(1)
+    pm = solver_params("c4", "mixed")
+    st = _lib.SolveStats()
+
+    def block():
+        ctx.check(ctx.lib.hexa_solve_multi_rhs(ctx.h, C.byref(grid), C.byref(bc), fac_d.data_ptr(), k, F_d.data_ptr(),
+                                               C.byref(pm), U_d.data_ptr(), C.byref(st)), allow=(_lib.HEXA_OK,))
+        return st.as_dict()
+
+    def columns():
+        out = []
+        for j in range(k):
+            ctx.check(ctx.lib.hexa_solve(ctx.h, C.byref(grid), C.byref(bc), fac_d.data_ptr(), F_d[j].data_ptr(),
+                                         C.byref(pm), None, u_d.data_ptr(), C.byref(st)), allow=(_lib.HEXA_OK,))
+            out.append(st.as_dict())
+        return out
+
+    tb, sb = _timed(block, a.warmup, a.steps)
+    tc, sc = _timed(columns, 1, 1)
+    print(json.dumps({"metric": "s per 8-load-case solve to FP64 rel.res 1e-9 per column", "value": round(tb, 4),
+                      "unit": "s", "config": {"workload": f"c4 cantilever {nx}x{ny}x{nz}, {ndof} DOF, 8 point loads, "
+                                                          "block PCG, FP32 inner / FP64 reliable updates"},
+                      "steps": a.steps, "warmup": a.warmup, "block": sb,
+                      "separate_mixed_solves_s": round(tc, 4), "separate_iterations": [q["iterations"] for q in sc],
+                      "compliance_sum_block": sb["compliance"],
+                      "compliance_sum_separate": sum(q["compliance"] for q in sc),
+                      "block_over_separate": round(tb / tc, 4)}))
+    ctx.close()
+
+
+def run_c5(a):
+    """64 uneven cantilevers: every instance's Helmholtz filter (r = 1.5) and
+    mixed GMG-PCG solve as two batches, against the same work one instance at
+    a time through the single-grid entry points."""
+    import torch
+    from v119_2025_12_19_hexatop_aws_gb300 import _lib, workloads as W
+    from v119_2025_12_19_hexatop_aws_gb300 import build as libbuild
+    from v119_2025_12_19_hexatop_aws_gb300.helmholtz import filter_batch, filter_density
+    from v119_2025_12_19_hexatop_aws_gb300.solver import solve, solve_batch
+    libbuild.build()
+    ctx = _lib.Context(0)
+    dims = W.batch_sizes(64)
+    grids = [_lib.make_grid(*d) for d in dims]
+    rhos, forces = [], []
+    for i, (d, g) in enumerate(zip(dims, grids)):
+        def filt(x, R, g=g):
+            out, _ = filter_density(g, np.ascontiguousarray(x), R, tol=1e-10, max_iter=20000, quirk=False, ctx=ctx)
+            return out
+        rhos.append(W.smooth_density(*d, filt, seed=W.SEED + 1000 + i, r_elems=2.0))
+        forces.append(W.point_loads(*d, 1, seed=W.SEED + 2000 + i)[0])
+    rho_d = [torch.from_numpy(r).cuda() for r in rhos]
+    f_d = [torch.from_numpy(f).cuda() for f in forces]
+    filt_d = [torch.empty_like(r) for r in rho_d]
+    u_d = [torch.empty_like(f) for f in f_d]
+    R = W.helmholtz_R(1.5)
+    pm = solver_params("c5", "mixed")
+
+    def batch():
+        filter_batch(grids, rho_d, R, tol=1e-9, max_iter=2000, quirk=False, out=filt_d, ctx=ctx)
+        facs = [W.EMIN + r ** W.PENAL * (W.E0 - W.EMIN) for r in filt_d]
+        _, st, rc = solve_batch(grids, facs, f_d, clamp_faces=1, params=pm, u_out=u_d, ctx=ctx)
+        return st
+
+    def one_by_one():
+        st = []
+        for i, g in enumerate(grids):
+            fr, _ = filter_density(g, rho_d[i], R, tol=1e-9, max_iter=2000, quirk=False, out=filt_d[i], ctx=ctx)
+            fac = W.EMIN + filt_d[i] ** W.PENAL * (W.E0 - W.EMIN)
+            _, s = solve(g, fac, f_d[i], clamp_faces=1, params=pm, u_out=u_d[i], ctx=ctx)
+            st.append(s)
+        return st
+
+    tb, sb = _timed(batch, a.warmup, a.steps)
+    comp_b = [s["compliance"] for s in sb]
+    ts, ss = _timed(one_by_one, 1, 1)
+    comp_s = [s["compliance"] for s in ss]
+    nelem = sum(d[0] * d[1] * d[2] for d in dims)
+    print(json.dumps({"metric": "s per batch of 64 uneven cantilevers (filter + solve to FP64 rel.res 1e-9)",
+                      "value": round(tb, 4), "unit": "s", "steps": a.steps, "warmup": a.warmup,
+                      "config": {"workload": f"c5: 64 cantilevers nx in 16..96 step 8, ny=nz=nx/2, "
+                                             f"{nelem} elements in total, filter r=1.5, mixed GMG-PCG"},
+                      "max_true_relres": max(s["true_relres"] for s in sb),
+                      "iterations_max": max(s["iterations"] for s in sb),
+                      "one_by_one_s": round(ts, 4), "batch_over_one_by_one": round(tb / ts, 4),
+                      "max_rel_compliance_diff": max(abs(x - y) / abs(y) for x, y in zip(comp_b, comp_s))}))
+    ctx.close()
+
+
 if __name__ == "__main__":
     args = parse()
     if args.impl == "reference":
         run_reference(args)
+    elif args.config == "c4":
+        run_c4(args)
+    elif args.config == "c5":
+        run_c5(args)
     else:
         run_ours(args)

@@ -192,6 +192,21 @@ int hexa_solve_multi_rhs(hexa_ctx* ctx, const hexa_grid* g, const hexa_bc* bc, c
                          int32_t k, const double* F, const hexa_solve_params* p, double* U,
                          hexa_solve_stats* stats);
 
+/* `count` independent problems on grids of uneven sizes solved together (no
+ * counterpart in the reference): one launch per kernel over all instances,
+ * per-instance reductions and convergence, the PCG iteration and V-cycle
+ * replayed from one CUDA graph.  grids[i], bcs[i] (clamp faces only:
+ * fixed_dof must be NULL; bcs may be NULL for no clamps), factors[i] (nElem_i),
+ * forces[i] (3*nNodes_i) and u_out[i] are per instance, host or device
+ * pointers; all instances share the element size and nu.  Mixed precision
+ * with the multigrid preconditioner only (FP32 GMG-PCG, FP64 reliable
+ * updates to p->tol per instance); p->autotune picks the operator's z-brick
+ * depth by timing.  stats (nullable) receives count entries; the return is
+ * HEXA_OK when every instance converged, HEXA_NOT_CONVERGED otherwise. */
+int hexa_solve_batch(hexa_ctx* ctx, int32_t count, const hexa_grid* grids, const hexa_bc* bcs, double nu,
+                     const double* const* factors, const double* const* forces, const hexa_solve_params* p,
+                     double* const* u_out, hexa_solve_stats* stats);
+
 /* ---- (d) Helmholtz density filter -------------------------------------- */
 /* Replaces GPUHelmholtz.apply_gpu_filter! (GPUHelmholtz.jl:422-443):
  * solves (R^2 K_s + M_s) psi = sum_e rho_e vol/8 with Jacobi-PCG (at most
@@ -218,6 +233,14 @@ int hexa_filter(hexa_ctx* ctx, const hexa_grid* g, const double* rho_in, double 
 #define HEXA_NOALLOC_MAX_NODES 262144
 int hexa_filter_noalloc(const hexa_grid* g, const double* rho_in, double radius, double tol, int32_t max_iter,
                         int32_t quirk, double* rho_out, void* stream, hexa_filter_stats* stats);
+
+/* The filter of hexa_filter over `count` grids of uneven sizes in one batch
+ * (no counterpart in the reference): every Jacobi-PCG kernel is one launch
+ * over all instances, each with its own dots, every-10 test and cap.  All
+ * grids share the element size; rho_in[i]/rho_out[i] host or device. */
+int hexa_filter_batch(hexa_ctx* ctx, int32_t count, const hexa_grid* grids, const double* const* rho_in,
+                      double radius, double tol, int32_t max_iter, int32_t quirk, int32_t precision,
+                      double* const* rho_out, hexa_filter_stats* stats);
 
 /* ---- (e) SIMP sensitivities and OC update ------------------------------ */
 /* dc_e = -penal * rho_e^(penal-1) * (E0 - Emin) * u_e^T K0 u_e and

@@ -95,7 +95,11 @@ SIGNATURES = {
                                     C.POINTER(D), C.c_char_p, I32, C.POINTER(SolveStats)]),
     "hexa_solve_multi_rhs": (I32, [P, C.POINTER(Grid), C.POINTER(BC), P, I32, P, C.POINTER(SolveParams), P,
                                    C.POINTER(SolveStats)]),
+    "hexa_solve_batch": (I32, [P, I32, C.POINTER(Grid), C.POINTER(BC), D, C.POINTER(P), C.POINTER(P),
+                               C.POINTER(SolveParams), C.POINTER(P), C.POINTER(SolveStats)]),
     "hexa_filter": (I32, [P, C.POINTER(Grid), P, D, D, I32, I32, I32, P, C.POINTER(FilterStats)]),
+    "hexa_filter_batch": (I32, [P, I32, C.POINTER(Grid), C.POINTER(P), D, D, I32, I32, I32, C.POINTER(P),
+                                C.POINTER(FilterStats)]),
     "hexa_filter_noalloc": (I32, [C.POINTER(Grid), P, D, D, I32, I32, P, P, C.POINTER(FilterStats)]),
     "hexa_sensitivities": (I32, [P, C.POINTER(Grid), D, P, P, D, D, D, P, C.POINTER(D)]),
     "hexa_simp_factors": (I32, [P, I64, P, D, D, D, P]),

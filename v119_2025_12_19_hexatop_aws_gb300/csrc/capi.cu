@@ -646,6 +646,45 @@ int hexa_filter(hexa_ctx* h, const hexa_grid* g, const double* rho_in, double ra
   return rc;
 }
 
+int hexa_solve_batch(hexa_ctx* h, int32_t count, const hexa_grid* grids, const hexa_bc* bcs, double nu,
+                     const double* const* factors, const double* const* forces, const hexa_solve_params* p,
+                     double* const* u_out, hexa_solve_stats* stats) {
+  if (!h) return HEXA_ERR_ARG;
+  if (count < 1 || !grids || !factors || !forces || !u_out) return set_err(h, HEXA_ERR_ARG, "invalid batch arguments");
+  if (!valid_params(p) || !(nu > -1.0 && nu < 0.5)) return set_err(h, HEXA_ERR_ARG, "invalid solver parameters");
+  for (int i = 0; i < count; ++i)
+    if (!valid_grid(grids + i) || !factors[i] || !forces[i] || !u_out[i])
+      return set_err(h, HEXA_ERR_ARG, "invalid grid or null array in instance " + std::to_string(i));
+  Ctx& c = h->c;
+  c.err.clear();
+  cudaSetDevice(c.device);
+  const int rc = batch_problem(c, count, grids, bcs, nu, factors, forces, *p, u_out, stats);
+  if (rc < 0 && c.err.empty()) c.err = "batch solve failed";
+  return rc;
+}
+
+int hexa_filter_batch(hexa_ctx* h, int32_t count, const hexa_grid* grids, const double* const* rho_in, double radius,
+                      double tol, int32_t max_iter, int32_t quirk, int32_t precision, double* const* rho_out,
+                      hexa_filter_stats* stats) {
+  if (!h) return HEXA_ERR_ARG;
+  if (count < 1 || !grids || !rho_in || !rho_out || !(radius >= 0) || !(tol > 0) || max_iter < 1)
+    return set_err(h, HEXA_ERR_ARG, "invalid batch filter arguments");
+  for (int i = 0; i < count; ++i)
+    if (!valid_grid(grids + i) || !rho_in[i] || !rho_out[i])
+      return set_err(h, HEXA_ERR_ARG, "invalid grid or null array in instance " + std::to_string(i));
+  Ctx& c = h->c;
+  c.err.clear();
+  cudaSetDevice(c.device);
+  const auto t0 = std::chrono::steady_clock::now();
+  const int rc = batch_filter(c, count, grids, rho_in, radius, tol, max_iter, quirk, precision, rho_out, stats);
+  if (stats && rc == HEXA_OK) {
+    const double ms = wall_ms(t0);
+    for (int i = 0; i < count; ++i) stats[i].solve_ms = ms;
+  }
+  if (rc < 0 && c.err.empty()) c.err = "batch filter failed";
+  return rc;
+}
+
 int hexa_simp_factors(hexa_ctx* h, int64_t n, const double* rho, double Emin, double E0, double penal,
                       double* factor_out) {
   if (!h) return HEXA_ERR_ARG;

@@ -50,12 +50,11 @@ struct HelmKT {
 };
 
 template <typename T>
-__global__ void helm_apply_kernel(Grid g, HelmKT<T> K, const T* __restrict__ x, T* __restrict__ y, RedArgs red,
-                                  const int* halt) {
-  if (halt && *((volatile const int*)halt)) return;
-  double acc[1] = {0.0};
+__device__ __forceinline__ double helm_apply_body(const Grid& g, const HelmKT<T>& K, const T* __restrict__ x,
+                                                  T* __restrict__ y, long long first, long long stride) {
+  double acc = 0.0;
   const long long nn = g.nnode();
-  for (long long n = blockIdx.x * (long long)blockDim.x + threadIdx.x; n < nn; n += (long long)gridDim.x * blockDim.x) {
+  for (long long n = first; n < nn; n += stride) {
     const int i = (int)(n % g.NX);
     const long long t = n / g.NX;
     const int j = (int)(t % g.NY), k = (int)(t / g.NY);
@@ -78,9 +77,43 @@ __global__ void helm_apply_kernel(Grid g, HelmKT<T> K, const T* __restrict__ x, 
           }
         }
     y[n] = s;
-    acc[0] += (double)x[n] * (double)s;
+    acc += (double)x[n] * (double)s;
   }
+  return acc;
+}
+template <typename T>
+__global__ void helm_apply_kernel(Grid g, HelmKT<T> K, const T* __restrict__ x, T* __restrict__ y, RedArgs red,
+                                  const int* halt) {
+  if (halt && *((volatile const int*)halt)) return;
+  double acc[1] = {helm_apply_body<T>(g, K, x, y, blockIdx.x * (long long)blockDim.x + threadIdx.x,
+                                      (long long)gridDim.x * blockDim.x)};
   block_reduce_finalize<1>(red, acc);
+}
+
+// Batch form over node vectors: instance I's nodes start at I.noff.
+template <typename T>
+__global__ void batch_helm_apply_kernel(const BatchInst* in, int ninst, HelmKT<T> K, const T* __restrict__ x,
+                                        T* __restrict__ y, RedArgs red, const PcgScalars* s) {
+  int lo = 0, hi = ninst - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (in[mid].vblk0 <= (int)blockIdx.x) lo = mid;
+    else hi = mid - 1;
+  }
+  const BatchInst& I = in[lo];
+  if (s && *((volatile const int*)&s[I.id].halt)) return;
+  double acc[1] = {helm_apply_body<T>(I.g, K, x + I.noff, y + I.noff,
+                                      (long long)(blockIdx.x - I.vblk0) * blockDim.x + threadIdx.x,
+                                      (long long)I.vnblk * blockDim.x)};
+  block_reduce_finalize_at<1>(red, acc, I.id, blockIdx.x, I.vnblk, I.vblk0, 1);
+}
+template <typename T>
+void launch_batch_helm_apply_dot(const BatchInst* in, int ninst, int nblocks, const HelmK& K, const T* x, T* y,
+                                 const RedArgs& red, const PcgScalars* s, cudaStream_t st) {
+  HelmKT<T> k;
+  for (int a = 0; a < 8; ++a)
+    for (int b = 0; b < 8; ++b) k.A[a][b] = (T)K.A[a][b];
+  batch_helm_apply_kernel<T><<<nblocks, 256, 0, st>>>(in, ninst, k, x, y, red, s);
 }
 template <typename T>
 void launch_helm_apply_dot(const Grid& g, const HelmK& K, const T* x, T* y, const RedArgs& red, int nblocks,
@@ -144,7 +177,9 @@ void launch_helm_extract(const Grid& g, const T* psi, T* rho_out, cudaStream_t s
   template void launch_helm_apply_dot<T>(const Grid&, const HelmK&, const T*, T*, const RedArgs&, int,       \
                                          const int*, cudaStream_t);                                          \
   template void launch_helm_dinv<T>(const Grid&, const HelmK&, T*, cudaStream_t);                            \
-  template void launch_helm_extract<T>(const Grid&, const T*, T*, cudaStream_t);
+  template void launch_helm_extract<T>(const Grid&, const T*, T*, cudaStream_t);                            \
+  template void launch_batch_helm_apply_dot<T>(const BatchInst*, int, int, const HelmK&, const T*, T*,       \
+                                               const RedArgs&, const PcgScalars*, cudaStream_t);
 INST(double)
 INST(float)
 #undef INST

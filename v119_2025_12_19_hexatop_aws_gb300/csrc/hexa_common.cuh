@@ -214,20 +214,18 @@ __device__ __forceinline__ void finalize_scalars(const RedArgs& r, const double*
 }
 
 // Block reduction of nsum values per thread, then the last block (by ticket)
-// sums the per-block partials in block order and runs the finalize op.  The
-// order of every addition is fixed, so results are bitwise reproducible.
+// of the same reduction group sums the per-block partials in block order and
+// runs the finalize op.  The order of every addition is fixed, so results are
+// bitwise reproducible.  A group is column `col` of the scalars/tickets; its
+// nb blocks have partial slots base, base + step, ..., this block's slot is bid.
 template <int NSUM>
-__device__ __forceinline__ void block_reduce_finalize(const RedArgs& r, double (&v)[NSUM]) {
+__device__ __forceinline__ void block_reduce_finalize_at(const RedArgs& r, double (&v)[NSUM], int col, long long bid,
+                                                         long long nb, long long base, long long step) {
   __shared__ double sred[NSUM][32];
   __shared__ bool am_last;
   const int tid = threadIdx.x + blockDim.x * (threadIdx.y + blockDim.y * threadIdx.z);
   const int nthr = blockDim.x * blockDim.y * blockDim.z;
   const int lane = tid & 31, wid = tid >> 5, nw = (nthr + 31) >> 5;
-  const long long bid = blockIdx.x + (long long)gridDim.x * (blockIdx.y + (long long)gridDim.y * blockIdx.z);
-  const long long nball = (long long)gridDim.x * gridDim.y * gridDim.z;
-  const int ncol = r.ncol > 1 ? r.ncol : 1;
-  const int col = (int)(bid % ncol);
-  const long long nb = nball / ncol;  // blocks of this column
 #pragma unroll
   for (int q = 0; q < NSUM; ++q) {
     double t = warp_sum(v[q]);
@@ -256,7 +254,7 @@ __device__ __forceinline__ void block_reduce_finalize(const RedArgs& r, double (
   for (int q = 0; q < NSUM; ++q) acc[q] = 0.0;
   for (long long b = tid; b < nb; b += nthr) {
 #pragma unroll
-    for (int q = 0; q < NSUM; ++q) acc[q] += ((volatile double*)r.partials)[(b * ncol + col) * NSUM + q];
+    for (int q = 0; q < NSUM; ++q) acc[q] += ((volatile double*)r.partials)[(base + b * step) * NSUM + q];
   }
   __syncthreads();
 #pragma unroll
@@ -276,6 +274,16 @@ __device__ __forceinline__ void block_reduce_finalize(const RedArgs& r, double (
     finalize_scalars(r, tot, col);
     r.ticket[col] = 0u;
   }
+}
+
+// The whole grid is one group per column (block b works on column b % ncol).
+template <int NSUM>
+__device__ __forceinline__ void block_reduce_finalize(const RedArgs& r, double (&v)[NSUM]) {
+  const long long bid = blockIdx.x + (long long)gridDim.x * (blockIdx.y + (long long)gridDim.y * blockIdx.z);
+  const long long nball = (long long)gridDim.x * gridDim.y * gridDim.z;
+  const int ncol = r.ncol > 1 ? r.ncol : 1;
+  const int col = (int)(bid % ncol);
+  block_reduce_finalize_at<NSUM>(r, v, col, bid, nball / ncol, col, ncol);
 }
 
 }  // namespace hexa

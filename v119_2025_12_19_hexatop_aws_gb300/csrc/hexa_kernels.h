@@ -35,8 +35,8 @@ struct OpArgs {
   int diag_quirk;
   RedArgs red;
   const int* halt;  // nullable: PcgScalars::halt
-  int ncol = 1;     // columns (x, b, y, xin advance by ndof per column); the dot
-                    // modes sum over all columns
+  int ncol = 1;     // columns (x, b, y advance by ndof per column): OP_APPLY and
+                    // OP_RESID only
 };
 
 template <typename T>
@@ -179,5 +179,96 @@ void launch_cols_from64(T* dst, const double* src, const double* scale, long lon
 // u_j += d_j / scale[j] (columns with scale 0 are left alone)
 template <typename T>
 void launch_cols_accum(double* u, const T* d, const double* scale, long long n, int k, cudaStream_t st);
+
+
+// ---- batches of independent grids (one launch over all instances) -------
+// One instance of a batched launch.  Vectors of a batch level are the
+// instances' vectors back to back: DOF vectors from `off`, node vectors from
+// `noff`, element arrays from `eoff`.  A launch gives instance i the blocks
+// [blk0, blk0 + nblk) of its grid; reductions and halts are per instance (id).
+struct BatchInst {
+  Grid g;
+  Mask m;
+  long long off, noff, eoff;
+  // the other level of a transfer (restriction: the finer grid; prolongation:
+  // the coarser grid) and its DOF offset
+  Grid g2;
+  Mask m2;
+  long long off2;
+  double sigma;
+  int id;
+  int kchunk, tiles_x, tiles_y, nchunks;  // operator tiling
+  int oblk0, onblk;                       // operator blocks
+  int vblk0, vnblk;                       // vector / transfer pass blocks
+  int pad;
+};
+
+// Fills the operator tiling (z-bricks of kchunk node layers, 0 = 16) and the
+// block ranges of n instances (targeting the resident CTAs of the operator in
+// precision T); returns the grid size.
+template <typename T>
+int op_batch_plan(BatchInst* in, int n, int kchunk);
+// s[i].beta = s[i].rz * coef[i] for i < n (direction kept across a reliable update)
+void launch_batch_set_beta(PcgScalars* s, const double* coef, int n, cudaStream_t st);
+// Fills the vector-pass block ranges in proportion to units(i) (DOFs, nodes
+// or elements by `unit`: 0 DOF, 1 node, 2 element, 3 node of g2); returns the grid.
+int vec_batch_plan(BatchInst* in, int n, int unit, int max_blocks);
+
+template <typename T>
+struct BatchOpArgs {
+  ModalK<T> K;
+  T c1, c2, omega;
+  int diag_quirk;
+  const BatchInst* inst;  // device table
+  int ninst, nblocks;
+  const T* x;
+  const T* fac;
+  const T* b;
+  T* y;
+  const T* xin;
+  RedArgs red;            // group = instance id
+  const PcgScalars* s;    // per-instance halts (nullable)
+};
+template <typename T>
+void launch_op_batch(int mode, const BatchOpArgs<T>& a, bool idx32, cudaStream_t st);
+
+// vector passes over a batch (n per instance = its DOFs, or nodes if node_sized)
+template <typename T>
+void launch_batch_pcg_update(const BatchInst* in, int ninst, int nblocks, int node_sized, T* x, T* r, T* z,
+                             const T* p, const T* q, const T* dinv, const RedArgs& red, const PcgScalars* s,
+                             cudaStream_t st);
+template <typename T>
+void launch_batch_p_update(const BatchInst* in, int ninst, int nblocks, int node_sized, T* p, const T* z,
+                           const PcgScalars* s, cudaStream_t st);
+// sums a.b (and c.d when c is given) per instance
+template <typename T>
+void launch_batch_dot(const BatchInst* in, int ninst, int nblocks, int node_sized, const T* a, const T* b,
+                      const T* c, const T* d, const RedArgs& red, const PcgScalars* s, cudaStream_t st);
+// dst = (T)(src * scale[id]) ; u += d / scale[id] (scale 0: left alone)
+template <typename T>
+void launch_batch_from64(const BatchInst* in, int ninst, int nblocks, T* dst, const double* src,
+                         const double* scale, cudaStream_t st);
+template <typename T>
+void launch_batch_accum(const BatchInst* in, int ninst, int nblocks, double* u, const T* d, const double* scale,
+                        cudaStream_t st);
+// multigrid over a batch level
+template <typename T>
+void launch_batch_restrict(const BatchInst* in, int ninst, int nblocks, const T* rf, T* bc, const PcgScalars* s,
+                           cudaStream_t st);
+template <typename T>
+void launch_batch_prolong_add(const BatchInst* in, int ninst, int nblocks, const T* xc, T* xf,
+                              const PcgScalars* s, cudaStream_t st);
+template <typename T>
+void launch_batch_jacobi0(const BatchInst* in, int ninst, int nblocks, const T* fac, const ModalK<T>& K, int quirk,
+                          T omega, const T* b, T* x, const PcgScalars* s, cudaStream_t st);
+// one CTA per instance: iters Jacobi-PCG iterations on its coarsest grid
+template <typename T>
+void launch_batch_coarse_pcg(const BatchInst* in, int ninst, const T* fac, const ModalK<T>& K, const T* dinv,
+                             const T* b, T* x, T* r, T* z, T* p, T* q, T* w, int iters, const PcgScalars* s,
+                             cudaStream_t st);
+// Helmholtz matvec + p.Ap per instance over node vectors
+template <typename T>
+void launch_batch_helm_apply_dot(const BatchInst* in, int ninst, int nblocks, const HelmK& K, const T* x, T* y,
+                                 const RedArgs& red, const PcgScalars* s, cudaStream_t st);
 
 }  // namespace hexa

@@ -60,12 +60,10 @@ void launch_coarsen_mask(const Grid& gf, const uint8_t* mf, const Grid& gc, uint
 }
 
 template <typename T>
-__global__ void restrict_kernel(Grid gf, const T* __restrict__ rf, Grid gc, Mask mc, T* __restrict__ bc,
-                                const int* halt) {
-  if (halt && *((volatile const int*)halt)) return;
+__device__ __forceinline__ void restrict_body(const Grid& gf, const T* __restrict__ rf, const Grid& gc, const Mask& mc,
+                                              T* __restrict__ bc, long long first, long long stride) {
   const long long nn = gc.nnode();
-  for (long long n = blockIdx.x * (long long)blockDim.x + threadIdx.x; n < nn;
-       n += (long long)gridDim.x * blockDim.x) {
+  for (long long n = first; n < nn; n += stride) {
     const int I = (int)(n % gc.NX);
     const long long t = n / gc.NX;
     const int J = (int)(t % gc.NY), K = (int)(t / gc.NY);
@@ -100,18 +98,23 @@ __global__ void restrict_kernel(Grid gf, const T* __restrict__ rf, Grid gc, Mask
   }
 }
 template <typename T>
+__global__ void restrict_kernel(Grid gf, const T* __restrict__ rf, Grid gc, Mask mc, T* __restrict__ bc,
+                                const int* halt) {
+  if (halt && *((volatile const int*)halt)) return;
+  restrict_body<T>(gf, rf, gc, mc, bc, blockIdx.x * (long long)blockDim.x + threadIdx.x,
+                   (long long)gridDim.x * blockDim.x);
+}
+template <typename T>
 void launch_restrict(const Grid& gf, const T* rf, const Grid& gc, const Mask& mc, T* bc, const int* halt,
                      cudaStream_t st) {
   restrict_kernel<T><<<mg_blocks(gc.nnode()), 256, 0, st>>>(gf, rf, gc, mc, bc, halt);
 }
 
 template <typename T>
-__global__ void prolong_add_kernel(Grid gc, const T* __restrict__ xc, Grid gf, Mask mf, T* __restrict__ xf,
-                                   const int* halt) {
-  if (halt && *((volatile const int*)halt)) return;
+__device__ __forceinline__ void prolong_add_body(const Grid& gc, const T* __restrict__ xc, const Grid& gf,
+                                                 const Mask& mf, T* __restrict__ xf, long long first, long long stride) {
   const long long nn = gf.nnode();
-  for (long long n = blockIdx.x * (long long)blockDim.x + threadIdx.x; n < nn;
-       n += (long long)gridDim.x * blockDim.x) {
+  for (long long n = first; n < nn; n += stride) {
     const int i = (int)(n % gf.NX);
     const long long t = n / gf.NX;
     const int j = (int)(t % gf.NY), k = (int)(t / gf.NY);
@@ -136,18 +139,25 @@ __global__ void prolong_add_kernel(Grid gc, const T* __restrict__ xc, Grid gf, M
   }
 }
 template <typename T>
+__global__ void prolong_add_kernel(Grid gc, const T* __restrict__ xc, Grid gf, Mask mf, T* __restrict__ xf,
+                                   const int* halt) {
+  if (halt && *((volatile const int*)halt)) return;
+  prolong_add_body<T>(gc, xc, gf, mf, xf, blockIdx.x * (long long)blockDim.x + threadIdx.x,
+                      (long long)gridDim.x * blockDim.x);
+}
+template <typename T>
 void launch_prolong_add(const Grid& gc, const T* xc, const Grid& gf, const Mask& mf, T* xf, const int* halt,
                         cudaStream_t st) {
   prolong_add_kernel<T><<<mg_blocks(gf.nnode()), 256, 0, st>>>(gc, xc, gf, mf, xf, halt);
 }
 
 template <typename T>
-__global__ void jacobi0_kernel(Grid g, Mask m, const T* __restrict__ fac, ModalK<T> K, int quirk, T sigma,
-                               T omega, const T* __restrict__ b, T* __restrict__ x, const int* halt) {
-  if (halt && *((volatile const int*)halt)) return;
+__device__ __forceinline__ void jacobi0_body(const Grid& g, const Mask& m, const T* __restrict__ fac,
+                                             const ModalK<T>& K, int quirk, T sigma, T omega,
+                                             const T* __restrict__ b, T* __restrict__ x, long long first,
+                                             long long stride) {
   const long long nn = g.nnode();
-  for (long long n = blockIdx.x * (long long)blockDim.x + threadIdx.x; n < nn;
-       n += (long long)gridDim.x * blockDim.x) {
+  for (long long n = first; n < nn; n += stride) {
     const int i = (int)(n % g.NX);
     const long long t = n / g.NX;
     const int j = (int)(t % g.NY), k = (int)(t / g.NY);
@@ -169,6 +179,13 @@ __global__ void jacobi0_kernel(Grid g, Mask m, const T* __restrict__ fac, ModalK
       x[3 * n + c] = ((fx >> c) & 1u) ? T(0) : omega * b[3 * n + c] / d;
     }
   }
+}
+template <typename T>
+__global__ void jacobi0_kernel(Grid g, Mask m, const T* __restrict__ fac, ModalK<T> K, int quirk, T sigma,
+                               T omega, const T* __restrict__ b, T* __restrict__ x, const int* halt) {
+  if (halt && *((volatile const int*)halt)) return;
+  jacobi0_body<T>(g, m, fac, K, quirk, sigma, omega, b, x, blockIdx.x * (long long)blockDim.x + threadIdx.x,
+                  (long long)gridDim.x * blockDim.x);
 }
 template <typename T>
 void launch_jacobi0(const Grid& g, const Mask& m, const T* fac, const ModalK<T>& K, int quirk, T sigma, T omega,
@@ -206,11 +223,10 @@ __device__ __forceinline__ bool modal_nz_mg(int q, int c, int c2) {
 }
 
 template <typename T>
-__global__ void __launch_bounds__(1024) coarse_pcg_kernel(Grid g, Mask m, const T* __restrict__ fac, ModalK<T> K,
-                                                          T sigma, const T* __restrict__ dinv, const T* __restrict__ b,
-                                                          T* x, T* r, T* z, T* p, T* q, T* w, int iters,
-                                                          const int* halt) {
-  if (halt && *((volatile const int*)halt)) return;
+__device__ __forceinline__ void coarse_pcg_body(const Grid& g, const Mask& m, const T* __restrict__ fac,
+                                                const ModalK<T>& K, T sigma, const T* __restrict__ dinv,
+                                                const T* __restrict__ b, T* x, T* r, T* z, T* p, T* q, T* w,
+                                                int iters) {
   __shared__ double red[32];
   const int tid = threadIdx.x, nthr = blockDim.x;
   const long long n3 = g.ndof(), ne = g.nelem(), nn = g.nnode();
@@ -335,9 +351,94 @@ __global__ void __launch_bounds__(1024) coarse_pcg_kernel(Grid g, Mask m, const 
   }
 }
 template <typename T>
+__global__ void __launch_bounds__(1024) coarse_pcg_kernel(Grid g, Mask m, const T* __restrict__ fac, ModalK<T> K,
+                                                          T sigma, const T* __restrict__ dinv, const T* __restrict__ b,
+                                                          T* x, T* r, T* z, T* p, T* q, T* w, int iters,
+                                                          const int* halt) {
+  if (halt && *((volatile const int*)halt)) return;
+  coarse_pcg_body<T>(g, m, fac, K, sigma, dinv, b, x, r, z, p, q, w, iters);
+}
+template <typename T>
 void launch_coarse_pcg(const Grid& g, const Mask& m, const T* fac, const ModalK<T>& K, T sigma, const T* dinv,
                        const T* b, T* x, T* r, T* z, T* p, T* q, T* w, int iters, const int* halt, cudaStream_t st) {
   coarse_pcg_kernel<T><<<1, 1024, 0, st>>>(g, m, fac, K, sigma, dinv, b, x, r, z, p, q, w, iters, halt);
+}
+
+// ------------------------------------------------------------ batch forms
+__device__ __forceinline__ const BatchInst& batch_inst_vec(const BatchInst* in, int n, int b) {
+  int lo = 0, hi = n - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (in[mid].vblk0 <= b) lo = mid;
+    else hi = mid - 1;
+  }
+  return in[lo];
+}
+__device__ __forceinline__ bool batch_halted(const PcgScalars* s, int id) {
+  return s && *((volatile const int*)&s[id].halt);
+}
+
+// in[i]: g/m/off = the coarse level, g2/off2 = the fine level; blocks by coarse nodes
+template <typename T>
+__global__ void batch_restrict_kernel(const BatchInst* in, int ninst, const T* __restrict__ rf, T* __restrict__ bc,
+                                      const PcgScalars* s) {
+  const BatchInst& I = batch_inst_vec(in, ninst, blockIdx.x);
+  if (batch_halted(s, I.id)) return;
+  restrict_body<T>(I.g2, rf + I.off2, I.g, I.m, bc + I.off,
+                   (long long)(blockIdx.x - I.vblk0) * blockDim.x + threadIdx.x, (long long)I.vnblk * blockDim.x);
+}
+template <typename T>
+void launch_batch_restrict(const BatchInst* in, int ninst, int nblocks, const T* rf, T* bc, const PcgScalars* s,
+                           cudaStream_t st) {
+  batch_restrict_kernel<T><<<nblocks, 256, 0, st>>>(in, ninst, rf, bc, s);
+}
+
+// in[i]: g/m/off = the fine level, g2/off2 = the coarse level; blocks by fine nodes
+template <typename T>
+__global__ void batch_prolong_add_kernel(const BatchInst* in, int ninst, const T* __restrict__ xc, T* __restrict__ xf,
+                                         const PcgScalars* s) {
+  const BatchInst& I = batch_inst_vec(in, ninst, blockIdx.x);
+  if (batch_halted(s, I.id)) return;
+  prolong_add_body<T>(I.g2, xc + I.off2, I.g, I.m, xf + I.off,
+                      (long long)(blockIdx.x - I.vblk0) * blockDim.x + threadIdx.x, (long long)I.vnblk * blockDim.x);
+}
+template <typename T>
+void launch_batch_prolong_add(const BatchInst* in, int ninst, int nblocks, const T* xc, T* xf,
+                              const PcgScalars* s, cudaStream_t st) {
+  batch_prolong_add_kernel<T><<<nblocks, 256, 0, st>>>(in, ninst, xc, xf, s);
+}
+
+template <typename T>
+__global__ void batch_jacobi0_kernel(const BatchInst* in, int ninst, const T* __restrict__ fac, ModalK<T> K, int quirk,
+                                     T omega, const T* __restrict__ b, T* __restrict__ x, const PcgScalars* s) {
+  const BatchInst& I = batch_inst_vec(in, ninst, blockIdx.x);
+  if (batch_halted(s, I.id)) return;
+  jacobi0_body<T>(I.g, I.m, fac + I.eoff, K, quirk, (T)I.sigma, omega, b + I.off, x + I.off,
+                  (long long)(blockIdx.x - I.vblk0) * blockDim.x + threadIdx.x, (long long)I.vnblk * blockDim.x);
+}
+template <typename T>
+void launch_batch_jacobi0(const BatchInst* in, int ninst, int nblocks, const T* fac, const ModalK<T>& K, int quirk,
+                          T omega, const T* b, T* x, const PcgScalars* s, cudaStream_t st) {
+  batch_jacobi0_kernel<T><<<nblocks, 256, 0, st>>>(in, ninst, fac, K, quirk, omega, b, x, s);
+}
+
+// CTA i solves instance in[i] (vectors at off, element scratch w at 24 * eoff)
+template <typename T>
+__global__ void __launch_bounds__(1024) batch_coarse_pcg_kernel(const BatchInst* in, const T* __restrict__ fac,
+                                                                ModalK<T> K, const T* __restrict__ dinv,
+                                                                const T* __restrict__ b, T* x, T* r, T* z, T* p, T* q,
+                                                                T* w, int iters, const PcgScalars* s) {
+  const BatchInst& I = in[blockIdx.x];
+  if (batch_halted(s, I.id)) return;
+  const long long o = I.off;
+  coarse_pcg_body<T>(I.g, I.m, fac + I.eoff, K, (T)I.sigma, dinv + o, b + o, x + o, r + o, z + o, p + o, q + o,
+                     w + 24 * I.eoff, iters);
+}
+template <typename T>
+void launch_batch_coarse_pcg(const BatchInst* in, int ninst, const T* fac, const ModalK<T>& K, const T* dinv,
+                             const T* b, T* x, T* r, T* z, T* p, T* q, T* w, int iters, const PcgScalars* s,
+                             cudaStream_t st) {
+  batch_coarse_pcg_kernel<T><<<ninst, 1024, 0, st>>>(in, fac, K, dinv, b, x, r, z, p, q, w, iters, s);
 }
 
 #define INST(T)                                                                                     \
@@ -349,7 +450,16 @@ void launch_coarse_pcg(const Grid& g, const Mask& m, const T* fac, const ModalK<
   template void launch_jacobi0<T>(const Grid&, const Mask&, const T*, const ModalK<T>&, int, T, T,  \
                                   const T*, T*, const int*, cudaStream_t);                          \
   template void launch_coarse_pcg<T>(const Grid&, const Mask&, const T*, const ModalK<T>&, T, const T*, \
-                                     const T*, T*, T*, T*, T*, T*, T*, int, const int*, cudaStream_t);
+                                     const T*, T*, T*, T*, T*, T*, T*, int, const int*, cudaStream_t);     \
+  template void launch_batch_restrict<T>(const BatchInst*, int, int, const T*, T*, const PcgScalars*,     \
+                                         cudaStream_t);                                                   \
+  template void launch_batch_prolong_add<T>(const BatchInst*, int, int, const T*, T*, const PcgScalars*,  \
+                                            cudaStream_t);                                                \
+  template void launch_batch_jacobi0<T>(const BatchInst*, int, int, const T*, const ModalK<T>&, int, T,   \
+                                        const T*, T*, const PcgScalars*, cudaStream_t);                   \
+  template void launch_batch_coarse_pcg<T>(const BatchInst*, int, const T*, const ModalK<T>&, const T*,   \
+                                           const T*, T*, T*, T*, T*, T*, T*, int, const PcgScalars*,      \
+                                           cudaStream_t);
 INST(double)
 INST(float)
 #undef INST

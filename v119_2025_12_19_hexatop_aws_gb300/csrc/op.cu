@@ -15,6 +15,8 @@
 // epilogue fuses the PCG dot, the residual b - Ax, a damped-Jacobi step or a
 // Chebyshev step.
 #include <algorithm>
+#include <cmath>
+#include <vector>
 
 #include "hexa_common.cuh"
 #include "hexa_kernels.h"
@@ -149,12 +151,40 @@ __device__ __forceinline__ void element_modal(const ModalK<T>& K, const T (&L)[4
     }
 }
 
+// CTA height in warps: FP32 CTAs of 8 warps, two resident per SM, so that one
+// CTA's warps issue while the other waits at its per-layer barrier.
+#ifndef HEXA_OP_TYW32
+#define HEXA_OP_TYW32 8
+#endif
+template <typename T>
+constexpr int op_tyw() { return sizeof(T) == 8 ? 8 : HEXA_OP_TYW32; }
+template <typename T>
+constexpr int op_min_ctas() { return sizeof(T) == 8 ? 1 : (HEXA_OP_TYW32 <= 8 ? 2 : 1); }
+
+// Four values of the y-exchange as one 16-byte shared-memory access per thread
+// (float4; two 16-byte halves for double).
+__device__ __forceinline__ void store4(float* p, float a, float b, float c, float d) {
+  *reinterpret_cast<float4*>(p) = make_float4(a, b, c, d);
+}
+__device__ __forceinline__ void store4(double* p, double a, double b, double c, double d) {
+  reinterpret_cast<double2*>(p)[0] = make_double2(a, b);
+  reinterpret_cast<double2*>(p)[1] = make_double2(c, d);
+}
+__device__ __forceinline__ void load4(const float* p, float (&v)[4]) {
+  const float4 t = *reinterpret_cast<const float4*>(p);
+  v[0] = t.x, v[1] = t.y, v[2] = t.z, v[3] = t.w;
+}
+__device__ __forceinline__ void load4(const double* p, double (&v)[4]) {
+  const double2 t0 = reinterpret_cast<const double2*>(p)[0], t1 = reinterpret_cast<const double2*>(p)[1];
+  v[0] = t0.x, v[1] = t0.y, v[2] = t1.x, v[3] = t1.y;
+}
+
 // One work item: the node columns of tile (tx, ty) for node layers [k0, k1).
 // IX is the index type: int whenever 3 * nNodes fits, which halves the
 // integer work of the address arithmetic.
-template <typename T, int MODE, int TYW, typename IX>
-__device__ __forceinline__ void op_item(const OpArgs<T>& a, int tx, int ty, int chunk,
-                                        T (&xch)[2][TYW][32][(MODE == OP_JACOBI || MODE == OP_CHEB2) ? 4 : 3],
+template <typename T, int MODE, int TYW, typename IX, typename A>
+__device__ __forceinline__ void op_item(const A& a, int tx, int ty, int chunk,
+                                        T (&xch)[2][TYW][32][4],
                                         double& acc0, long long co) {
   constexpr int NX_OWN = 31, NY_OWN = TYW - 1;
   constexpr bool NEED_F = (MODE == OP_JACOBI || MODE == OP_CHEB2);
@@ -251,21 +281,21 @@ __device__ __forceinline__ void op_item(const OpArgs<T>& a, int tx, int ty, int 
     }
     fprev = f;
     const int buf = k & 1;
-#pragma unroll
-    for (int c = 0; c < 3; ++c) xch[buf][wy][lane][c] = T0[c];
-    if (NEED_F) xch[buf][wy][lane][NEED_F ? 3 : 0] = F1;
+    store4(&xch[buf][wy][lane][0], T0[0], T0[1], T0[2], F1);  // one vector store, no bank conflicts
     __syncthreads();
     if (own) {
       const IX n = ncol + nplane * (IX)k;
       unsigned fx = colfix;
       if (((F & 16u) && k == 0) || ((F & 32u) && k == g.NZ - 1)) fx = 7u;
       if (a.m.node) fx |= (unsigned)__ldg(a.m.node + n);
+      T nb[4];
+      load4(&xch[buf][wy + 1][lane][0], nb);
       T Kx[3];
 #pragma unroll
-      for (int c = 0; c < 3; ++c) Kx[c] = T1[c] + xch[buf][wy + 1][lane][c];
+      for (int c = 0; c < 3; ++c) Kx[c] = T1[c] + nb[c];
       T dinv[3] = {T(0), T(0), T(0)};
       if (NEED_F) {
-        const T fsum = F1 + xch[buf][wy + 1][lane][NEED_F ? 3 : 0];
+        const T fsum = F1 + nb[3];
         if (a.diag_quirk) {
           const T r = recip(fma(a.K.dd[0], fsum, a.sigma));
           dinv[0] = dinv[1] = dinv[2] = r;
@@ -305,10 +335,10 @@ __device__ __forceinline__ void op_item(const OpArgs<T>& a, int tx, int ty, int 
   __syncthreads();  // the next item reuses xch
 }
 
-template <typename T, int MODE, int TYW, typename IX>
-__global__ void __launch_bounds__(32 * TYW) op_kernel(const OpArgs<T> a) {
+template <typename T, int MODE, int TYW, typename IX, bool MULTI>
+__global__ void __launch_bounds__(32 * TYW, op_min_ctas<T>()) op_kernel(const OpArgs<T> a) {
   if (a.halt && *((volatile const int*)a.halt)) return;
-  __shared__ T xch[2][TYW][32][(MODE == OP_JACOBI || MODE == OP_CHEB2) ? 4 : 3];
+  __shared__ __align__(16) T xch[2][TYW][32][4];
   double acc0 = 0.0;
   // static stride over (tile x, tile y, z-chunk) items: deterministic, and
   // with the grid sized to the resident CTAs no wave is left half empty
@@ -317,8 +347,11 @@ __global__ void __launch_bounds__(32 * TYW) op_kernel(const OpArgs<T> a) {
   for (int item = blockIdx.x; item < items; item += gridDim.x) {
     const int chunk = item / nxy, t = item - chunk * nxy;
     const int ty = t / a.tiles_x, tx = t - ty * a.tiles_x;
-    // every column of a multi-column apply reuses the item's factors from L1
-    for (int col = 0; col < a.ncol; ++col) op_item<T, MODE, TYW, IX>(a, tx, ty, chunk, xch, acc0, col * a.g.ndof());
+    if (MULTI) {  // every column of a multi-column apply reuses the item's factors from L1
+      for (int col = 0; col < a.ncol; ++col) op_item<T, MODE, TYW, IX>(a, tx, ty, chunk, xch, acc0, col * a.g.ndof());
+    } else {
+      op_item<T, MODE, TYW, IX>(a, tx, ty, chunk, xch, acc0, 0);
+    }
   }
   if (MODE == OP_APPLY_DOT || MODE == OP_RESID_NORM) {
     double v[1] = {acc0};
@@ -336,8 +369,6 @@ static ModalK<T> cast_modal(const ModalK<double>& K) {
   return o;
 }
 
-template <typename T>
-constexpr int op_tyw() { return sizeof(T) == 8 ? 8 : 16; }
 
 template <typename T, int MODE>
 static int op_resident_ctas() {
@@ -346,7 +377,7 @@ static int op_resident_ctas() {
     int dev = 0, sms = 0, occ = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, op_kernel<T, MODE, op_tyw<T>(), long long>, 32 * op_tyw<T>(), 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, op_kernel<T, MODE, op_tyw<T>(), long long, false>, 32 * op_tyw<T>(), 0);
     cached = std::max(1, sms) * std::max(1, occ);
   }
   return cached;
@@ -400,10 +431,20 @@ void launch_op(int mode, const OpArgs<T>& a0, cudaStream_t st) {
   const int grid = (int)std::min<long long>(items, resident_ctas<T>(mode));
   const dim3 block(32, TYW);
   const bool i32 = a.g.ndof() < (1LL << 30) && a.g.nelem() < (1LL << 30);
+  if (a.ncol > 1) {  // multi-column forms: the plain apply and the residual
+    if (mode == OP_APPLY) {
+      if (i32) op_kernel<T, OP_APPLY, TYW, int, true><<<grid, block, 0, st>>>(a);
+      else op_kernel<T, OP_APPLY, TYW, long long, true><<<grid, block, 0, st>>>(a);
+    } else if (mode == OP_RESID) {
+      if (i32) op_kernel<T, OP_RESID, TYW, int, true><<<grid, block, 0, st>>>(a);
+      else op_kernel<T, OP_RESID, TYW, long long, true><<<grid, block, 0, st>>>(a);
+    }
+    return;
+  }
 #define HEXA_OP_CASE(M)                                                              \
   case M:                                                                           \
-    if (i32) op_kernel<T, M, TYW, int><<<grid, block, 0, st>>>(a);                  \
-    else op_kernel<T, M, TYW, long long><<<grid, block, 0, st>>>(a);                \
+    if (i32) op_kernel<T, M, TYW, int, false><<<grid, block, 0, st>>>(a);           \
+    else op_kernel<T, M, TYW, long long, false><<<grid, block, 0, st>>>(a);         \
     break;
   switch (mode) {
     HEXA_OP_CASE(OP_APPLY)
@@ -416,6 +457,110 @@ void launch_op(int mode, const OpArgs<T>& a0, cudaStream_t st) {
   }
 #undef HEXA_OP_CASE
 }
+
+// ---------------------------------------------------------------- batches
+// The arguments op_item reads, for one instance of a batch: the grid, the
+// mask and the pointers of the instance, the shared K0 blocks by reference
+// (to the kernel's __grid_constant__ parameter: no copy).
+template <typename T>
+struct ItemArgs {
+  Grid g;
+  Mask m;
+  const T* x;
+  const T* fac;
+  const T* b;
+  T* y;
+  const T* xin;
+  T c1, c2;
+  const ModalK<T>& K;
+  T sigma, omega;
+  int kchunk, diag_quirk;
+};
+
+__device__ __forceinline__ int batch_find_op(const BatchInst* in, int n, int b) {
+  int lo = 0, hi = n - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (in[mid].oblk0 <= b) lo = mid;
+    else hi = mid - 1;
+  }
+  return lo;
+}
+
+// One launch over every instance of a batch: instance i's blocks run the
+// static-stride item loop of op_kernel over its own (tile, z-chunk) items;
+// an instance whose solve has halted returns at once.
+template <typename T, int MODE, int TYW, typename IX>
+__global__ void __launch_bounds__(32 * TYW, op_min_ctas<T>()) op_batch_kernel(const __grid_constant__ BatchOpArgs<T> a) {
+  __shared__ __align__(16) T xch[2][TYW][32][4];
+  const BatchInst& I = a.inst[batch_find_op(a.inst, a.ninst, blockIdx.x)];
+  const int id = I.id;
+  if (a.s && *((volatile const int*)&a.s[id].halt)) return;
+  const ItemArgs<T> ia{I.g,      I.m,      a.x + I.off,  a.fac + I.eoff,  a.b ? a.b + I.off : a.b,
+                       a.y + I.off, a.xin ? a.xin + I.off : a.xin, a.c1, a.c2, a.K, (T)I.sigma, a.omega,
+                       I.kchunk, a.diag_quirk};
+  const int txs = I.tiles_x, nxy = I.tiles_x * I.tiles_y, items = nxy * I.nchunks;
+  const int local = blockIdx.x - I.oblk0, nb = I.onblk;
+  double acc0 = 0.0;
+  for (int item = local; item < items; item += nb) {
+    const int chunk = item / nxy, t = item - chunk * nxy;
+    const int ty = t / txs, tx = t - ty * txs;
+    op_item<T, MODE, TYW, IX>(ia, tx, ty, chunk, xch, acc0, 0);
+  }
+  if (MODE == OP_APPLY_DOT || MODE == OP_RESID_NORM) {
+    double v[1] = {acc0};
+    block_reduce_finalize_at<1>(a.red, v, id, blockIdx.x, nb, I.oblk0, 1);
+  }
+}
+
+template <typename T>
+int op_batch_plan(BatchInst* in, int n, int kchunk) {
+  long long total = 0;
+  std::vector<long long> items(n);
+  const int kc = kchunk > 0 ? kchunk : 16;
+  for (int i = 0; i < n; ++i) {
+    BatchInst& b = in[i];
+    b.kchunk = std::max(1, std::min(kc, b.g.NZ));
+    op_tiles<T>(b.g, b.kchunk, &b.tiles_x, &b.tiles_y, &b.nchunks);
+    items[i] = (long long)b.tiles_x * b.tiles_y * b.nchunks;
+    total += items[i];
+  }
+  const double per = std::max(1.0, (double)total / std::max(1, resident_ctas<T>(OP_CHEB2)));
+  int blk = 0;
+  for (int i = 0; i < n; ++i) {
+    const long long want = (long long)std::ceil((double)items[i] / per);
+    in[i].oblk0 = blk;
+    in[i].onblk = (int)std::max<long long>(1, std::min<long long>(items[i], want));
+    blk += in[i].onblk;
+  }
+  return blk;
+}
+
+template <typename T>
+void launch_op_batch(int mode, const BatchOpArgs<T>& a, bool idx32, cudaStream_t st) {
+  constexpr int TYW = op_tyw<T>();
+  const dim3 block(32, TYW);
+#define HEXA_OPB_CASE(M)                                                                          \
+  case M:                                                                                        \
+    if (idx32) op_batch_kernel<T, M, TYW, int><<<a.nblocks, block, 0, st>>>(a);                  \
+    else op_batch_kernel<T, M, TYW, long long><<<a.nblocks, block, 0, st>>>(a);                  \
+    break;
+  switch (mode) {
+    HEXA_OPB_CASE(OP_APPLY)
+    HEXA_OPB_CASE(OP_APPLY_DOT)
+    HEXA_OPB_CASE(OP_RESID)
+    HEXA_OPB_CASE(OP_RESID_NORM)
+    HEXA_OPB_CASE(OP_JACOBI)
+    HEXA_OPB_CASE(OP_CHEB2)
+    default: break;
+  }
+#undef HEXA_OPB_CASE
+}
+
+template int op_batch_plan<double>(BatchInst*, int, int);
+template int op_batch_plan<float>(BatchInst*, int, int);
+template void launch_op_batch<double>(int, const BatchOpArgs<double>&, bool, cudaStream_t);
+template void launch_op_batch<float>(int, const BatchOpArgs<float>&, bool, cudaStream_t);
 
 template void launch_op<double>(int, const OpArgs<double>&, cudaStream_t);
 template void launch_op<float>(int, const OpArgs<float>&, cudaStream_t);

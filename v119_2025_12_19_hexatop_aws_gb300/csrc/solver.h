@@ -55,6 +55,12 @@ int solve_problem(Ctx& c, const Problem& P, const hexa_solve_params& prm, const 
 int multi_rhs_problem(Ctx& c, const Problem& P, int k, const double* F_dev,
                       const hexa_solve_params& prm, double* U_dev, hexa_solve_stats* st);
 
+int batch_problem(Ctx& c, int count, const hexa_grid* grids, const hexa_bc* bcs, double nu,
+                  const double* const* factors, const double* const* forces, const hexa_solve_params& prm,
+                  double* const* u_out, hexa_solve_stats* stats);
+int batch_filter(Ctx& c, int count, const hexa_grid* grids, const double* const* rho_in, double radius, double tol,
+                 int max_iter, int quirk, int precision, double* const* rho_out, hexa_filter_stats* stats);
+
 bool build_modal(double dx, double dy, double dz, double nu, ModalK<double>* K, std::string* err);
 
 }  // namespace hexa

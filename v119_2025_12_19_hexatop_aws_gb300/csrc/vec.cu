@@ -9,6 +9,7 @@
 // live in device memory, so no scalar ever returns to the host inside an
 // iteration.
 #include <algorithm>
+#include <cmath>
 
 #include "hexa_common.cuh"
 #include "hexa_kernels.h"
@@ -375,6 +376,177 @@ void launch_scalars_init(PcgScalars* s, const PcgScalars* parent, int max_iter, 
   scalars_init_kernel<<<1, 64, 0, st>>>(s, parent, max_iter, ncol);
 }
 
+// ------------------------------------------------------------ batch passes
+// Block b belongs to the instance whose [vblk0, vblk0 + vnblk) holds b; it
+// strides over that instance's segment with the instance's block count.
+__device__ __forceinline__ int batch_find_vec(const BatchInst* in, int n, int b) {
+  int lo = 0, hi = n - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (in[mid].vblk0 <= b) lo = mid;
+    else hi = mid - 1;
+  }
+  return lo;
+}
+
+struct BatchSeg {
+  int id;
+  long long off, n, first, stride, blk0, nblk;
+};
+__device__ __forceinline__ BatchSeg batch_seg(const BatchInst* in, int ninst, int node_sized) {
+  const BatchInst& I = in[batch_find_vec(in, ninst, blockIdx.x)];
+  BatchSeg sg;
+  sg.id = I.id;
+  sg.off = node_sized ? I.noff : I.off;
+  sg.n = node_sized ? I.g.nnode() : I.g.ndof();
+  sg.blk0 = I.vblk0;
+  sg.nblk = I.vnblk;
+  sg.first = (long long)(blockIdx.x - I.vblk0) * blockDim.x + threadIdx.x;
+  sg.stride = (long long)I.vnblk * blockDim.x;
+  return sg;
+}
+__device__ __forceinline__ bool inst_halted(const PcgScalars* s, int id) {
+  return s && *((volatile const int*)&s[id].halt);
+}
+
+template <typename T, bool JAC>
+__global__ void batch_pcg_update_kernel(const BatchInst* in, int ninst, int node_sized, T* __restrict__ x,
+                                        T* __restrict__ r, T* __restrict__ z, const T* __restrict__ p,
+                                        const T* __restrict__ q, const T* __restrict__ dinv, RedArgs red,
+                                        const PcgScalars* s) {
+  const BatchSeg sg = batch_seg(in, ninst, node_sized);
+  if (inst_halted(s, sg.id)) return;
+  const T alpha = (T)s[sg.id].alpha;
+  constexpr int NS = JAC ? 2 : 1;
+  double acc[NS];
+  T part[NS];
+#pragma unroll
+  for (int k = 0; k < NS; ++k) acc[k] = 0.0, part[k] = T(0);
+  int cnt = 0;
+  for (long long i = sg.first; i < sg.n; i += sg.stride) {
+    const long long k = sg.off + i;
+    x[k] = fma(alpha, p[k], x[k]);
+    const T ri = fma(-alpha, q[k], r[k]);
+    r[k] = ri;
+    part[0] = fma(ri, ri, part[0]);
+    if (JAC) {
+      const T zi = ri * dinv[k];
+      z[k] = zi;
+      part[NS - 1] = fma(ri, zi, part[NS - 1]);
+    }
+    if (++cnt == kChunk) flush_parts<T, NS>(acc, part, cnt);
+  }
+  flush_parts<T, NS>(acc, part, cnt);
+  block_reduce_finalize_at<NS>(red, acc, sg.id, blockIdx.x, sg.nblk, sg.blk0, 1);
+}
+template <typename T>
+void launch_batch_pcg_update(const BatchInst* in, int ninst, int nblocks, int node_sized, T* x, T* r, T* z,
+                             const T* p, const T* q, const T* dinv, const RedArgs& red, const PcgScalars* s,
+                             cudaStream_t st) {
+  if (dinv) batch_pcg_update_kernel<T, true><<<nblocks, 256, 0, st>>>(in, ninst, node_sized, x, r, z, p, q, dinv, red, s);
+  else batch_pcg_update_kernel<T, false><<<nblocks, 256, 0, st>>>(in, ninst, node_sized, x, r, z, p, q, dinv, red, s);
+}
+
+template <typename T>
+__global__ void batch_p_update_kernel(const BatchInst* in, int ninst, int node_sized, T* __restrict__ p,
+                                      const T* __restrict__ z, const PcgScalars* s) {
+  const BatchSeg sg = batch_seg(in, ninst, node_sized);
+  if (inst_halted(s, sg.id)) return;
+  const T beta = (T)s[sg.id].beta;
+  for (long long i = sg.first; i < sg.n; i += sg.stride) p[sg.off + i] = fma(beta, p[sg.off + i], z[sg.off + i]);
+}
+template <typename T>
+void launch_batch_p_update(const BatchInst* in, int ninst, int nblocks, int node_sized, T* p, const T* z,
+                           const PcgScalars* s, cudaStream_t st) {
+  batch_p_update_kernel<T><<<nblocks, 256, 0, st>>>(in, ninst, node_sized, p, z, s);
+}
+
+template <typename T, int NS>
+__global__ void batch_dot_kernel(const BatchInst* in, int ninst, int node_sized, const T* __restrict__ a,
+                                 const T* __restrict__ b, const T* __restrict__ c, const T* __restrict__ d,
+                                 RedArgs red, const PcgScalars* s) {
+  const BatchSeg sg = batch_seg(in, ninst, node_sized);
+  if (inst_halted(s, sg.id)) return;
+  double acc[NS];
+  T part[NS];
+#pragma unroll
+  for (int k = 0; k < NS; ++k) acc[k] = 0.0, part[k] = T(0);
+  int cnt = 0;
+  for (long long i = sg.first; i < sg.n; i += sg.stride) {
+    const long long k = sg.off + i;
+    part[0] = fma(a[k], b[k], part[0]);
+    if (NS > 1) part[NS - 1] = fma(c[k], d[k], part[NS - 1]);
+    if (++cnt == kChunk) flush_parts<T, NS>(acc, part, cnt);
+  }
+  flush_parts<T, NS>(acc, part, cnt);
+  block_reduce_finalize_at<NS>(red, acc, sg.id, blockIdx.x, sg.nblk, sg.blk0, 1);
+}
+template <typename T>
+void launch_batch_dot(const BatchInst* in, int ninst, int nblocks, int node_sized, const T* a, const T* b,
+                      const T* c, const T* d, const RedArgs& red, const PcgScalars* s, cudaStream_t st) {
+  if (c) batch_dot_kernel<T, 2><<<nblocks, 256, 0, st>>>(in, ninst, node_sized, a, b, c, d, red, s);
+  else batch_dot_kernel<T, 1><<<nblocks, 256, 0, st>>>(in, ninst, node_sized, a, b, c, d, red, s);
+}
+
+template <typename T>
+__global__ void batch_from64_kernel(const BatchInst* in, int ninst, T* __restrict__ dst,
+                                    const double* __restrict__ src, const double* scale) {
+  const BatchSeg sg = batch_seg(in, ninst, 0);
+  const double sc = scale[sg.id];
+  for (long long i = sg.first; i < sg.n; i += sg.stride) dst[sg.off + i] = (T)(src[sg.off + i] * sc);
+}
+template <typename T>
+void launch_batch_from64(const BatchInst* in, int ninst, int nblocks, T* dst, const double* src,
+                         const double* scale, cudaStream_t st) {
+  batch_from64_kernel<T><<<nblocks, 256, 0, st>>>(in, ninst, dst, src, scale);
+}
+
+template <typename T>
+__global__ void batch_accum_kernel(const BatchInst* in, int ninst, double* __restrict__ u, const T* __restrict__ d,
+                                   const double* scale) {
+  const BatchSeg sg = batch_seg(in, ninst, 0);
+  const double sc = scale[sg.id];
+  if (sc == 0.0) return;
+  const double inv = 1.0 / sc;
+  for (long long i = sg.first; i < sg.n; i += sg.stride) u[sg.off + i] = fma((double)d[sg.off + i], inv, u[sg.off + i]);
+}
+template <typename T>
+void launch_batch_accum(const BatchInst* in, int ninst, int nblocks, double* u, const T* d, const double* scale,
+                        cudaStream_t st) {
+  batch_accum_kernel<T><<<nblocks, 256, 0, st>>>(in, ninst, u, d, scale);
+}
+
+__global__ void batch_set_beta_kernel(PcgScalars* s, const double* coef, int n) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) s[i].beta = s[i].rz * coef[i];
+}
+void launch_batch_set_beta(PcgScalars* s, const double* coef, int n, cudaStream_t st) {
+  batch_set_beta_kernel<<<(n + 127) / 128, 128, 0, st>>>(s, coef, n);
+}
+
+int vec_batch_plan(BatchInst* in, int n, int unit, int max_blocks) {
+  auto units = [&](const BatchInst& b) -> long long {
+    switch (unit) {
+      case 1: return b.g.nnode();
+      case 2: return b.g.nelem();
+      case 3: return b.g2.nnode();
+      default: return b.g.ndof();
+    }
+  };
+  long long total = 0;
+  for (int i = 0; i < n; ++i) total += units(in[i]);
+  const double per = std::max(256.0, (double)total / std::max(1, max_blocks));
+  int blk = 0;
+  for (int i = 0; i < n; ++i) {
+    const long long u = units(in[i]);
+    const long long want = (long long)std::ceil((double)u / per);
+    in[i].vblk0 = blk;
+    in[i].vnblk = (int)std::max<long long>(1, std::min<long long>((u + 255) / 256, want));
+    blk += in[i].vnblk;
+  }
+  return blk;
+}
+
 #define INST(T)                                                                                 \
   template void launch_fill<T>(T*, T, long long, cudaStream_t);                                 \
   template void launch_copy<T>(T*, const T*, long long, cudaStream_t);                          \
@@ -388,7 +560,17 @@ void launch_scalars_init(PcgScalars* s, const PcgScalars* parent, int max_iter, 
   template void launch_scale_add_cols<T>(T*, const double*, const T*, long long, int, cudaStream_t); \
   template void launch_jacobi_precond<T>(T*, const T*, const T*, long long, const RedArgs&, int, \
                                          const int*, cudaStream_t);                             \
-  template void launch_axpby<T>(T*, T, const T*, T, long long, cudaStream_t);
+  template void launch_axpby<T>(T*, T, const T*, T, long long, cudaStream_t);                    \
+  template void launch_batch_pcg_update<T>(const BatchInst*, int, int, int, T*, T*, T*, const T*, const T*, \
+                                           const T*, const RedArgs&, const PcgScalars*, cudaStream_t);      \
+  template void launch_batch_p_update<T>(const BatchInst*, int, int, int, T*, const T*, const PcgScalars*,  \
+                                         cudaStream_t);                                                     \
+  template void launch_batch_dot<T>(const BatchInst*, int, int, int, const T*, const T*, const T*, const T*, \
+                                    const RedArgs&, const PcgScalars*, cudaStream_t);                       \
+  template void launch_batch_from64<T>(const BatchInst*, int, int, T*, const double*, const double*,        \
+                                       cudaStream_t);                                                       \
+  template void launch_batch_accum<T>(const BatchInst*, int, int, double*, const T*, const double*,         \
+                                      cudaStream_t);
 INST(double)
 INST(float)
 #undef INST

@@ -40,6 +40,27 @@ def filter_density(grid: _lib.Grid, rho, radius: float, *, tol: float = 1e-5, ma
     return out, {"iterations": st.iterations, "relres": st.relres, "solve_ms": st.solve_ms}
 
 
+def filter_batch(grids, rhos, radius: float, *, tol: float = 1e-5, max_iter: int = 200, quirk: bool = True,
+                 precision: str = "fp64", out=None, ctx: _lib.Context | None = None):
+    """The filter of filter_density over grids of uneven sizes in one batch.
+    Returns (list of filtered densities, list of stats dicts)."""
+    ctx = ctx or context()
+    n = len(grids)
+    if len(rhos) != n or n < 1:
+        raise ValueError("grids and rhos must have the same (non-zero) length")
+    if out is None:
+        out = [np.empty(g.nx * g.ny * g.nz) for g in grids]
+    G = (_lib.Grid * n)(*grids)
+    rp = (C.c_void_p * n)(*[_lib.ptr(a) for a in rhos])
+    op = (C.c_void_p * n)(*[_lib.ptr(a) for a in out])
+    st = (_lib.FilterStats * n)()
+    rc = ctx.lib.hexa_filter_batch(ctx.h, n, G, rp, float(radius), float(tol), int(max_iter), int(bool(quirk)),
+                                   _lib.PRECISION[precision], op, st)
+    ctx.check(rc, allow=(_lib.HEXA_OK,))
+    return out, [{"iterations": st[i].iterations, "relres": st[i].relres, "solve_ms": st[i].solve_ms}
+                 for i in range(n)]
+
+
 def apply_gpu_filter(density_cpu, nElem_x, nElem_y, nElem_z, dx, dy, dz, radius, elements_cpu=None, tol=1.0e-5,
                      *, quirk=True, precision="fp32", max_iter=200):
     """Drop-in for apply_gpu_filter! (GPUHelmholtz.jl:422-443).

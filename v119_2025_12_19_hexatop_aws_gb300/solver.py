@@ -114,6 +114,33 @@ def solve_multi_rhs(grid: _lib.Grid, factor, F, *, clamp_faces: int = 0, fixed_d
     return U_out, st.as_dict()
 
 
+def solve_batch(grids, factors, forces, *, clamp_faces=0, nu: float = 0.3, params: _lib.SolveParams | None = None,
+                u_out=None, ctx: _lib.Context | None = None):
+    """Solve independent problems on grids of uneven sizes in one batch.
+
+    grids: list of _lib.Grid (same element size); factors[i] (nElem_i) and
+    forces[i] (3*nNodes_i) float64 numpy arrays or CUDA tensors; clamp_faces an
+    int for all instances or one per instance.  Mixed precision GMG-PCG.
+    Returns (list of u, list of stats dicts, status)."""
+    ctx = ctx or context()
+    params = params or _lib.default_params(precision="mixed", precond="multigrid")
+    n = len(grids)
+    if not (len(factors) == len(forces) == n) or n < 1:
+        raise ValueError("grids, factors and forces must have the same (non-zero) length")
+    faces = [clamp_faces] * n if np.isscalar(clamp_faces) else list(clamp_faces)
+    if u_out is None:
+        u_out = [np.empty(3 * (g.nx + 1) * (g.ny + 1) * (g.nz + 1)) for g in grids]
+    G = (_lib.Grid * n)(*grids)
+    bcs = (_lib.BC * n)(*[_lib.make_bc(fc) for fc in faces])
+    fac_p = (C.c_void_p * n)(*[_lib.ptr(a) for a in factors])
+    f_p = (C.c_void_p * n)(*[_lib.ptr(a) for a in forces])
+    u_p = (C.c_void_p * n)(*[_lib.ptr(a) for a in u_out])
+    st = (_lib.SolveStats * n)()
+    rc = ctx.lib.hexa_solve_batch(ctx.h, n, G, bcs, float(nu), fac_p, f_p, C.byref(params), u_p, st)
+    ctx.check(rc)
+    return u_out, [st[i].as_dict() for i in range(n)], rc
+
+
 def solve_system_gpu(nodes, elements, E, nu, bc, f, density, *, max_iter=40000, tol=1e-6, method="native",
                      solver="cg", use_precond=True, shift_factor=1.0e-4, min_stiffness_threshold=1.0e-3,
                      u_guess=None, config=None):
