@@ -83,7 +83,9 @@ typedef struct hexa_solve_params {
   int32_t smoother;           /* HEXA_SMOOTH_* */
   double jacobi_omega;
   int32_t cheb_degree;
-  int32_t coarse_iters;       /* Jacobi-PCG iterations of the coarsest-level solve */
+  int32_t coarse_iters;       /* Jacobi-PCG iterations of the coarsest-level solve when that grid
+                                 has more than 640 DOFs (smaller ones are solved exactly, by the
+                                 dense inverse of their operator) */
   double inner_tol;           /* mixed: relative tolerance of each FP32 correction solve */
   int32_t max_outer;          /* mixed: maximum refinement steps */
   int32_t use_graphs;         /* capture PCG iterations / V-cycles in CUDA graphs */

@@ -261,6 +261,9 @@ void launch_batch_prolong_add(const BatchInst* in, int ninst, int nblocks, const
 template <typename T>
 void launch_batch_jacobi0(const BatchInst* in, int ninst, int nblocks, const T* fac, const ModalK<T>& K, int quirk,
                           T omega, const T* b, T* x, const PcgScalars* s, cudaStream_t st);
+// x = A^-1 b with a dense symmetric n x n inverse (exact coarsest-level solve)
+template <typename T>
+void launch_dense_coarse(long long n, const T* A, const T* b, T* x, const int* halt, cudaStream_t st);
 // one CTA per instance: iters Jacobi-PCG iterations on its coarsest grid
 template <typename T>
 void launch_batch_coarse_pcg(const BatchInst* in, int ninst, const T* fac, const ModalK<T>& K, const T* dinv,

@@ -441,6 +441,33 @@ void launch_batch_coarse_pcg(const BatchInst* in, int ninst, const T* fac, const
   batch_coarse_pcg_kernel<T><<<ninst, 1024, 0, st>>>(in, fac, K, dinv, b, x, r, z, p, q, w, iters, s);
 }
 
+// Exact coarsest-level solve: x = A^-1 b with the dense symmetric inverse
+// (n x n, zero rows/columns at fixed DOFs).  CTA = 32 rows, 8 warps split the
+// columns; lane = row, so each column read is one coalesced 128-byte access.
+template <typename T>
+__global__ void __launch_bounds__(256) dense_coarse_kernel(int n, const T* __restrict__ A, const T* __restrict__ b,
+                                                           T* __restrict__ x, const int* halt) {
+  if (halt && *((volatile const int*)halt)) return;
+  __shared__ T part[8][32];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int row = blockIdx.x * 32 + lane;
+  T s = T(0);
+  if (row < n)
+    for (int j = w; j < n; j += 8) s = fma(A[(long long)j * n + row], b[j], s);
+  part[w][lane] = s;
+  __syncthreads();
+  if (w == 0 && row < n) {
+    T t = T(0);
+#pragma unroll
+    for (int q = 0; q < 8; ++q) t += part[q][lane];
+    x[row] = t;
+  }
+}
+template <typename T>
+void launch_dense_coarse(long long n, const T* A, const T* b, T* x, const int* halt, cudaStream_t st) {
+  dense_coarse_kernel<T><<<(int)((n + 31) / 32), 256, 0, st>>>((int)n, A, b, x, halt);
+}
+
 #define INST(T)                                                                                     \
   template void launch_coarsen_factors<T>(const Grid&, const T*, const Grid&, T*, cudaStream_t);    \
   template void launch_restrict<T>(const Grid&, const T*, const Grid&, const Mask&, T*, const int*, \
@@ -451,6 +478,7 @@ void launch_batch_coarse_pcg(const BatchInst* in, int ninst, const T* fac, const
                                   const T*, T*, const int*, cudaStream_t);                          \
   template void launch_coarse_pcg<T>(const Grid&, const Mask&, const T*, const ModalK<T>&, T, const T*, \
                                      const T*, T*, T*, T*, T*, T*, T*, int, const int*, cudaStream_t);     \
+  template void launch_dense_coarse<T>(long long, const T*, const T*, T*, const int*, cudaStream_t);     \
   template void launch_batch_restrict<T>(const BatchInst*, int, int, const T*, T*, const PcgScalars*,     \
                                          cudaStream_t);                                                   \
   template void launch_batch_prolong_add<T>(const BatchInst*, int, int, const T*, T*, const PcgScalars*,  \

@@ -127,6 +127,7 @@ struct Lev {
   T* r = nullptr;   // level residual
   T* dinv = nullptr, *p = nullptr, *q = nullptr, *z = nullptr;  // coarsest-level PCG
   T* w = nullptr;  // element-product scratch of the single-CTA coarse solve
+  T* ainv = nullptr;  // dense inverse of the coarsest operator (small coarse grids)
   T sigma = 0;
   int kchunk = 4;
 };
@@ -143,6 +144,7 @@ struct MG {
   // d_s = c1[s] d_{s-1} + c2[s] D^-1 r_s
   T inv_theta = T(0);
   std::vector<T> c1, c2;
+  std::vector<double> ke;  // FP64 K0 of the fine element (dense coarse inverse)
 
   void set_chebyshev(double lmax, int nmax) {
     const double lmin = lmax / 30.0, th = 0.5 * (lmax + lmin), de = 0.5 * (lmax - lmin), sg = th / de;
@@ -260,6 +262,112 @@ bool build_mg(Ctx& c, MG<T>& mg, const Grid& g0, const Mask& m0, const T* fac0, 
   return Lc.dinv && Lc.p && Lc.q && Lc.z && Lc.xa;
 }
 
+// Coarsest grids of at most this many DOFs are solved exactly by one dense
+// matvec with the inverse of (K + sigma I) on their free DOFs (Cholesky in FP64
+// on the host at setup, n^3/3 flops); larger ones by the coarse PCG.
+constexpr long long kDenseCoarse = 640;
+
+template <typename T>
+void coarse_dense_setup(Ctx& c, MG<T>& mg, double sigma_c) {
+  Lev<T>& V = mg.L.back();
+  V.ainv = nullptr;
+  const long long n = V.g.ndof();
+  if (n > kDenseCoarse || mg.ke.size() != 576) return;
+  const Grid& g = V.g;
+  std::vector<T> fac(g.nelem());
+  std::vector<uint8_t> mask;
+  cudaMemcpyAsync(fac.data(), V.fac, sizeof(T) * fac.size(), cudaMemcpyDeviceToHost, c.st);
+  if (V.m.node) {
+    mask.resize(g.nnode());
+    cudaMemcpyAsync(mask.data(), V.m.node, mask.size(), cudaMemcpyDeviceToHost, c.st);
+  }
+  if (cudaStreamSynchronize(c.st) != cudaSuccess) {
+    cudaGetLastError();
+    return;
+  }
+  // free DOFs: the device's fixed_bits (clamped faces, then the node mask)
+  const uint32_t F = V.m.faces;
+  std::vector<int> fidx(n, -1);
+  int nf = 0;
+  for (int k = 0; k < g.NZ; ++k)
+    for (int j = 0; j < g.NY; ++j)
+      for (int i = 0; i < g.NX; ++i) {
+        const long long nd = i + (long long)g.NX * (j + (long long)g.NY * k);
+        unsigned fx = (((F & 1u) && i == 0) || ((F & 2u) && i == g.NX - 1) || ((F & 4u) && j == 0) ||
+                       ((F & 8u) && j == g.NY - 1) || ((F & 16u) && k == 0) || ((F & 32u) && k == g.NZ - 1))
+                          ? 7u : 0u;
+        if (!mask.empty()) fx |= mask[nd];
+        for (int cc = 0; cc < 3; ++cc)
+          if (!((fx >> cc) & 1u)) fidx[3 * nd + cc] = nf++;
+      }
+  if (nf == 0) return;
+  std::vector<double> A((size_t)nf * nf, 0.0);
+  for (int q = 0; q < nf; ++q) A[(size_t)q * nf + q] = sigma_c;
+  static const int ref_to_corner[8] = {0, 1, 3, 2, 4, 5, 7, 6};  // K0 node order (Mesh.jl:45-53) -> dx + 2dy + 4dz
+  long long dof[24];
+  for (int k = 0; k < g.nz; ++k)
+    for (int j = 0; j < g.ny; ++j)
+      for (int i = 0; i < g.nx; ++i) {
+        const double f = (double)fac[i + (long long)g.nx * (j + (long long)g.ny * k)];
+        for (int a = 0; a < 8; ++a) {
+          const int cc = ref_to_corner[a];
+          const long long nd = (i + (cc & 1)) + (long long)g.NX * ((j + ((cc >> 1) & 1)) + (long long)g.NY * (k + (cc >> 2)));
+          for (int d = 0; d < 3; ++d) dof[3 * a + d] = fidx[3 * nd + d];
+        }
+        for (int r = 0; r < 24; ++r) {
+          if (dof[r] < 0) continue;
+          for (int q = 0; q < 24; ++q)
+            if (dof[q] >= 0) A[(size_t)dof[r] * nf + dof[q]] += f * mg.ke[r + 24 * q];
+        }
+      }
+  // Cholesky A = L L^T (lower, in place); give up (coarse PCG) on a non-positive pivot
+  for (int jj = 0; jj < nf; ++jj) {
+    double d = A[(size_t)jj * nf + jj];
+    for (int m = 0; m < jj; ++m) d -= A[(size_t)jj * nf + m] * A[(size_t)jj * nf + m];
+    if (!(d > 0.0)) return;
+    const double ljj = std::sqrt(d);
+    A[(size_t)jj * nf + jj] = ljj;
+    for (int ii = jj + 1; ii < nf; ++ii) {
+      double v = A[(size_t)ii * nf + jj];
+      for (int m = 0; m < jj; ++m) v -= A[(size_t)ii * nf + m] * A[(size_t)jj * nf + m];
+      A[(size_t)ii * nf + jj] = v / ljj;
+    }
+  }
+  // inverse, column by column: L y = e_q, L^T x = y
+  std::vector<double> inv((size_t)nf * nf), y(nf);
+  for (int q = 0; q < nf; ++q) {
+    for (int ii = 0; ii < nf; ++ii) {
+      double v = ii == q ? 1.0 : 0.0;
+      for (int m = q; m < ii; ++m) v -= A[(size_t)ii * nf + m] * y[m];
+      y[ii] = ii < q ? 0.0 : v / A[(size_t)ii * nf + ii];
+    }
+    for (int ii = nf - 1; ii >= 0; --ii) {
+      double v = y[ii];
+      for (int m = ii + 1; m < nf; ++m) v -= A[(size_t)m * nf + ii] * y[m];
+      y[ii] = v / A[(size_t)ii * nf + ii];
+    }
+    for (int ii = 0; ii < nf; ++ii) inv[(size_t)ii * nf + q] = y[ii];
+  }
+  // embed (zero rows/columns at fixed DOFs); symmetric, so either order reads coalesced
+  std::vector<T> full((size_t)n * n, T(0));
+  for (long long a = 0; a < n; ++a) {
+    if (fidx[a] < 0) continue;
+    for (long long b = 0; b < n; ++b)
+      if (fidx[b] >= 0) full[(size_t)a * n + b] = (T)inv[(size_t)fidx[a] * nf + fidx[b]];
+  }
+  T* d = c.vec<T>(std::string(sizeof(T) == 8 ? "mgdense64" : "mgdense32"), (size_t)n * n);
+  if (!d) {
+    c.err.clear();
+    return;
+  }
+  cudaMemcpyAsync(d, full.data(), sizeof(T) * full.size(), cudaMemcpyHostToDevice, c.st);
+  if (cudaStreamSynchronize(c.st) != cudaSuccess) {
+    cudaGetLastError();
+    return;
+  }
+  V.ainv = d;
+}
+
 template <typename T>
 void mg_set_shift(Ctx& c, MG<T>& mg, double sigma) {
   double s = sigma;
@@ -270,12 +378,18 @@ void mg_set_shift(Ctx& c, MG<T>& mg, double sigma) {
   Lev<T>& Lc = mg.L.back();
   launch_diag<T>(Lc.g, Lc.m, Lc.fac, mg.K, mg.quirk, Lc.sigma, nullptr, Lc.dinv, c.st);
   c.launches++;
+  coarse_dense_setup<T>(c, mg, sigma * std::pow(8.0, (double)(mg.L.size() - 1)));
 }
 
 template <typename T>
 void coarse_solve(Ctx& c, MG<T>& mg, const T* b, T* x, const int* halt_main) {
   Lev<T>& V = mg.L.back();
   const long long n = V.g.ndof();
+  if (V.ainv) {  // exact: one dense matvec
+    launch_dense_coarse<T>(n, V.ainv, b, x, halt_main, c.st);
+    c.launches++;
+    return;
+  }
   if (V.w) {
     launch_coarse_pcg<T>(V.g, V.m, V.fac, mg.K, V.sigma, V.dinv, b, x, V.r, V.z, V.p, V.q, V.w, mg.citers, halt_main,
                          c.st);
@@ -609,6 +723,8 @@ void configure_mg(MG<T>& mg, const Problem& P, const hexa_solve_params& prm) {
   mg.nu2 = prm.post_smooth >= 0 ? prm.post_smooth : 2;
   mg.citers = prm.coarse_iters >= 0 ? prm.coarse_iters : 30;
   mg.set_chebyshev(lmax, std::max(mg.nu1, mg.nu2) + 1);
+  mg.ke.assign(576, 0.0);
+  if (canonical_stiffness(P.dx, P.dy, P.dz, P.nu, mg.ke.data()) != 0) mg.ke.clear();
 }
 
 bool setup_common(Ctx& c, const Problem& P, const hexa_solve_params& prm, ModalK<double>* K64, double* max_diag,
