@@ -1264,11 +1264,36 @@ int solve_block(Ctx& c, const Problem& P, int k, const hexa_solve_params& prm, d
   const bool use_mg = prm.precond == HEXA_PRECOND_MULTIGRID;
   if (use_mg) {
     hexa_solve_params prm2 = prm;
-    auto it = c.tuned.find(std::to_string(P.g.nx) + "x" + std::to_string(P.g.ny) + "x" + std::to_string(P.g.nz) +
-                           (Is64<T>::v ? "/64" : "/32"));
-    if (prm.autotune && it != c.tuned.end()) {
-      prm2.mg_levels = it->second.first;
-      prm2.pre_smooth = prm2.post_smooth = it->second.second;
+    if constexpr (!Is64<T>::v) {
+      // the single-grid autotuner (cached per grid), run on the first loaded column
+      int j0 = 0;
+      while (j0 < k - 1 && !(fnorm[j0] > 0)) ++j0;
+      if (prm.autotune && fnorm[j0] > 0) {
+        Problem P0 = P;
+        P0.f64 = P.f64 + (long long)j0 * n;
+        PcgEnv<float> E;
+        E.K = K;
+        E.quirk = prm.diag_quirk;
+        E.n = n;
+        E.x = X;
+        E.r = R;
+        E.zA = Z;
+        E.zB = Q;
+        E.p = Pd;
+        E.q = Q + n * (k > 1 ? 1 : 0);
+        E.dinv = dinv;
+        E.use_graphs = prm.use_graphs != 0;
+        E.graph_iters = prm.graph_iters > 0 ? prm.graph_iters : 10;
+        float* b32 = c.vec<float>("blk_tune_b", n);
+        float* qbuf = k > 1 ? nullptr : c.vec<float>("blk_tune_q", n);
+        if (!b32 || (k == 1 && !qbuf)) return HEXA_ERR_NOMEM;
+        if (k == 1) E.q = qbuf;
+        MG<float> tmg;
+        const std::pair<int, int> t =
+            autotune_mixed(c, P0, prm, const_cast<float*>(fac), K, sigma, E, b32, fnorm[j0], tmg);
+        prm2.mg_levels = t.first;
+        prm2.pre_smooth = prm2.post_smooth = t.second;
+      }
     }
     mg.K = K;
     configure_mg<T>(mg, P, prm2);
