@@ -245,8 +245,12 @@ def pcg_reference(g: Grid, K0, factor, f, fixed, *, tol, max_iter, shift_factor,
     return u, final_rel, PcgInfo(iters, shifts, final_rel, success, "Jacobi_GPU")
 
 
-def cg_tight(g: Grid, K0, factor, f, fixed, sigma=0.0, tol=1e-13, max_iter=200000):
-    """Plain Jacobi-PCG to a tight relative residual (oracle solution for grids too big for LU)."""
+def cg_tight(g: Grid, K0, factor, f, fixed, sigma=0.0, tol=1e-13, max_iter=200000, x0=None):
+    """Plain Jacobi-PCG to a tight relative residual (oracle solution for grids too big for LU).
+
+    x0 (full DOF vector) only shortens the run: the iteration stops on this
+    operator's own residual ||b - A x|| / ||b|| < tol, so the answer is the
+    oracle's whatever the start."""
     free = ~fixed
     d = diag_K(g, K0, factor, quirk=False)[free] + sigma
     b = np.asarray(f, dtype=np.float64)[free]
@@ -256,8 +260,8 @@ def cg_tight(g: Grid, K0, factor, f, fixed, sigma=0.0, tol=1e-13, max_iter=20000
         full[free] = v
         return apply_K(g, K0, factor, full)[free] + sigma * v
 
-    x = np.zeros_like(b)
-    r = b.copy()
+    x = np.zeros_like(b) if x0 is None else np.asarray(x0, dtype=np.float64)[free].copy()
+    r = b - A(x) if x0 is not None else b.copy()
     z = r / d
     p = z.copy()
     rz = r @ z
@@ -338,18 +342,29 @@ def helmholtz_reference(g: Grid, rho, R, tol, max_iter=200, quirk=True):
     return helm_extract(g, x), final_iter, final_rel
 
 
+_HELM_LU = {}
+
+
 def helmholtz_direct(g: Grid, rho, R, quirk=True, shift=0.0):
     """assemble_helmholtz_system + apply_helmholtz_filter_cpu (TopOpt.jl:32-127);
-    the reference's CPU path adds a 1e-9 diagonal shift (TopOpt.jl:75-76)."""
-    Ae = helm_matrix(g, R, quirk)
-    en = element_nodes(g)
-    rows = np.repeat(en, 8, axis=1).ravel()
-    cols = np.tile(en, (1, 8)).ravel()
-    vals = np.tile(Ae.ravel(order="C"), g.nelem)
-    A = sp.csc_matrix((vals, (rows, cols)), shape=(g.nnode, g.nnode))
-    if shift:
-        A = A + shift * sp.identity(g.nnode, format="csc")
-    psi = spla.spsolve(A.tocsc(), helm_rhs(g, rho))
+    the reference's CPU path adds a 1e-9 diagonal shift (TopOpt.jl:75-76).  The
+    sparse LU of the (constant) filter matrix is cached per grid and radius."""
+    key = (g.nx, g.ny, g.nz, g.dx, g.dy, g.dz, float(R), bool(quirk), float(shift))
+    lu = _HELM_LU.get(key)
+    if lu is None:
+        Ae = helm_matrix(g, R, quirk)
+        en = element_nodes(g)
+        rows = np.repeat(en, 8, axis=1).ravel()
+        cols = np.tile(en, (1, 8)).ravel()
+        vals = np.tile(Ae.ravel(order="C"), g.nelem)
+        A = sp.csc_matrix((vals, (rows, cols)), shape=(g.nnode, g.nnode))
+        if shift:
+            A = A + shift * sp.identity(g.nnode, format="csc")
+        lu = spla.splu(A.tocsc())
+        if len(_HELM_LU) > 8:
+            _HELM_LU.clear()
+        _HELM_LU[key] = lu
+    psi = lu.solve(helm_rhs(g, rho))
     return helm_extract(g, psi)
 
 
@@ -390,8 +405,11 @@ def oc_update(x, dc, dv, volfrac, move=0.2, tol=1e-12):
 
 
 def simp_loop(g: Grid, x0, f, fixed, *, nu=0.3, Emin=1e-9, E0=1.0, penal=3.0, volfrac=0.3, R=0.6, move=0.2,
-              n_iter=10, sigma_factor=1e-10, solve_tol=1e-13):
-    """The SIMP + OC loop of topopt.run_simp, with exact (LU) filters and tight solves."""
+              n_iter=10, sigma_factor=1e-10, solve_tol=1e-13, start=None):
+    """The SIMP + OC loop of topopt.run_simp, with exact (LU) filters and tight solves.
+
+    start(i) may return a starting vector for iteration i's CG on grids too big
+    for LU; it changes the run time only (see cg_tight)."""
     K0 = canonical_stiffness(g.dx, g.dy, g.dz, nu)
     dv = helmholtz_direct(g, np.ones(g.nelem), R, quirk=False)
     x = np.asarray(x0, dtype=np.float64).copy()
@@ -403,7 +421,8 @@ def simp_loop(g: Grid, x0, f, fixed, *, nu=0.3, Emin=1e-9, E0=1.0, penal=3.0, vo
         if g.ndof <= 60000:
             u = direct_solve(g, K0, fac, f, fixed, sigma)
         else:
-            u, _, _ = cg_tight(g, K0, fac, f, fixed, sigma, tol=solve_tol)
+            u, _, _ = cg_tight(g, K0, fac, f, fixed, sigma, tol=solve_tol,
+                               x0=start(len(hist)) if start else None)
         dc, c = sensitivities(g, K0, xphys, u, Emin, E0, penal)
         dcx = helmholtz_direct(g, dc, R, quirk=False)
         hist.append(dict(compliance=c, u=u, dc=dc, xphys=xphys))

@@ -157,10 +157,16 @@ __device__ __forceinline__ void element_modal(const ModalK<T>& K, const T (&L)[4
 #ifndef HEXA_OP_TYW32
 #define HEXA_OP_TYW32 16
 #endif
+#ifndef HEXA_OP_ASYNC
+#define HEXA_OP_ASYNC 1
+#endif
+constexpr int kRingStages = 3, kRingSlots = 20;
 template <typename T>
 constexpr int op_tyw() { return sizeof(T) == 8 ? 8 : HEXA_OP_TYW32; }
 template <typename T>
 constexpr int op_min_ctas() { return sizeof(T) == 8 ? 1 : (HEXA_OP_TYW32 <= 8 ? 2 : 1); }
+template <typename T, bool MULTI>
+constexpr bool op_async() { return HEXA_OP_ASYNC && sizeof(T) == 4 && !MULTI; }
 
 // Four values of the y-exchange as one 16-byte shared-memory access per thread
 // (float4; two 16-byte halves for double).
@@ -180,13 +186,28 @@ __device__ __forceinline__ void load4(const double* p, double (&v)[4]) {
   v[0] = t0.x, v[1] = t0.y, v[2] = t1.x, v[3] = t1.y;
 }
 
+// FP32 operator loads staged through a per-thread shared-memory ring with
+// cp.async (4-byte copies, zero-filled where masked), two node layers ahead:
+// each thread copies exactly the 19 values it later reads (12 corner values,
+// its element factor, b and the previous iterate at its node), so the ring
+// needs no cross-thread synchronisation and the loads' latency is hidden
+// without the registers a deeper register prefetch would take.
+
+__device__ __forceinline__ void cp_async4(float* dst, const float* src, bool ok) {
+  const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;\n" ::"r"(d), "l"(src), "r"(ok ? 4 : 0) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait1() { asm volatile("cp.async.wait_group 1;\n" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait0() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
+
 // One work item: the node columns of tile (tx, ty) for node layers [k0, k1).
 // IX is the index type: int whenever 3 * nNodes fits, which halves the
 // integer work of the address arithmetic.
-template <typename T, int MODE, int TYW, typename IX, typename A>
+template <typename T, int MODE, int TYW, typename IX, typename A, bool ASYNC = false>
 __device__ __forceinline__ void op_item(const A& a, int tx, int ty, int chunk,
                                         T (&xch)[2][TYW][32][4],
-                                        double& acc0, long long co) {
+                                        double& acc0, long long co, float* ring = nullptr) {
   constexpr int NX_OWN = 31, NY_OWN = TYW - 1;
   constexpr bool NEED_F = (MODE == OP_JACOBI || MODE == OP_CHEB2);
   const Grid& g = a.g;
@@ -218,18 +239,74 @@ __device__ __forceinline__ void op_item(const A& a, int tx, int ty, int chunk,
   auto facload = [&](int k) -> T {
     return (colv && k >= 0 && k < g.nz) ? ldx(fac + ecol + eplane * k) : T(0);
   };
+  // ---- staged loads (ASYNC): ring slot q of node layer kk for this thread
+  constexpr int NT = 32 * TYW;
+  const int tid = lane + 32 * wy;
+  auto rslot = [&](int kk, int q) -> float* {
+    const int st = ((kk % kRingStages) + kRingStages) % kRingStages;
+    return ring + (st * kRingSlots + q) * NT + tid;
+  };
+  constexpr bool NEED_B = MODE == OP_RESID || MODE == OP_RESID_NORM || MODE == OP_JACOBI || MODE == OP_CHEB2;
+  auto issue = [&](int kk) {  // node layer kk: corners, element factor kk, b and x_prev at the own node
+    if constexpr (ASYNC) {
+      const bool kok = (kk >= 0) && (kk < g.NZ);
+      const IX lb = ca.base + ca.plane3 * (IX)kk;
+#pragma unroll
+      for (int cc = 0; cc < 4; ++cc) {
+        const bool ok = kok && ca.ok[cc];
+        const IX o = ok ? lb + ((cc & 1) ? 3 : 0) + ((cc >> 1) ? ca.row3 : (IX)0) : (IX)0;
+#pragma unroll
+        for (int c = 0; c < 3; ++c) cp_async4(rslot(kk, 3 * cc + c), (const float*)x + o + c, ok);
+      }
+      const bool fok = colv && kk >= 0 && kk < g.nz;
+      cp_async4(rslot(kk, 12), (const float*)fac + (fok ? ecol + eplane * kk : (IX)0), fok);
+      if (NEED_B) {
+        const bool bok = own && kok;
+        const IX nb3 = bok ? (IX)3 * (ncol + nplane * (IX)kk) : (IX)0;
+#pragma unroll
+        for (int c = 0; c < 3; ++c) cp_async4(rslot(kk, 13 + c), (const float*)bv + nb3 + c, bok);
+        if (MODE == OP_CHEB2) {
+          const bool pok = bok && xinv;
+#pragma unroll
+          for (int c = 0; c < 3; ++c) cp_async4(rslot(kk, 16 + c), pok ? (const float*)xinv + nb3 + c : (const float*)x, pok);
+        }
+      }
+      cp_async_commit();
+    }
+  };
+  auto corners = [&](int kk, T (&v)[4][3]) {
+    if constexpr (ASYNC) {
+#pragma unroll
+      for (int cc = 0; cc < 4; ++cc)
+#pragma unroll
+        for (int c = 0; c < 3; ++c) v[cc][c] = *rslot(kk, 3 * cc + c);
+    } else {
+      load_corners<T, IX>(g, ca, x, kk, v);
+    }
+  };
+  auto facval = [&](int kk) -> T {
+    if constexpr (ASYNC) return *rslot(kk, 12);
+    else return facload(kk);
+  };
+
   T Lm[4][3], carry[4][3], xown[3];
   T fprev;
+  if constexpr (ASYNC) {
+    issue(k0 - 1);
+    issue(k0);
+    issue(k0 + 1);
+    cp_async_wait1();  // layers k0-1 and k0 have landed
+  }
   {
     T raw[4][3];
-    load_corners<T, IX>(g, ca, x, k0 - 1, raw);
+    corners(k0 - 1, raw);
     T Lprev[4][3];
     xy_forward<T>(raw, Lprev);
-    load_corners<T, IX>(g, ca, x, k0, raw);
+    corners(k0, raw);
 #pragma unroll
     for (int c = 0; c < 3; ++c) xown[c] = raw[3][c];
     xy_forward<T>(raw, Lm);
-    fprev = facload(k0 - 1);
+    fprev = facval(k0 - 1);
     T lo[4][3];
     element_modal<T>(a.K, Lprev, Lm, fprev, lo, carry);
   }
@@ -239,20 +316,32 @@ __device__ __forceinline__ void op_item(const A& a, int tx, int ty, int chunk,
   // FP64 arithmetic in the FP32 kernels would run at GB300's FP64 rate
   T accT = T(0);
   T nraw[4][3];
-  load_corners<T, IX>(g, ca, x, k0 + 1, nraw);
-  T fnext = facload(k0);
+  T fnext = T(0);
+  if constexpr (!ASYNC) {
+    load_corners<T, IX>(g, ca, x, k0 + 1, nraw);
+    fnext = facload(k0);
+  }
 
 #pragma unroll 2
   for (int k = k0; k < k1; ++k) {
     T raw[4][3];
+    T f;
+    if constexpr (ASYNC) {
+      if (k + 2 <= k1) issue(k + 2);  // into the slot layer k-1 used
+      else cp_async_commit();          // empty group keeps the wait count uniform
+      cp_async_wait1();                // layers k and k+1 have landed
+      corners(k + 1, raw);
+      f = facval(k);
+    } else {
 #pragma unroll
-    for (int cc = 0; cc < 4; ++cc)
+      for (int cc = 0; cc < 4; ++cc)
 #pragma unroll
-      for (int c = 0; c < 3; ++c) raw[cc][c] = nraw[cc][c];
-    const T f = fnext;
-    if (k + 1 < k1) {  // prefetch the next layer
-      load_corners<T, IX>(g, ca, x, k + 2, nraw);
-      fnext = facload(k + 1);
+        for (int c = 0; c < 3; ++c) raw[cc][c] = nraw[cc][c];
+      f = fnext;
+      if (k + 1 < k1) {  // prefetch the next layer
+        load_corners<T, IX>(g, ca, x, k + 2, nraw);
+        fnext = facload(k + 1);
+      }
     }
     T Um[4][3];
     xy_forward<T>(raw, Um);
@@ -316,14 +405,18 @@ __device__ __forceinline__ void op_item(const A& a, int tx, int ty, int chunk,
           out = fixd ? T(0) : Ax;
           accT = fma(xown[c], out, accT);
         } else if (MODE == OP_RESID || MODE == OP_RESID_NORM) {
-          out = fixd ? T(0) : (ldx(bv + 3 * n + c) - Ax);
+          const T bvc = ASYNC ? (T)*rslot(k, 13 + c) : ldx(bv + 3 * n + c);
+          out = fixd ? T(0) : (bvc - Ax);
           if (MODE == OP_RESID_NORM) accT = fma(out, out, accT);
         } else if (MODE == OP_JACOBI) {  // x + omega (b - Ax) / D
-          out = fixd ? T(0) : fma(a.omega * dinv[c], ldx(bv + 3 * n + c) - Ax, xown[c]);
+          const T bvc = ASYNC ? (T)*rslot(k, 13 + c) : ldx(bv + 3 * n + c);
+          out = fixd ? T(0) : fma(a.omega * dinv[c], bvc - Ax, xown[c]);
         } else {  // OP_CHEB2: x + c1 (x - x_prev) + c2 D^-1 (b - Ax)
-          const T xp = xinv ? xinv[3 * n + c] : T(0);  // plain load: y may alias xin
+          // plain load: y may alias xin (the staged copy was taken before this thread's write)
+          const T xp = ASYNC ? (T)*rslot(k, 16 + c) : (xinv ? xinv[3 * n + c] : T(0));
+          const T bvc = ASYNC ? (T)*rslot(k, 13 + c) : ldx(bv + 3 * n + c);
           const T t = fma(a.c1, xown[c] - xp, xown[c]);
-          out = fixd ? T(0) : fma(a.c2 * dinv[c], ldx(bv + 3 * n + c) - Ax, t);
+          out = fixd ? T(0) : fma(a.c2 * dinv[c], bvc - Ax, t);
         }
         yv[3 * n + c] = out;
       }
@@ -333,6 +426,7 @@ __device__ __forceinline__ void op_item(const A& a, int tx, int ty, int chunk,
   }
 
   acc0 += (double)accT;
+  if constexpr (ASYNC) cp_async_wait0();
   __syncthreads();  // the next item reuses xch
 }
 
@@ -340,6 +434,7 @@ template <typename T, int MODE, int TYW, typename IX, bool MULTI>
 __global__ void __launch_bounds__(32 * TYW, op_min_ctas<T>()) op_kernel(const OpArgs<T> a) {
   if (a.halt && *((volatile const int*)a.halt)) return;
   __shared__ __align__(16) T xch[2][TYW][32][4];
+  extern __shared__ __align__(16) float op_ring[];  // staged loads (FP32 single-column forms)
   double acc0 = 0.0;
   // static stride over (tile x, tile y, z-chunk) items: deterministic, and
   // with the grid sized to the resident CTAs no wave is left half empty
@@ -351,7 +446,7 @@ __global__ void __launch_bounds__(32 * TYW, op_min_ctas<T>()) op_kernel(const Op
     if (MULTI) {  // every column of a multi-column apply reuses the item's factors from L1
       for (int col = 0; col < a.ncol; ++col) op_item<T, MODE, TYW, IX>(a, tx, ty, chunk, xch, acc0, col * a.g.ndof());
     } else {
-      op_item<T, MODE, TYW, IX>(a, tx, ty, chunk, xch, acc0, 0);
+      op_item<T, MODE, TYW, IX, OpArgs<T>, op_async<T, MULTI>()>(a, tx, ty, chunk, xch, acc0, 0, op_ring);
     }
   }
   if (MODE == OP_APPLY_DOT || MODE == OP_RESID_NORM) {
@@ -371,6 +466,24 @@ static ModalK<T> cast_modal(const ModalK<double>& K) {
 }
 
 
+// Dynamic shared memory of the staged-load ring (0 for the direct forms).
+template <typename T, bool MULTI>
+constexpr int op_ring_bytes() {
+  return op_async<T, MULTI>() ? kRingStages * kRingSlots * 32 * op_tyw<T>() * (int)sizeof(float) : 0;
+}
+
+// Raises the kernel's dynamic shared-memory limit to the ring size, once.
+template <typename T, int MODE, typename IX, bool MULTI>
+static void op_prepare() {
+  static bool done = false;
+  if (!done) {
+    if (op_ring_bytes<T, MULTI>() > 0)
+      cudaFuncSetAttribute(op_kernel<T, MODE, op_tyw<T>(), IX, MULTI>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           op_ring_bytes<T, MULTI>());
+    done = true;
+  }
+}
+
 template <typename T, int MODE>
 static int op_resident_ctas() {
   static int cached = 0;
@@ -378,7 +491,9 @@ static int op_resident_ctas() {
     int dev = 0, sms = 0, occ = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, op_kernel<T, MODE, op_tyw<T>(), long long, false>, 32 * op_tyw<T>(), 0);
+    op_prepare<T, MODE, long long, false>();
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, op_kernel<T, MODE, op_tyw<T>(), long long, false>,
+                                                  32 * op_tyw<T>(), op_ring_bytes<T, false>());
     cached = std::max(1, sms) * std::max(1, occ);
   }
   return cached;
@@ -442,10 +557,15 @@ void launch_op(int mode, const OpArgs<T>& a0, cudaStream_t st) {
     }
     return;
   }
-#define HEXA_OP_CASE(M)                                                              \
-  case M:                                                                           \
-    if (i32) op_kernel<T, M, TYW, int, false><<<grid, block, 0, st>>>(a);           \
-    else op_kernel<T, M, TYW, long long, false><<<grid, block, 0, st>>>(a);         \
+#define HEXA_OP_CASE(M)                                                                      \
+  case M:                                                                                   \
+    if (i32) {                                                                              \
+      op_prepare<T, M, int, false>();                                                       \
+      op_kernel<T, M, TYW, int, false><<<grid, block, op_ring_bytes<T, false>(), st>>>(a);  \
+    } else {                                                                                \
+      op_prepare<T, M, long long, false>();                                                 \
+      op_kernel<T, M, TYW, long long, false><<<grid, block, op_ring_bytes<T, false>(), st>>>(a); \
+    }                                                                                       \
     break;
   switch (mode) {
     HEXA_OP_CASE(OP_APPLY)
