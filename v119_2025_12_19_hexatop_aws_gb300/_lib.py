@@ -44,7 +44,7 @@ class SolveParams(C.Structure):
         ("shift_factor", C.c_double), ("stagnation_tol", C.c_double), ("max_shift_attempts", C.c_int32),
         ("shift_multiplier", C.c_double), ("check_cadence", C.c_int32), ("diag_quirk", C.c_int32),
         ("precision", C.c_int32), ("mg_levels", C.c_int32), ("pre_smooth", C.c_int32), ("post_smooth", C.c_int32),
-        ("smoother", C.c_int32), ("jacobi_omega", C.c_double), ("cheb_degree", C.c_int32),
+        ("smoother", C.c_int32), ("jacobi_omega", C.c_double), ("cheb_ratio", C.c_int32),
         ("coarse_iters", C.c_int32), ("inner_tol", C.c_double), ("max_outer", C.c_int32),
         ("use_graphs", C.c_int32), ("graph_iters", C.c_int32), ("true_residual", C.c_int32),
         ("divergence_check", C.c_int32), ("autotune", C.c_int32),

@@ -441,7 +441,7 @@ int batch_problem(Ctx& c, int count, const hexa_grid* grids, const hexa_bc* bcs,
     mg.nu2 = prm.post_smooth >= 0 ? prm.post_smooth : 2;
     mg.citers = prm.coarse_iters >= 0 ? prm.coarse_iters : 30;
     const int nmax = std::max(mg.nu1, mg.nu2) + 1;
-    const double lmin = lmax / 30.0, th = 0.5 * (lmax + lmin), de = 0.5 * (lmax - lmin), sg = th / de;
+    const double lmin = lmax / (prm.cheb_ratio > 1 ? prm.cheb_ratio : 30.0), th = 0.5 * (lmax + lmin), de = 0.5 * (lmax - lmin), sg = th / de;
     double rho = 1.0 / sg;
     mg.inv_theta = (T)(1.0 / th);
     mg.c1.assign(nmax + 1, T(0));

@@ -60,13 +60,10 @@ void launch_coarsen_mask(const Grid& gf, const uint8_t* mf, const Grid& gc, uint
 }
 
 template <typename T>
-__device__ __forceinline__ void restrict_body(const Grid& gf, const T* __restrict__ rf, const Grid& gc, const Mask& mc,
-                                              T* __restrict__ bc, long long first, long long stride) {
-  const long long nn = gc.nnode();
-  for (long long n = first; n < nn; n += stride) {
-    const int I = (int)(n % gc.NX);
-    const long long t = n / gc.NX;
-    const int J = (int)(t % gc.NY), K = (int)(t / gc.NY);
+__device__ __forceinline__ void restrict_node(const Grid& gf, const T* __restrict__ rf, const Grid& gc, const Mask& mc,
+                                              T* __restrict__ bc, int I, int J, int K) {
+  {
+    const long long n = (long long)I + (long long)gc.NX * ((long long)J + (long long)gc.NY * K);
     const unsigned fx = fixed_bits(gc, mc, I, J, K, n);
     T s0 = T(0), s1 = T(0), s2 = T(0);
     if (fx != 7u) {
@@ -98,28 +95,40 @@ __device__ __forceinline__ void restrict_body(const Grid& gf, const T* __restric
   }
 }
 template <typename T>
+__device__ __forceinline__ void restrict_body(const Grid& gf, const T* __restrict__ rf, const Grid& gc, const Mask& mc,
+                                              T* __restrict__ bc, long long first, long long stride) {
+  const long long nn = gc.nnode();
+  for (long long n = first; n < nn; n += stride) {
+    const int I = (int)(n % gc.NX);
+    const long long t = n / gc.NX;
+    restrict_node<T>(gf, rf, gc, mc, bc, I, (int)(t % gc.NY), (int)(t / gc.NY));
+  }
+}
+// Single-grid launches index nodes in 3D (block (32, 4), grid (x, y, z) over
+// (I, J, K)): no integer division per node.
+static inline dim3 node_grid3(const Grid& g) {
+  return dim3((unsigned)((g.NX + 31) / 32), (unsigned)((g.NY + 3) / 4), (unsigned)g.NZ);
+}
+template <typename T>
 __global__ void restrict_kernel(Grid gf, const T* __restrict__ rf, Grid gc, Mask mc, T* __restrict__ bc,
                                 const int* halt) {
   if (halt && *((volatile const int*)halt)) return;
-  restrict_body<T>(gf, rf, gc, mc, bc, blockIdx.x * (long long)blockDim.x + threadIdx.x,
-                   (long long)gridDim.x * blockDim.x);
+  const int I = blockIdx.x * 32 + threadIdx.x, J = blockIdx.y * 4 + threadIdx.y, K = blockIdx.z;
+  if (I < gc.NX && J < gc.NY) restrict_node<T>(gf, rf, gc, mc, bc, I, J, K);
 }
 template <typename T>
 void launch_restrict(const Grid& gf, const T* rf, const Grid& gc, const Mask& mc, T* bc, const int* halt,
                      cudaStream_t st) {
-  restrict_kernel<T><<<mg_blocks(gc.nnode()), 256, 0, st>>>(gf, rf, gc, mc, bc, halt);
+  restrict_kernel<T><<<node_grid3(gc), dim3(32, 4), 0, st>>>(gf, rf, gc, mc, bc, halt);
 }
 
 template <typename T>
-__device__ __forceinline__ void prolong_add_body(const Grid& gc, const T* __restrict__ xc, const Grid& gf,
-                                                 const Mask& mf, T* __restrict__ xf, long long first, long long stride) {
-  const long long nn = gf.nnode();
-  for (long long n = first; n < nn; n += stride) {
-    const int i = (int)(n % gf.NX);
-    const long long t = n / gf.NX;
-    const int j = (int)(t % gf.NY), k = (int)(t / gf.NY);
+__device__ __forceinline__ void prolong_add_node(const Grid& gc, const T* __restrict__ xc, const Grid& gf,
+                                                 const Mask& mf, T* __restrict__ xf, int i, int j, int k) {
+  {
+    const long long n = (long long)i + (long long)gf.NX * ((long long)j + (long long)gf.NY * k);
     const unsigned fx = fixed_bits(gf, mf, i, j, k, n);
-    if (fx == 7u) continue;
+    if (fx == 7u) return;
     const int I0 = i >> 1, J0 = j >> 1, K0 = k >> 1;
     const int ni = (i & 1) ? 2 : 1, nj = (j & 1) ? 2 : 1, nk = (k & 1) ? 2 : 1;
     const T wi = (i & 1) ? T(0.5) : T(1), wj = (j & 1) ? T(0.5) : T(1), wk = (k & 1) ? T(0.5) : T(1);
@@ -139,28 +148,34 @@ __device__ __forceinline__ void prolong_add_body(const Grid& gc, const T* __rest
   }
 }
 template <typename T>
+__device__ __forceinline__ void prolong_add_body(const Grid& gc, const T* __restrict__ xc, const Grid& gf,
+                                                 const Mask& mf, T* __restrict__ xf, long long first, long long stride) {
+  const long long nn = gf.nnode();
+  for (long long n = first; n < nn; n += stride) {
+    const int i = (int)(n % gf.NX);
+    const long long t = n / gf.NX;
+    prolong_add_node<T>(gc, xc, gf, mf, xf, i, (int)(t % gf.NY), (int)(t / gf.NY));
+  }
+}
+template <typename T>
 __global__ void prolong_add_kernel(Grid gc, const T* __restrict__ xc, Grid gf, Mask mf, T* __restrict__ xf,
                                    const int* halt) {
   if (halt && *((volatile const int*)halt)) return;
-  prolong_add_body<T>(gc, xc, gf, mf, xf, blockIdx.x * (long long)blockDim.x + threadIdx.x,
-                      (long long)gridDim.x * blockDim.x);
+  const int i = blockIdx.x * 32 + threadIdx.x, j = blockIdx.y * 4 + threadIdx.y, k = blockIdx.z;
+  if (i < gf.NX && j < gf.NY) prolong_add_node<T>(gc, xc, gf, mf, xf, i, j, k);
 }
 template <typename T>
 void launch_prolong_add(const Grid& gc, const T* xc, const Grid& gf, const Mask& mf, T* xf, const int* halt,
                         cudaStream_t st) {
-  prolong_add_kernel<T><<<mg_blocks(gf.nnode()), 256, 0, st>>>(gc, xc, gf, mf, xf, halt);
+  prolong_add_kernel<T><<<node_grid3(gf), dim3(32, 4), 0, st>>>(gc, xc, gf, mf, xf, halt);
 }
 
 template <typename T>
-__device__ __forceinline__ void jacobi0_body(const Grid& g, const Mask& m, const T* __restrict__ fac,
+__device__ __forceinline__ void jacobi0_node(const Grid& g, const Mask& m, const T* __restrict__ fac,
                                              const ModalK<T>& K, int quirk, T sigma, T omega,
-                                             const T* __restrict__ b, T* __restrict__ x, long long first,
-                                             long long stride) {
-  const long long nn = g.nnode();
-  for (long long n = first; n < nn; n += stride) {
-    const int i = (int)(n % g.NX);
-    const long long t = n / g.NX;
-    const int j = (int)(t % g.NY), k = (int)(t / g.NY);
+                                             const T* __restrict__ b, T* __restrict__ x, int i, int j, int k) {
+  {
+    const long long n = (long long)i + (long long)g.NX * ((long long)j + (long long)g.NY * k);
     const unsigned fx = fixed_bits(g, m, i, j, k, n);
     T fs = T(0);
 #pragma unroll
@@ -181,16 +196,28 @@ __device__ __forceinline__ void jacobi0_body(const Grid& g, const Mask& m, const
   }
 }
 template <typename T>
+__device__ __forceinline__ void jacobi0_body(const Grid& g, const Mask& m, const T* __restrict__ fac,
+                                             const ModalK<T>& K, int quirk, T sigma, T omega,
+                                             const T* __restrict__ b, T* __restrict__ x, long long first,
+                                             long long stride) {
+  const long long nn = g.nnode();
+  for (long long n = first; n < nn; n += stride) {
+    const int i = (int)(n % g.NX);
+    const long long t = n / g.NX;
+    jacobi0_node<T>(g, m, fac, K, quirk, sigma, omega, b, x, i, (int)(t % g.NY), (int)(t / g.NY));
+  }
+}
+template <typename T>
 __global__ void jacobi0_kernel(Grid g, Mask m, const T* __restrict__ fac, ModalK<T> K, int quirk, T sigma,
                                T omega, const T* __restrict__ b, T* __restrict__ x, const int* halt) {
   if (halt && *((volatile const int*)halt)) return;
-  jacobi0_body<T>(g, m, fac, K, quirk, sigma, omega, b, x, blockIdx.x * (long long)blockDim.x + threadIdx.x,
-                  (long long)gridDim.x * blockDim.x);
+  const int i = blockIdx.x * 32 + threadIdx.x, j = blockIdx.y * 4 + threadIdx.y, k = blockIdx.z;
+  if (i < g.NX && j < g.NY) jacobi0_node<T>(g, m, fac, K, quirk, sigma, omega, b, x, i, j, k);
 }
 template <typename T>
 void launch_jacobi0(const Grid& g, const Mask& m, const T* fac, const ModalK<T>& K, int quirk, T sigma, T omega,
                     const T* b, T* x, const int* halt, cudaStream_t st) {
-  jacobi0_kernel<T><<<mg_blocks(g.nnode()), 256, 0, st>>>(g, m, fac, K, quirk, sigma, omega, b, x, halt);
+  jacobi0_kernel<T><<<node_grid3(g), dim3(32, 4), 0, st>>>(g, m, fac, K, quirk, sigma, omega, b, x, halt);
 }
 
 // ---------------------------------------------------------------------------

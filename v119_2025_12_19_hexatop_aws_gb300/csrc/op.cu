@@ -158,13 +158,16 @@ __device__ __forceinline__ void element_modal(const ModalK<T>& K, const T (&L)[4
 #define HEXA_OP_TYW32 16
 #endif
 #ifndef HEXA_OP_ASYNC
-#define HEXA_OP_ASYNC 1
+#define HEXA_OP_ASYNC 0
 #endif
 constexpr int kRingStages = 3, kRingSlots = 20;
 template <typename T>
 constexpr int op_tyw() { return sizeof(T) == 8 ? 8 : HEXA_OP_TYW32; }
+#ifndef HEXA_OP_MINCTAS32
+#define HEXA_OP_MINCTAS32 (HEXA_OP_TYW32 <= 8 ? 2 : 1)
+#endif
 template <typename T>
-constexpr int op_min_ctas() { return sizeof(T) == 8 ? 1 : (HEXA_OP_TYW32 <= 8 ? 2 : 1); }
+constexpr int op_min_ctas() { return sizeof(T) == 8 ? 1 : HEXA_OP_MINCTAS32; }
 template <typename T, bool MULTI>
 constexpr bool op_async() { return HEXA_OP_ASYNC && sizeof(T) == 4 && !MULTI; }
 

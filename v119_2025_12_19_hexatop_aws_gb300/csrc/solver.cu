@@ -140,14 +140,14 @@ struct MG {
   T omega = T(0.6);
   int nu1 = 2, nu2 = 2, citers = 30;
   int smoother = HEXA_SMOOTH_CHEBYSHEV;
-  // Chebyshev on [lmax/30, lmax] of D^-1 A: d_0 = D^-1 r / theta,
+  // Chebyshev on [lmax/ratio, lmax] of D^-1 A (ratio 30 by default): d_0 = D^-1 r / theta,
   // d_s = c1[s] d_{s-1} + c2[s] D^-1 r_s
   T inv_theta = T(0);
   std::vector<T> c1, c2;
   std::vector<double> ke;  // FP64 K0 of the fine element (dense coarse inverse)
 
-  void set_chebyshev(double lmax, int nmax) {
-    const double lmin = lmax / 30.0, th = 0.5 * (lmax + lmin), de = 0.5 * (lmax - lmin), sg = th / de;
+  void set_chebyshev(double lmax, int nmax, double ratio) {
+    const double lmin = lmax / ratio, th = 0.5 * (lmax + lmin), de = 0.5 * (lmax - lmin), sg = th / de;
     double rho = 1.0 / sg;
     inv_theta = (T)(1.0 / th);
     c1.assign(nmax + 1, T(0));
@@ -722,7 +722,7 @@ void configure_mg(MG<T>& mg, const Problem& P, const hexa_solve_params& prm) {
   mg.nu1 = prm.pre_smooth > 0 ? prm.pre_smooth : 1;
   mg.nu2 = prm.post_smooth >= 0 ? prm.post_smooth : 2;
   mg.citers = prm.coarse_iters >= 0 ? prm.coarse_iters : 30;
-  mg.set_chebyshev(lmax, std::max(mg.nu1, mg.nu2) + 1);
+  mg.set_chebyshev(lmax, std::max(mg.nu1, mg.nu2) + 1, prm.cheb_ratio > 1 ? prm.cheb_ratio : 30.0);
   mg.ke.assign(576, 0.0);
   if (canonical_stiffness(P.dx, P.dy, P.dz, P.nu, mg.ke.data()) != 0) mg.ke.clear();
 }

@@ -10,6 +10,8 @@
 // iteration.
 #include <algorithm>
 #include <cmath>
+#include <cstdint>
+#include <initializer_list>
 
 #include "hexa_common.cuh"
 #include "hexa_kernels.h"
@@ -35,6 +37,36 @@ __device__ __forceinline__ void flush_parts(double (&acc)[NS], T (&part)[NS], in
     part[q] = T(0);
   }
   cnt = 0;
+}
+
+// 16-byte vector access of the PCG passes: W elements per load/store.
+template <typename T>
+struct V16;
+template <>
+struct V16<float> {
+  using V = float4;
+  static constexpr int W = 4;
+};
+template <>
+struct V16<double> {
+  using V = double2;
+  static constexpr int W = 2;
+};
+template <typename T>
+__device__ __forceinline__ void ldv(const T* p, long long i, T (&a)[V16<T>::W]) {
+  *reinterpret_cast<typename V16<T>::V*>(a) = reinterpret_cast<const typename V16<T>::V*>(p)[i];
+}
+template <typename T>
+__device__ __forceinline__ void stv(T* p, long long i, const T (&a)[V16<T>::W]) {
+  reinterpret_cast<typename V16<T>::V*>(p)[i] = *reinterpret_cast<const typename V16<T>::V*>(a);
+}
+// Whether the column bases stay 16-byte aligned: all pointers aligned and
+// (one column, or a column length that keeps later columns aligned).
+template <typename T>
+static bool vec_ok(long long n, int ncol, std::initializer_list<const void*> ptrs) {
+  for (const void* q : ptrs)
+    if (q && (reinterpret_cast<uintptr_t>(q) & 15u)) return false;
+  return ncol <= 1 || (n % V16<T>::W) == 0;
 }
 
 template <typename T>
@@ -193,7 +225,7 @@ static inline int col_blocks(int nblocks, int ncol) {
   return per * nc;
 }
 
-template <typename T, int NS>
+template <typename T, int NS, bool VEC>
 __global__ void dot_kernel(const T* __restrict__ a, const T* __restrict__ b, const T* __restrict__ c,
                            const T* __restrict__ d, long long n, RedArgs red, const int* halt) {
   const ColMap cm = colmap(red.ncol);
@@ -204,7 +236,25 @@ __global__ void dot_kernel(const T* __restrict__ a, const T* __restrict__ b, con
 #pragma unroll
   for (int q = 0; q < NS; ++q) acc[q] = 0.0, part[q] = T(0);
   int cnt = 0;
-  for (long long i = cm.first; i < n; i += cm.stride) {
+  long long tail = 0;
+  if (VEC) {
+    constexpr int W = V16<T>::W;
+    const long long nv = n / W;
+    tail = nv * W;
+    for (long long i = cm.first; i < nv; i += cm.stride) {
+      T av[W], bv[W], cv[W], dv[W];
+      ldv(a + off, i, av);
+      ldv(b + off, i, bv);
+      if (NS > 1) ldv(c + off, i, cv), ldv(d + off, i, dv);
+#pragma unroll
+      for (int w = 0; w < W; ++w) {
+        part[0] = fma(av[w], bv[w], part[0]);
+        if (NS > 1) part[NS - 1] = fma(cv[w], dv[w], part[NS - 1]);
+      }
+      if ((cnt += W) >= kChunk) flush_parts<T, NS>(acc, part, cnt);
+    }
+  }
+  for (long long i = tail + cm.first; i < n; i += cm.stride) {
     part[0] = fma(a[off + i], b[off + i], part[0]);
     if (NS > 1) part[NS - 1] = fma(c[off + i], d[off + i], part[NS - 1]);
     if (++cnt == kChunk) flush_parts<T, NS>(acc, part, cnt);
@@ -216,11 +266,17 @@ template <typename T>
 void launch_dot(const T* a, const T* b, const T* c, const T* d, long long n, const RedArgs& red,
                 int nblocks, const int* halt, cudaStream_t st) {
   const int g = col_blocks(nblocks, red.ncol);
-  if (c) dot_kernel<T, 2><<<g, 256, 0, st>>>(a, b, c, d, n, red, halt);
-  else dot_kernel<T, 1><<<g, 256, 0, st>>>(a, b, c, d, n, red, halt);
+  const bool v = vec_ok<T>(n, red.ncol, {a, b, c, d});
+  if (c) {
+    if (v) dot_kernel<T, 2, true><<<g, 256, 0, st>>>(a, b, c, d, n, red, halt);
+    else dot_kernel<T, 2, false><<<g, 256, 0, st>>>(a, b, c, d, n, red, halt);
+  } else {
+    if (v) dot_kernel<T, 1, true><<<g, 256, 0, st>>>(a, b, c, d, n, red, halt);
+    else dot_kernel<T, 1, false><<<g, 256, 0, st>>>(a, b, c, d, n, red, halt);
+  }
 }
 
-template <typename T, bool JAC>
+template <typename T, bool JAC, bool VEC>
 __global__ void pcg_update_kernel(T* __restrict__ x, T* __restrict__ r, T* __restrict__ z,
                                   const T* __restrict__ p, const T* __restrict__ q,
                                   const T* __restrict__ dinv, long long n, RedArgs red,
@@ -235,7 +291,35 @@ __global__ void pcg_update_kernel(T* __restrict__ x, T* __restrict__ r, T* __res
 #pragma unroll
   for (int q2 = 0; q2 < NS; ++q2) acc[q2] = 0.0, part[q2] = T(0);
   int cnt = 0;
-  for (long long i = cm.first; i < n; i += cm.stride) {
+  long long tail = 0;
+  if (VEC) {
+    constexpr int W = V16<T>::W;
+    const long long nv = n / W;
+    tail = nv * W;
+    for (long long i = cm.first; i < nv; i += cm.stride) {
+      T xv[W], rv[W], pv[W], qv[W], dv[W], zv[W];
+      ldv(x + off, i, xv);
+      ldv(r + off, i, rv);
+      ldv(p + off, i, pv);
+      ldv(q + off, i, qv);
+      if (JAC) ldv(dinv, i, dv);
+#pragma unroll
+      for (int w = 0; w < W; ++w) {
+        xv[w] = fma(alpha, pv[w], xv[w]);
+        rv[w] = fma(-alpha, qv[w], rv[w]);
+        part[0] = fma(rv[w], rv[w], part[0]);
+        if (JAC) {
+          zv[w] = rv[w] * dv[w];
+          part[NS - 1] = fma(rv[w], zv[w], part[NS - 1]);
+        }
+      }
+      stv(x + off, i, xv);
+      stv(r + off, i, rv);
+      if (JAC) stv(z + off, i, zv);
+      if ((cnt += W) >= kChunk) flush_parts<T, NS>(acc, part, cnt);
+    }
+  }
+  for (long long i = tail + cm.first; i < n; i += cm.stride) {
     const long long k = off + i;
     x[k] = fma(alpha, p[k], x[k]);
     const T ri = fma(-alpha, q[k], r[k]);
@@ -255,22 +339,43 @@ template <typename T>
 void launch_pcg_update(T* x, T* r, T* z, const T* p, const T* q, const T* dinv, long long n,
                        const RedArgs& red, int nblocks, const PcgScalars* s, cudaStream_t st) {
   const int g = col_blocks(nblocks, red.ncol);
-  if (dinv) pcg_update_kernel<T, true><<<g, 256, 0, st>>>(x, r, z, p, q, dinv, n, red, s);
-  else pcg_update_kernel<T, false><<<g, 256, 0, st>>>(x, r, z, p, q, dinv, n, red, s);
+  const bool v = vec_ok<T>(n, red.ncol, {x, r, z, p, q, dinv}) && (red.ncol <= 1 || !dinv);
+  if (dinv) {
+    if (v) pcg_update_kernel<T, true, true><<<g, 256, 0, st>>>(x, r, z, p, q, dinv, n, red, s);
+    else pcg_update_kernel<T, true, false><<<g, 256, 0, st>>>(x, r, z, p, q, dinv, n, red, s);
+  } else {
+    if (v) pcg_update_kernel<T, false, true><<<g, 256, 0, st>>>(x, r, z, p, q, dinv, n, red, s);
+    else pcg_update_kernel<T, false, false><<<g, 256, 0, st>>>(x, r, z, p, q, dinv, n, red, s);
+  }
 }
 
-template <typename T>
+template <typename T, bool VEC>
 __global__ void p_update_kernel(T* __restrict__ p, const T* __restrict__ z, long long n,
                                 const PcgScalars* s, int ncol) {
   const ColMap cm = colmap(ncol);
   if (*((volatile const int*)&s[cm.col].halt)) return;
   const T beta = (T)s[cm.col].beta;
   const long long off = (long long)cm.col * n;
-  for (long long i = cm.first; i < n; i += cm.stride) p[off + i] = fma(beta, p[off + i], z[off + i]);
+  long long tail = 0;
+  if (VEC) {
+    constexpr int W = V16<T>::W;
+    const long long nv = n / W;
+    tail = nv * W;
+    for (long long i = cm.first; i < nv; i += cm.stride) {
+      T pv[W], zv[W];
+      ldv(p + off, i, pv);
+      ldv(z + off, i, zv);
+#pragma unroll
+      for (int w = 0; w < W; ++w) pv[w] = fma(beta, pv[w], zv[w]);
+      stv(p + off, i, pv);
+    }
+  }
+  for (long long i = tail + cm.first; i < n; i += cm.stride) p[off + i] = fma(beta, p[off + i], z[off + i]);
 }
 template <typename T>
 void launch_p_update(T* p, const T* z, long long n, const PcgScalars* s, cudaStream_t st, int ncol) {
-  p_update_kernel<T><<<col_blocks(vec_blocks(n), ncol), 256, 0, st>>>(p, z, n, s, ncol);
+  if (vec_ok<T>(n, ncol, {p, z})) p_update_kernel<T, true><<<col_blocks(vec_blocks(n), ncol), 256, 0, st>>>(p, z, n, s, ncol);
+  else p_update_kernel<T, false><<<col_blocks(vec_blocks(n), ncol), 256, 0, st>>>(p, z, n, s, ncol);
 }
 
 template <typename T>
