@@ -82,7 +82,7 @@ typedef struct hexa_solve_params {
   int32_t pre_smooth, post_smooth;
   int32_t smoother;           /* HEXA_SMOOTH_* */
   double jacobi_omega;
-  int32_t cheb_ratio;         /* Chebyshev smoothing interval [lmax/cheb_ratio, lmax] of D^-1 A (30) */
+  int32_t cheb_ratio;         /* Chebyshev smoothing interval [lmax/cheb_ratio, lmax] of D^-1 A (10) */
   int32_t coarse_iters;       /* Jacobi-PCG iterations of the coarsest-level solve when that grid
                                  has more than 640 DOFs (smaller ones are solved exactly, by the
                                  dense inverse of their operator) */

@@ -441,7 +441,7 @@ int batch_problem(Ctx& c, int count, const hexa_grid* grids, const hexa_bc* bcs,
     mg.nu2 = prm.post_smooth >= 0 ? prm.post_smooth : 2;
     mg.citers = prm.coarse_iters >= 0 ? prm.coarse_iters : 30;
     const int nmax = std::max(mg.nu1, mg.nu2) + 1;
-    const double lmin = lmax / (prm.cheb_ratio > 1 ? prm.cheb_ratio : 30.0), th = 0.5 * (lmax + lmin), de = 0.5 * (lmax - lmin), sg = th / de;
+    const double lmin = lmax / (prm.cheb_ratio > 1 ? prm.cheb_ratio : 10.0), th = 0.5 * (lmax + lmin), de = 0.5 * (lmax - lmin), sg = th / de;
     double rho = 1.0 / sg;
     mg.inv_theta = (T)(1.0 / th);
     mg.c1.assign(nmax + 1, T(0));
@@ -460,7 +460,7 @@ int batch_problem(Ctx& c, int count, const hexa_grid* grids, const hexa_bc* bcs,
   bool tuned = false;
   if (prm.autotune) {
     auto it = c.tuned.find(tkey);
-    if (it != c.tuned.end()) kchunk = it->second.first, tuned = true;
+    if (it != c.tuned.end()) kchunk = it->second.a, tuned = true;
   }
   if (!build_batch_mg<T>(c, mg, g0, faces, sigma, nlev, fac32, kchunk)) return HEXA_ERR_NOMEM;
   if (prm.autotune && !tuned && mg.L[0].smooth.n()) {
@@ -488,7 +488,7 @@ int batch_problem(Ctx& c, int count, const hexa_grid* grids, const hexa_bc* bcs,
       c.launches += 6;
       if (ms < best) best = ms, bestk = kc;
     }
-    c.tuned[tkey] = {bestk, 0};
+    c.tuned[tkey] = {bestk, 0, 0};
     kchunk = bestk;
     if (!build_batch_mg<T>(c, mg, g0, faces, sigma, nlev, fac32, kchunk)) return HEXA_ERR_NOMEM;
   }

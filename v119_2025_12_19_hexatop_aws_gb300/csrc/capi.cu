@@ -140,7 +140,7 @@ void hexa_default_params(hexa_solve_params* p) {
   p->post_smooth = 2;
   p->smoother = HEXA_SMOOTH_CHEBYSHEV;
   p->jacobi_omega = 0.0;        // 0: 1.2 / (element bound on lambda_max(D^-1 A))
-  p->cheb_ratio = 30;
+  p->cheb_ratio = 10;
   p->coarse_iters = 30;
   p->inner_tol = 1e-4;
   p->max_outer = 20;

@@ -115,6 +115,64 @@ __device__ __forceinline__ void xy_inverse(const T (&m)[4][3], T (&v)[4][3]) {
   }
 }
 
+// FP32 forms with the (x, y) components packed in a float2, so that the
+// butterflies and the z stage run as Blackwell's two-lane FP32 instructions
+// (FADD2/FFMA2: one issue slot for two operations); z stays scalar.
+#ifndef HEXA_OP_PACKED
+#define HEXA_OP_PACKED 1
+#endif
+__device__ __forceinline__ float2 pk(float a, float b) { return make_float2(a, b); }
+__device__ __forceinline__ float2 pk_add(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 pk_sub(float2 a, float2 b) { return __ffma2_rn(b, make_float2(-1.f, -1.f), a); }
+
+#if HEXA_OP_PACKED
+template <>
+__device__ __forceinline__ void xy_forward<float>(const float (&v)[4][3], float (&m)[4][3]) {
+  const float2 v0 = pk(v[0][0], v[0][1]), v1 = pk(v[1][0], v[1][1]), v2 = pk(v[2][0], v[2][1]),
+               v3 = pk(v[3][0], v[3][1]);
+  const float2 a0 = pk_add(v0, v1), a1 = pk_sub(v1, v0), b0 = pk_add(v2, v3), b1 = pk_sub(v3, v2);
+  const float2 m0 = pk_add(a0, b0), m1 = pk_add(a1, b1), m2 = pk_sub(b0, a0), m3 = pk_sub(b1, a1);
+  m[0][0] = m0.x, m[0][1] = m0.y, m[1][0] = m1.x, m[1][1] = m1.y;
+  m[2][0] = m2.x, m[2][1] = m2.y, m[3][0] = m3.x, m[3][1] = m3.y;
+  const float a0z = v[0][2] + v[1][2], a1z = v[1][2] - v[0][2];
+  const float b0z = v[2][2] + v[3][2], b1z = v[3][2] - v[2][2];
+  m[0][2] = a0z + b0z, m[1][2] = a1z + b1z, m[2][2] = b0z - a0z, m[3][2] = b1z - a1z;
+}
+
+template <>
+__device__ __forceinline__ void xy_inverse<float>(const float (&m)[4][3], float (&v)[4][3]) {
+  const float2 m0 = pk(m[0][0], m[0][1]), m1 = pk(m[1][0], m[1][1]), m2 = pk(m[2][0], m[2][1]),
+               m3 = pk(m[3][0], m[3][1]);
+  const float2 A0 = pk_sub(m0, m2), B0 = pk_add(m0, m2), A1 = pk_sub(m1, m3), B1 = pk_add(m1, m3);
+  const float2 v0 = pk_sub(A0, A1), v1 = pk_add(A0, A1), v2 = pk_sub(B0, B1), v3 = pk_add(B0, B1);
+  v[0][0] = v0.x, v[0][1] = v0.y, v[1][0] = v1.x, v[1][1] = v1.y;
+  v[2][0] = v2.x, v[2][1] = v2.y, v[3][0] = v3.x, v[3][1] = v3.y;
+  const float A0z = m[0][2] - m[2][2], B0z = m[0][2] + m[2][2];
+  const float A1z = m[1][2] - m[3][2], B1z = m[1][2] + m[3][2];
+  v[0][2] = A0z - A1z, v[1][2] = A0z + A1z, v[2][2] = B0z - B1z, v[3][2] = B0z + B1z;
+}
+#endif
+
+// lo += carry (the upper half of the element below)
+template <typename T>
+__device__ __forceinline__ void add_carry(T (&lo)[4][3], const T (&carry)[4][3]) {
+#pragma unroll
+  for (int m = 0; m < 4; ++m)
+#pragma unroll
+    for (int c = 0; c < 3; ++c) lo[m][c] += carry[m][c];
+}
+#if HEXA_OP_PACKED
+template <>
+__device__ __forceinline__ void add_carry<float>(float (&lo)[4][3], const float (&carry)[4][3]) {
+#pragma unroll
+  for (int m = 0; m < 4; ++m) {
+    const float2 t = pk_add(pk(lo[m][0], lo[m][1]), pk(carry[m][0], carry[m][1]));
+    lo[m][0] = t.x, lo[m][1] = t.y;
+    lo[m][2] += carry[m][2];
+  }
+}
+#endif
+
 // One element: lower/upper xy-modal node data -> lower/upper xy-modal
 // contributions of f * K0 * u_e.
 template <typename T>
@@ -151,16 +209,53 @@ __device__ __forceinline__ void element_modal(const ModalK<T>& K, const T (&L)[4
     }
 }
 
+#if HEXA_OP_PACKED
+template <>
+__device__ __forceinline__ void element_modal<float>(const ModalK<float>& K, const float (&L)[4][3],
+                                                     const float (&U)[4][3], float f, float (&lo)[4][3],
+                                                     float (&hi)[4][3]) {
+  const float2 f2 = pk(f, f), nf2 = pk(-f, -f);
+  float uh[8][3];
+#pragma unroll
+  for (int mxy = 0; mxy < 4; ++mxy) {
+    const float2 fu = __fmul2_rn(f2, pk(U[mxy][0], U[mxy][1]));
+    const float2 l = pk(L[mxy][0], L[mxy][1]);
+    const float2 s0 = __ffma2_rn(f2, l, fu), s1 = __ffma2_rn(nf2, l, fu);
+    uh[mxy][0] = s0.x, uh[mxy][1] = s0.y, uh[mxy + 4][0] = s1.x, uh[mxy + 4][1] = s1.y;
+    const float fuz = f * U[mxy][2];
+    uh[mxy][2] = fmaf(f, L[mxy][2], fuz);
+    uh[mxy + 4][2] = fmaf(-f, L[mxy][2], fuz);
+  }
+  float wh[8][3];
+#pragma unroll
+  for (int m = 0; m < 8; ++m)
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      const int q = m ^ (1 << c);
+      float s = 0.f;
+#pragma unroll
+      for (int c2 = 0; c2 < 3; ++c2)
+        if (modal_nz(q, c, c2)) s = fmaf(K.B[q][c][c2], uh[q ^ (1 << c2)][c2], s);
+      wh[m][c] = s;
+    }
+#pragma unroll
+  for (int mxy = 0; mxy < 4; ++mxy) {
+    const float2 w0 = pk(wh[mxy][0], wh[mxy][1]), w1 = pk(wh[mxy + 4][0], wh[mxy + 4][1]);
+    const float2 l = pk_sub(w0, w1), h = pk_add(w0, w1);
+    lo[mxy][0] = l.x, lo[mxy][1] = l.y, hi[mxy][0] = h.x, hi[mxy][1] = h.y;
+    lo[mxy][2] = wh[mxy][2] - wh[mxy + 4][2];
+    hi[mxy][2] = wh[mxy][2] + wh[mxy + 4][2];
+  }
+}
+#endif
+
 // CTA height in warps.  FP32: 16 warps, one CTA per SM (127 registers); 8-warp
 // CTAs two per SM measured 5 % slower on the 384x192x192 Chebyshev step
 // (359 us against 340 us), the larger halo outweighing the shorter barriers.
 #ifndef HEXA_OP_TYW32
 #define HEXA_OP_TYW32 16
 #endif
-#ifndef HEXA_OP_ASYNC
-#define HEXA_OP_ASYNC 0
-#endif
-constexpr int kRingStages = 3, kRingSlots = 20;
+
 template <typename T>
 constexpr int op_tyw() { return sizeof(T) == 8 ? 8 : HEXA_OP_TYW32; }
 #ifndef HEXA_OP_MINCTAS32
@@ -168,8 +263,7 @@ constexpr int op_tyw() { return sizeof(T) == 8 ? 8 : HEXA_OP_TYW32; }
 #endif
 template <typename T>
 constexpr int op_min_ctas() { return sizeof(T) == 8 ? 1 : HEXA_OP_MINCTAS32; }
-template <typename T, bool MULTI>
-constexpr bool op_async() { return HEXA_OP_ASYNC && sizeof(T) == 4 && !MULTI; }
+
 
 // Four values of the y-exchange as one 16-byte shared-memory access per thread
 // (float4; two 16-byte halves for double).
@@ -189,28 +283,13 @@ __device__ __forceinline__ void load4(const double* p, double (&v)[4]) {
   v[0] = t0.x, v[1] = t0.y, v[2] = t1.x, v[3] = t1.y;
 }
 
-// FP32 operator loads staged through a per-thread shared-memory ring with
-// cp.async (4-byte copies, zero-filled where masked), two node layers ahead:
-// each thread copies exactly the 19 values it later reads (12 corner values,
-// its element factor, b and the previous iterate at its node), so the ring
-// needs no cross-thread synchronisation and the loads' latency is hidden
-// without the registers a deeper register prefetch would take.
-
-__device__ __forceinline__ void cp_async4(float* dst, const float* src, bool ok) {
-  const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
-  asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;\n" ::"r"(d), "l"(src), "r"(ok ? 4 : 0) : "memory");
-}
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
-__device__ __forceinline__ void cp_async_wait1() { asm volatile("cp.async.wait_group 1;\n" ::: "memory"); }
-__device__ __forceinline__ void cp_async_wait0() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
-
 // One work item: the node columns of tile (tx, ty) for node layers [k0, k1).
 // IX is the index type: int whenever 3 * nNodes fits, which halves the
 // integer work of the address arithmetic.
-template <typename T, int MODE, int TYW, typename IX, typename A, bool ASYNC = false>
+template <typename T, int MODE, int TYW, typename IX, typename A>
 __device__ __forceinline__ void op_item(const A& a, int tx, int ty, int chunk,
                                         T (&xch)[2][TYW][32][4],
-                                        double& acc0, long long co, float* ring = nullptr) {
+                                        double& acc0, long long co) {
   constexpr int NX_OWN = 31, NY_OWN = TYW - 1;
   constexpr bool NEED_F = (MODE == OP_JACOBI || MODE == OP_CHEB2);
   const Grid& g = a.g;
@@ -242,119 +321,71 @@ __device__ __forceinline__ void op_item(const A& a, int tx, int ty, int chunk,
   auto facload = [&](int k) -> T {
     return (colv && k >= 0 && k < g.nz) ? ldx(fac + ecol + eplane * k) : T(0);
   };
-  // ---- staged loads (ASYNC): ring slot q of node layer kk for this thread
-  constexpr int NT = 32 * TYW;
-  const int tid = lane + 32 * wy;
-  auto rslot = [&](int kk, int q) -> float* {
-    const int st = ((kk % kRingStages) + kRingStages) % kRingStages;
-    return ring + (st * kRingSlots + q) * NT + tid;
-  };
-  constexpr bool NEED_B = MODE == OP_RESID || MODE == OP_RESID_NORM || MODE == OP_JACOBI || MODE == OP_CHEB2;
-  auto issue = [&](int kk) {  // node layer kk: corners, element factor kk, b and x_prev at the own node
-    if constexpr (ASYNC) {
-      const bool kok = (kk >= 0) && (kk < g.NZ);
-      const IX lb = ca.base + ca.plane3 * (IX)kk;
-#pragma unroll
-      for (int cc = 0; cc < 4; ++cc) {
-        const bool ok = kok && ca.ok[cc];
-        const IX o = ok ? lb + ((cc & 1) ? 3 : 0) + ((cc >> 1) ? ca.row3 : (IX)0) : (IX)0;
-#pragma unroll
-        for (int c = 0; c < 3; ++c) cp_async4(rslot(kk, 3 * cc + c), (const float*)x + o + c, ok);
-      }
-      const bool fok = colv && kk >= 0 && kk < g.nz;
-      cp_async4(rslot(kk, 12), (const float*)fac + (fok ? ecol + eplane * kk : (IX)0), fok);
-      if (NEED_B) {
-        const bool bok = own && kok;
-        const IX nb3 = bok ? (IX)3 * (ncol + nplane * (IX)kk) : (IX)0;
-#pragma unroll
-        for (int c = 0; c < 3; ++c) cp_async4(rslot(kk, 13 + c), (const float*)bv + nb3 + c, bok);
-        if (MODE == OP_CHEB2) {
-          const bool pok = bok && xinv;
-#pragma unroll
-          for (int c = 0; c < 3; ++c) cp_async4(rslot(kk, 16 + c), pok ? (const float*)xinv + nb3 + c : (const float*)x, pok);
-        }
-      }
-      cp_async_commit();
-    }
-  };
-  auto corners = [&](int kk, T (&v)[4][3]) {
-    if constexpr (ASYNC) {
-#pragma unroll
-      for (int cc = 0; cc < 4; ++cc)
-#pragma unroll
-        for (int c = 0; c < 3; ++c) v[cc][c] = *rslot(kk, 3 * cc + c);
-    } else {
-      load_corners<T, IX>(g, ca, x, kk, v);
-    }
-  };
-  auto facval = [&](int kk) -> T {
-    if constexpr (ASYNC) return *rslot(kk, 12);
-    else return facload(kk);
-  };
-
   T Lm[4][3], carry[4][3], xown[3];
   T fprev;
-  if constexpr (ASYNC) {
-    issue(k0 - 1);
-    issue(k0);
-    issue(k0 + 1);
-    cp_async_wait1();  // layers k0-1 and k0 have landed
-  }
   {
     T raw[4][3];
-    corners(k0 - 1, raw);
+    load_corners<T, IX>(g, ca, x, k0 - 1, raw);
     T Lprev[4][3];
     xy_forward<T>(raw, Lprev);
-    corners(k0, raw);
+    load_corners<T, IX>(g, ca, x, k0, raw);
 #pragma unroll
     for (int c = 0; c < 3; ++c) xown[c] = raw[3][c];
     xy_forward<T>(raw, Lm);
-    fprev = facval(k0 - 1);
+    fprev = facload(k0 - 1);
     T lo[4][3];
     element_modal<T>(a.K, Lprev, Lm, fprev, lo, carry);
   }
+  // b and the previous iterate at the own node are loaded one layer ahead, so
+  // their DRAM latency hides behind the next layer's element work
+  constexpr bool NEED_B = MODE == OP_RESID || MODE == OP_RESID_NORM || MODE == OP_JACOBI || MODE == OP_CHEB2;
+  constexpr bool NEED_P = MODE == OP_CHEB2;
+  T bnext[3] = {T(0), T(0), T(0)}, pnext[3] = {T(0), T(0), T(0)};
+  auto load_bp = [&](int kk) {
+    if (own) {
+      const IX n3 = (IX)3 * (ncol + nplane * (IX)kk);
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        if (NEED_B) bnext[c] = ldx(bv + n3 + c);
+        if (NEED_P) pnext[c] = xinv ? xinv[n3 + c] : T(0);  // plain load: y may alias xin
+      }
+    }
+  };
+  if (NEED_B || NEED_P) load_bp(k0);
 
   // sums of this item in the kernel's own precision (one item is at most a
   // few dozen layers per thread), folded into the FP64 accumulator at the end:
   // FP64 arithmetic in the FP32 kernels would run at GB300's FP64 rate
   T accT = T(0);
   T nraw[4][3];
-  T fnext = T(0);
-  if constexpr (!ASYNC) {
-    load_corners<T, IX>(g, ca, x, k0 + 1, nraw);
-    fnext = facload(k0);
-  }
+  load_corners<T, IX>(g, ca, x, k0 + 1, nraw);
+  T fnext = facload(k0);
 
 #pragma unroll 2
   for (int k = k0; k < k1; ++k) {
     T raw[4][3];
-    T f;
-    if constexpr (ASYNC) {
-      if (k + 2 <= k1) issue(k + 2);  // into the slot layer k-1 used
-      else cp_async_commit();          // empty group keeps the wait count uniform
-      cp_async_wait1();                // layers k and k+1 have landed
-      corners(k + 1, raw);
-      f = facval(k);
-    } else {
 #pragma unroll
-      for (int cc = 0; cc < 4; ++cc)
+    for (int cc = 0; cc < 4; ++cc)
 #pragma unroll
-        for (int c = 0; c < 3; ++c) raw[cc][c] = nraw[cc][c];
-      f = fnext;
-      if (k + 1 < k1) {  // prefetch the next layer
-        load_corners<T, IX>(g, ca, x, k + 2, nraw);
-        fnext = facload(k + 1);
-      }
+      for (int c = 0; c < 3; ++c) raw[cc][c] = nraw[cc][c];
+    const T f = fnext;
+    T bk[3], pk3[3];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) bk[c] = bnext[c], pk3[c] = pnext[c];
+    if (k + 1 < k1) {  // prefetch the next layer
+      load_corners<T, IX>(g, ca, x, k + 2, nraw);
+      fnext = facload(k + 1);
+      if (NEED_B || NEED_P) load_bp(k + 1);
     }
     T Um[4][3];
     xy_forward<T>(raw, Um);
     T lo[4][3], hi[4][3];
     element_modal<T>(a.K, Lm, Um, f, lo, hi);
+    add_carry<T>(lo, carry);
 #pragma unroll
     for (int m = 0; m < 4; ++m)
 #pragma unroll
       for (int c = 0; c < 3; ++c) {
-        lo[m][c] += carry[m][c];
         carry[m][c] = hi[m][c];
         Lm[m][c] = Um[m][c];
       }
@@ -408,18 +439,13 @@ __device__ __forceinline__ void op_item(const A& a, int tx, int ty, int chunk,
           out = fixd ? T(0) : Ax;
           accT = fma(xown[c], out, accT);
         } else if (MODE == OP_RESID || MODE == OP_RESID_NORM) {
-          const T bvc = ASYNC ? (T)*rslot(k, 13 + c) : ldx(bv + 3 * n + c);
-          out = fixd ? T(0) : (bvc - Ax);
+          out = fixd ? T(0) : (bk[c] - Ax);
           if (MODE == OP_RESID_NORM) accT = fma(out, out, accT);
         } else if (MODE == OP_JACOBI) {  // x + omega (b - Ax) / D
-          const T bvc = ASYNC ? (T)*rslot(k, 13 + c) : ldx(bv + 3 * n + c);
-          out = fixd ? T(0) : fma(a.omega * dinv[c], bvc - Ax, xown[c]);
+          out = fixd ? T(0) : fma(a.omega * dinv[c], bk[c] - Ax, xown[c]);
         } else {  // OP_CHEB2: x + c1 (x - x_prev) + c2 D^-1 (b - Ax)
-          // plain load: y may alias xin (the staged copy was taken before this thread's write)
-          const T xp = ASYNC ? (T)*rslot(k, 16 + c) : (xinv ? xinv[3 * n + c] : T(0));
-          const T bvc = ASYNC ? (T)*rslot(k, 13 + c) : ldx(bv + 3 * n + c);
-          const T t = fma(a.c1, xown[c] - xp, xown[c]);
-          out = fixd ? T(0) : fma(a.c2 * dinv[c], bvc - Ax, t);
+          const T t = fma(a.c1, xown[c] - pk3[c], xown[c]);
+          out = fixd ? T(0) : fma(a.c2 * dinv[c], bk[c] - Ax, t);
         }
         yv[3 * n + c] = out;
       }
@@ -429,7 +455,6 @@ __device__ __forceinline__ void op_item(const A& a, int tx, int ty, int chunk,
   }
 
   acc0 += (double)accT;
-  if constexpr (ASYNC) cp_async_wait0();
   __syncthreads();  // the next item reuses xch
 }
 
@@ -437,7 +462,6 @@ template <typename T, int MODE, int TYW, typename IX, bool MULTI>
 __global__ void __launch_bounds__(32 * TYW, op_min_ctas<T>()) op_kernel(const OpArgs<T> a) {
   if (a.halt && *((volatile const int*)a.halt)) return;
   __shared__ __align__(16) T xch[2][TYW][32][4];
-  extern __shared__ __align__(16) float op_ring[];  // staged loads (FP32 single-column forms)
   double acc0 = 0.0;
   // static stride over (tile x, tile y, z-chunk) items: deterministic, and
   // with the grid sized to the resident CTAs no wave is left half empty
@@ -449,7 +473,7 @@ __global__ void __launch_bounds__(32 * TYW, op_min_ctas<T>()) op_kernel(const Op
     if (MULTI) {  // every column of a multi-column apply reuses the item's factors from L1
       for (int col = 0; col < a.ncol; ++col) op_item<T, MODE, TYW, IX>(a, tx, ty, chunk, xch, acc0, col * a.g.ndof());
     } else {
-      op_item<T, MODE, TYW, IX, OpArgs<T>, op_async<T, MULTI>()>(a, tx, ty, chunk, xch, acc0, 0, op_ring);
+      op_item<T, MODE, TYW, IX>(a, tx, ty, chunk, xch, acc0, 0);
     }
   }
   if (MODE == OP_APPLY_DOT || MODE == OP_RESID_NORM) {
@@ -469,24 +493,6 @@ static ModalK<T> cast_modal(const ModalK<double>& K) {
 }
 
 
-// Dynamic shared memory of the staged-load ring (0 for the direct forms).
-template <typename T, bool MULTI>
-constexpr int op_ring_bytes() {
-  return op_async<T, MULTI>() ? kRingStages * kRingSlots * 32 * op_tyw<T>() * (int)sizeof(float) : 0;
-}
-
-// Raises the kernel's dynamic shared-memory limit to the ring size, once.
-template <typename T, int MODE, typename IX, bool MULTI>
-static void op_prepare() {
-  static bool done = false;
-  if (!done) {
-    if (op_ring_bytes<T, MULTI>() > 0)
-      cudaFuncSetAttribute(op_kernel<T, MODE, op_tyw<T>(), IX, MULTI>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           op_ring_bytes<T, MULTI>());
-    done = true;
-  }
-}
-
 template <typename T, int MODE>
 static int op_resident_ctas() {
   static int cached = 0;
@@ -494,9 +500,8 @@ static int op_resident_ctas() {
     int dev = 0, sms = 0, occ = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    op_prepare<T, MODE, long long, false>();
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, op_kernel<T, MODE, op_tyw<T>(), long long, false>,
-                                                  32 * op_tyw<T>(), op_ring_bytes<T, false>());
+                                                  32 * op_tyw<T>(), 0);
     cached = std::max(1, sms) * std::max(1, occ);
   }
   return cached;
@@ -560,15 +565,10 @@ void launch_op(int mode, const OpArgs<T>& a0, cudaStream_t st) {
     }
     return;
   }
-#define HEXA_OP_CASE(M)                                                                      \
-  case M:                                                                                   \
-    if (i32) {                                                                              \
-      op_prepare<T, M, int, false>();                                                       \
-      op_kernel<T, M, TYW, int, false><<<grid, block, op_ring_bytes<T, false>(), st>>>(a);  \
-    } else {                                                                                \
-      op_prepare<T, M, long long, false>();                                                 \
-      op_kernel<T, M, TYW, long long, false><<<grid, block, op_ring_bytes<T, false>(), st>>>(a); \
-    }                                                                                       \
+#define HEXA_OP_CASE(M)                                                              \
+  case M:                                                                           \
+    if (i32) op_kernel<T, M, TYW, int, false><<<grid, block, 0, st>>>(a);           \
+    else op_kernel<T, M, TYW, long long, false><<<grid, block, 0, st>>>(a);         \
     break;
   switch (mode) {
     HEXA_OP_CASE(OP_APPLY)

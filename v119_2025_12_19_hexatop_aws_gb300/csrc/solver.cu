@@ -140,7 +140,7 @@ struct MG {
   T omega = T(0.6);
   int nu1 = 2, nu2 = 2, citers = 30;
   int smoother = HEXA_SMOOTH_CHEBYSHEV;
-  // Chebyshev on [lmax/ratio, lmax] of D^-1 A (ratio 30 by default): d_0 = D^-1 r / theta,
+  // Chebyshev on [lmax/ratio, lmax] of D^-1 A (ratio 10 by default): d_0 = D^-1 r / theta,
   // d_s = c1[s] d_{s-1} + c2[s] D^-1 r_s
   T inv_theta = T(0);
   std::vector<T> c1, c2;
@@ -722,7 +722,7 @@ void configure_mg(MG<T>& mg, const Problem& P, const hexa_solve_params& prm) {
   mg.nu1 = prm.pre_smooth > 0 ? prm.pre_smooth : 1;
   mg.nu2 = prm.post_smooth >= 0 ? prm.post_smooth : 2;
   mg.citers = prm.coarse_iters >= 0 ? prm.coarse_iters : 30;
-  mg.set_chebyshev(lmax, std::max(mg.nu1, mg.nu2) + 1, prm.cheb_ratio > 1 ? prm.cheb_ratio : 30.0);
+  mg.set_chebyshev(lmax, std::max(mg.nu1, mg.nu2) + 1, prm.cheb_ratio > 1 ? prm.cheb_ratio : 10.0);
   mg.ke.assign(576, 0.0);
   if (canonical_stiffness(P.dx, P.dy, P.dz, P.nu, mg.ke.data()) != 0) mg.ke.clear();
 }
@@ -934,14 +934,15 @@ int solve_plain(Ctx& c, const Problem& P, const hexa_solve_params& prm, const do
   return success ? HEXA_OK : HEXA_NOT_CONVERGED;
 }
 
-// Autotuner of the mixed form's multigrid: short FP32 GMG-PCG trials on
-// b = f/||f|| pick the level count (stage 1) and the Chebyshev smoothing steps
-// per side (stage 2) that minimise the estimated time to the tolerance,
-// (log10(1/tol) / digits gained per iteration) * device time per iteration.
-// The choice is cached in the context per grid.
-std::pair<int, int> autotune_mixed(Ctx& c, const Problem& P, const hexa_solve_params& prm, float* fac32,
-                                   const ModalK<float>& K32, double sigma, PcgEnv<float>& E, float* b32,
-                                   double bnorm, MG<float>& mg) {
+// Autotuner of the mixed form's multigrid: short FP32 GMG-PCG trials (120
+// iterations, the rate measured over the last 60) on b = f/||f|| pick the level count (stage 1), the Chebyshev
+// smoothing steps per side (stage 2) and the lower end lmax/ratio of the
+// Chebyshev interval (stage 3) that minimise the estimated time to the
+// tolerance, (log10(1/tol) / digits gained per iteration) * device time per
+// iteration.  The choice is cached in the context per grid.
+Ctx::Tuned autotune_mixed(Ctx& c, const Problem& P, const hexa_solve_params& prm, float* fac32,
+                          const ModalK<float>& K32, double sigma, PcgEnv<float>& E, float* b32, double bnorm,
+                          MG<float>& mg) {
   char key[96];
   std::snprintf(key, sizeof(key), "%d,%d,%d,%d,%g,%g", P.g.nx, P.g.ny, P.g.nz, prm.diag_quirk, P.nu, prm.tol);
   auto it = c.tuned.find(key);
@@ -953,10 +954,11 @@ std::pair<int, int> autotune_mixed(Ctx& c, const Problem& P, const hexa_solve_pa
   c.launches++;
   const double digits = std::log10(1.0 / prm.tol);
   const int lmax = plan_levels(P.g, 16);
-  const int trial_iters = 60;
-  auto trial = [&](int levels, int nu) -> double {
+  const int trial_iters = 120;
+  auto trial = [&](int levels, int nu, int ratio) -> double {
     hexa_solve_params q = prm;
     q.pre_smooth = q.post_smooth = nu;
+    q.cheb_ratio = ratio;
     mg = MG<float>();
     mg.K = K32;
     configure_mg<float>(mg, P, q);
@@ -967,26 +969,48 @@ std::pair<int, int> autotune_mixed(Ctx& c, const Problem& P, const hexa_solve_pa
     E.b = b32;
     launch_fill<float>(E.x, 0.0f, n, c.st);
     c.launches++;
+    // the rate is taken over the second half of the trial, past the quickly
+    // damped start, so that it reflects the slow modes that set the count
     PcgOut o;
     double ms = 0.0;
-    if (!run_pcg<float>(c, E, 1e-30, trial_iters, 1, true, 1.0, false, &o, &ms) || o.iters < 2) return INFINITY;
-    const double rel = o.relres;
-    if (!(rel > 0.0) || !(rel < 1.0)) return INFINITY;
-    const double per_digit = o.iters / (-std::log10(rel));
-    return digits * per_digit * (ms / o.iters);
+    if (!run_pcg<float>(c, E, 1e-30, trial_iters / 2, 1, true, 1.0, false, &o, &ms) || o.iters < 2) return INFINITY;
+    const double rel_half = o.relres;
+    PcgScalars h = *c.hs;
+    h.max_iter = trial_iters;
+    h.halt = 0;
+    h.status = 0;
+    *c.hs = h;
+    cudaMemcpyAsync(c.s, c.hs, sizeof(PcgScalars), cudaMemcpyHostToDevice, c.st);
+    Graph g2;
+    if (!pcg_drive<float>(c, E, g2, &h, &ms)) return INFINITY;
+    const int iters = h.iter - o.iters;
+    const double rel = h.relres;
+    if (iters < 2 || !(rel > 0.0) || !(rel_half > 0.0) || !(rel < rel_half) || !(rel_half < 1.0)) return INFINITY;
+    const double per_digit = iters / std::log10(rel_half / rel);
+    return digits * per_digit * (ms / h.iter);
   };
-  int best_l = std::max(2, lmax), best_nu = 3;
+  const int r0 = prm.cheb_ratio > 1 ? prm.cheb_ratio : 10;
+  int best_l = std::max(2, lmax), best_nu = 3, best_r = r0;
   double best = INFINITY;
   for (int l = std::max(2, lmax - 2); l <= lmax; ++l) {
-    const double t = trial(l, 3);
+    const double t = trial(l, 3, r0);
     if (t < best) best = t, best_l = l;
   }
   for (int nu : {2, 4, 5}) {
-    const double t = trial(best_l, nu);
+    const double t = trial(best_l, nu, r0);
     if (t < best) best = t, best_nu = nu;
   }
-  c.tuned[key] = {best_l, best_nu};
-  return {best_l, best_nu};
+  for (int r : {5, 10, 20, 40}) {  // the lower end of the Chebyshev interval
+    if (r == r0) continue;
+    const double t = trial(best_l, best_nu, r);
+    if (t < best) best = t, best_r = r;
+  }
+  Ctx::Tuned tu;
+  tu.a = best_l;
+  tu.b = best_nu;
+  tu.c = best_r;
+  c.tuned[key] = tu;
+  return tu;
 }
 
 // Mixed precision: FP64 iterative refinement around FP32 GMG-PCG correction
@@ -1044,9 +1068,10 @@ int solve_mixed(Ctx& c, const Problem& P, const hexa_solve_params& prm, const do
   const bool use_mg = prm.precond == HEXA_PRECOND_MULTIGRID;
   hexa_solve_params prm2 = prm;
   if (use_mg && prm.autotune) {
-    const std::pair<int, int> t = autotune_mixed(c, P, prm, fac32, K32, sigma, E, b32, bnorm, mg);
-    prm2.mg_levels = t.first;
-    prm2.pre_smooth = prm2.post_smooth = t.second;
+    const Ctx::Tuned t = autotune_mixed(c, P, prm, fac32, K32, sigma, E, b32, bnorm, mg);
+    prm2.mg_levels = t.a;
+    prm2.pre_smooth = prm2.post_smooth = t.b;
+    prm2.cheb_ratio = t.c;
   }
   if (use_mg) {
     const int nlev = plan_levels(P.g, prm2.mg_levels);
@@ -1289,10 +1314,11 @@ int solve_block(Ctx& c, const Problem& P, int k, const hexa_solve_params& prm, d
         if (!b32 || (k == 1 && !qbuf)) return HEXA_ERR_NOMEM;
         if (k == 1) E.q = qbuf;
         MG<float> tmg;
-        const std::pair<int, int> t =
+        const Ctx::Tuned t =
             autotune_mixed(c, P0, prm, const_cast<float*>(fac), K, sigma, E, b32, fnorm[j0], tmg);
-        prm2.mg_levels = t.first;
-        prm2.pre_smooth = prm2.post_smooth = t.second;
+        prm2.mg_levels = t.a;
+        prm2.pre_smooth = prm2.post_smooth = t.b;
+        prm2.cheb_ratio = t.c;
       }
     }
     mg.K = K;

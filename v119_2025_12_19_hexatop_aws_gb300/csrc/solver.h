@@ -27,8 +27,12 @@ struct Ctx {
   PcgScalars* s2 = nullptr;  // coarse-level PCG
   double* dscal = nullptr;   // 64 device doubles of scratch results
   PcgScalars* hs = nullptr;  // pinned host mirror of s
-  // autotuned multigrid settings per grid and precision: {levels, smoothing steps}
-  std::map<std::string, std::pair<int, int>> tuned;
+  // autotuned settings per problem: multigrid {levels, smoothing steps,
+  // Chebyshev ratio}; batches {z-brick depth, -, -}
+  struct Tuned {
+    int a = 0, b = 0, c = 0;
+  };
+  std::map<std::string, Tuned> tuned;
   double* hscal = nullptr;   // pinned host mirror of dscal
 
   void* get(const std::string& name, size_t bytes);
