@@ -91,6 +91,8 @@ enum FinalizeOp {
   FIN_INIT_RES = 5,     // rr = sum0 ; relres
   FIN_INIT_RZ = 6,      // rz = sum0
   FIN_BLOCK_RES = 7,    // nsum column norms ||R_j||^2 (to dst when given); rr = max; test, iter++
+  FIN_PCG_RES_MG = 8,   // FIN_PCG_RES with sum1 = r_new.z_old kept for FIN_PCG_BETA_RZ
+  FIN_PCG_BETA_RZ = 9,  // rz_new = sum0; flexible beta = (rz_new - r_new.z_old) / rz
 };
 
 // Reduction plumbing of one reducing launch: per-block partials, a ticket
@@ -141,6 +143,9 @@ __device__ __forceinline__ void finalize_scalars(const RedArgs& r, const double*
       }
       break;
     }
+    case FIN_PCG_RES_MG:
+      s->dtmp[0] = tot[1];
+      [[fallthrough]];
     case FIN_PCG_RES: {
       s->rr = tot[0];
       s->iter += 1;
@@ -150,7 +155,7 @@ __device__ __forceinline__ void finalize_scalars(const RedArgs& r, const double*
       const int cad = s->cadence;
       const bool test = (cad > 0) ? ((cad == 1) || (k == 1) || (k % cad == 0)) : ((cad < 0) && (k % (-cad) == 0));
       s->test_now = test ? 1 : 0;
-      if (r.nsum > 1) {  // Jacobi fused: rz_new available now
+      if (r.op == FIN_PCG_RES && r.nsum > 1) {  // Jacobi fused: rz_new available now
         s->rz_prev = s->rz;
         s->beta = (s->rz != 0.0) ? tot[1] / s->rz : 0.0;
         s->rz = tot[1];
@@ -175,6 +180,13 @@ __device__ __forceinline__ void finalize_scalars(const RedArgs& r, const double*
       const double rz_new = tot[0];
       const double num = (r.nsum > 1) ? (rz_new - tot[1]) : rz_new;
       s->beta = (s->rz != 0.0) ? num / s->rz : 0.0;
+      s->rz_prev = s->rz;
+      s->rz = rz_new;
+      break;
+    }
+    case FIN_PCG_BETA_RZ: {
+      const double rz_new = tot[0];
+      s->beta = (s->rz != 0.0) ? (rz_new - s->dtmp[0]) / s->rz : 0.0;
       s->rz_prev = s->rz;
       s->rz = rz_new;
       break;

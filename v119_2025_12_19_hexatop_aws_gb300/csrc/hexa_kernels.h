@@ -15,6 +15,8 @@ enum OpMode {
   OP_RESID_NORM = 3,  // y = b - Ax, sum y.y
   OP_JACOBI = 4,      // y = x + omega D^-1 (b - Ax)
   OP_CHEB2 = 5,       // y = x + c1 (x - xin) + c2 D^-1 (b - Ax)   (xin null: 0; y may alias xin)
+  OP_JACOBI_DOT = 6,  // OP_JACOBI, sum b.y (r.z of the V-cycle's last step)
+  OP_CHEB2_DOT = 7,   // OP_CHEB2, sum b.y
 };
 
 template <typename T>
@@ -79,6 +81,10 @@ void launch_pcg_update(T* x, T* r, T* z, const T* p, const T* q, const T* dinv, 
 // p = z + beta p
 template <typename T>
 void launch_p_update(T* p, const T* z, long long n, const PcgScalars* s, cudaStream_t st, int ncol = 1);
+// x += alpha p, r -= alpha q; sums ||r||^2 and r.zo (FIN_PCG_RES_MG), one column
+template <typename T>
+void launch_pcg_update_mg(T* x, T* r, const T* p, const T* q, const T* zo, long long n, const RedArgs& red,
+                          int nblocks, const PcgScalars* s, cudaStream_t st);
 // x = a[c] x + y per column c (a: ncol device doubles)
 template <typename T>
 void launch_scale_add_cols(T* x, const double* a, const T* y, long long n, int ncol, cudaStream_t st);

@@ -290,8 +290,11 @@ template <typename T, int MODE, int TYW, typename IX, typename A>
 __device__ __forceinline__ void op_item(const A& a, int tx, int ty, int chunk,
                                         T (&xch)[2][TYW][32][4],
                                         double& acc0, long long co) {
+  // the _DOT forms of the smoothing steps also sum b.y
+  constexpr int BM = MODE == OP_JACOBI_DOT ? OP_JACOBI : (MODE == OP_CHEB2_DOT ? OP_CHEB2 : MODE);
+  constexpr bool DOTB = MODE == OP_JACOBI_DOT || MODE == OP_CHEB2_DOT;
   constexpr int NX_OWN = 31, NY_OWN = TYW - 1;
-  constexpr bool NEED_F = (MODE == OP_JACOBI || MODE == OP_CHEB2);
+  constexpr bool NEED_F = (BM == OP_JACOBI || BM == OP_CHEB2);
   const Grid& g = a.g;
   const int lane = threadIdx.x, wy = threadIdx.y;
   const int i0 = tx * NX_OWN, j0 = ty * NY_OWN;
@@ -338,8 +341,8 @@ __device__ __forceinline__ void op_item(const A& a, int tx, int ty, int chunk,
   }
   // b and the previous iterate at the own node are loaded one layer ahead, so
   // their DRAM latency hides behind the next layer's element work
-  constexpr bool NEED_B = MODE == OP_RESID || MODE == OP_RESID_NORM || MODE == OP_JACOBI || MODE == OP_CHEB2;
-  constexpr bool NEED_P = MODE == OP_CHEB2;
+  constexpr bool NEED_B = BM == OP_RESID || BM == OP_RESID_NORM || BM == OP_JACOBI || BM == OP_CHEB2;
+  constexpr bool NEED_P = BM == OP_CHEB2;
   T bnext[3] = {T(0), T(0), T(0)}, pnext[3] = {T(0), T(0), T(0)};
   auto load_bp = [&](int kk) {
     if (own) {
@@ -433,20 +436,21 @@ __device__ __forceinline__ void op_item(const A& a, int tx, int ty, int chunk,
         const bool fixd = (fx >> c) & 1u;
         const T Ax = fma(a.sigma, xown[c], Kx[c]);
         T out;
-        if (MODE == OP_APPLY) {
+        if (BM == OP_APPLY) {
           out = fixd ? T(0) : Ax;
-        } else if (MODE == OP_APPLY_DOT) {
+        } else if (BM == OP_APPLY_DOT) {
           out = fixd ? T(0) : Ax;
           accT = fma(xown[c], out, accT);
-        } else if (MODE == OP_RESID || MODE == OP_RESID_NORM) {
+        } else if (BM == OP_RESID || BM == OP_RESID_NORM) {
           out = fixd ? T(0) : (bk[c] - Ax);
-          if (MODE == OP_RESID_NORM) accT = fma(out, out, accT);
-        } else if (MODE == OP_JACOBI) {  // x + omega (b - Ax) / D
+          if (BM == OP_RESID_NORM) accT = fma(out, out, accT);
+        } else if (BM == OP_JACOBI) {  // x + omega (b - Ax) / D
           out = fixd ? T(0) : fma(a.omega * dinv[c], bk[c] - Ax, xown[c]);
         } else {  // OP_CHEB2: x + c1 (x - x_prev) + c2 D^-1 (b - Ax)
           const T t = fma(a.c1, xown[c] - pk3[c], xown[c]);
           out = fixd ? T(0) : fma(a.c2 * dinv[c], bk[c] - Ax, t);
         }
+        if (DOTB) accT = fma(bk[c], out, accT);
         yv[3 * n + c] = out;
       }
     }
@@ -476,7 +480,7 @@ __global__ void __launch_bounds__(32 * TYW, op_min_ctas<T>()) op_kernel(const Op
       op_item<T, MODE, TYW, IX>(a, tx, ty, chunk, xch, acc0, 0);
     }
   }
-  if (MODE == OP_APPLY_DOT || MODE == OP_RESID_NORM) {
+  if (MODE == OP_APPLY_DOT || MODE == OP_RESID_NORM || MODE == OP_JACOBI_DOT || MODE == OP_CHEB2_DOT) {
     double v[1] = {acc0};
     block_reduce_finalize<1>(a.red, v);
   }
@@ -577,6 +581,8 @@ void launch_op(int mode, const OpArgs<T>& a0, cudaStream_t st) {
     HEXA_OP_CASE(OP_RESID_NORM)
     HEXA_OP_CASE(OP_JACOBI)
     HEXA_OP_CASE(OP_CHEB2)
+    HEXA_OP_CASE(OP_JACOBI_DOT)
+    HEXA_OP_CASE(OP_CHEB2_DOT)
     default: break;
   }
 #undef HEXA_OP_CASE

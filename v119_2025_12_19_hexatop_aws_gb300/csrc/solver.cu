@@ -413,12 +413,15 @@ void coarse_solve(Ctx& c, MG<T>& mg, const T* b, T* x, const int* halt_main) {
   (void)halt_main;
 }
 
+// One V-cycle from level l.  With fin given, the last post-smoothing step
+// of the cycle also sums b.x_out (r.z of the flexible PCG) into that reduction;
+// returns whether it did.
 template <typename T>
-void vcycle(Ctx& c, MG<T>& mg, int l, const T* b, T* xout, const int* halt) {
+bool vcycle(Ctx& c, MG<T>& mg, int l, const T* b, T* xout, const int* halt, const RedArgs* fin = nullptr) {
   Lev<T>& V = mg.L[l];
   if (l == (int)mg.L.size() - 1) {
     coarse_solve<T>(c, mg, b, xout, halt);
-    return;
+    return false;
   }
   // x buffers alternate between xout and V.xb so that the last write lands in xout
   const int nw = mg.nu1 + mg.nu2;
@@ -459,16 +462,32 @@ void vcycle(Ctx& c, MG<T>& mg, int l, const T* b, T* xout, const int* halt) {
   vcycle<T>(c, mg, l + 1, C.b, C.xa, halt);
   launch_prolong_add<T>(C.g, C.xa, V.g, V.m, cur, halt, c.st);
   c.launches++;
+  bool fused = false;
   for (int s = 0; s < mg.nu2; ++s) {
+    const bool last = fin && s == mg.nu2 - 1;
     if (cheb && s > 0) {
-      cheb_step(s);
+      if (last) {
+        T* nx = bufw(w++);
+        OpArgs<T> a = opargs<T>(V, mg.K, mg.quirk, cur, b, nx, T(0), halt, *fin);
+        a.xin = prev;
+        a.c1 = mg.c1[s];
+        a.c2 = mg.c2[s];
+        op<T>(c, OP_CHEB2_DOT, a);
+        prev = cur;
+        cur = nx;
+      } else {
+        cheb_step(s);
+      }
     } else {  // damped Jacobi, or the first Chebyshev step (omega = 1/theta)
       T* nx = bufw(w++);
-      op<T>(c, OP_JACOBI, opargs<T>(V, mg.K, mg.quirk, cur, b, nx, cheb ? mg.inv_theta : mg.omega, halt, none));
+      op<T>(c, last ? OP_JACOBI_DOT : OP_JACOBI,
+            opargs<T>(V, mg.K, mg.quirk, cur, b, nx, cheb ? mg.inv_theta : mg.omega, halt, last ? *fin : none));
       prev = cur;
       cur = nx;
     }
+    fused = fused || last;
   }
+  return fused;
 }
 
 // A CUDA graph replaying a fixed launch sequence.
@@ -548,12 +567,17 @@ void pcg_iteration(Ctx& c, PcgEnv<T>& E, int parity) {
   } else {
     T* zc = (parity == 0) ? E.zB : E.zA;
     T* zo = (parity == 0) ? E.zA : E.zB;
-    launch_pcg_update<T>(E.x, E.r, nullptr, E.p, E.q, nullptr, E.n, red(c, FIN_PCG_RES, 1, c.s), kRedBlocks, c.s, c.st);
+    // flexible beta = (r.z_new - r.z_old) / rz: r.z_old comes with the update
+    // pass, r.z_new with the V-cycle's last smoothing step (no separate dot pass)
+    launch_pcg_update_mg<T>(E.x, E.r, E.p, E.q, zo, E.n, red(c, FIN_PCG_RES_MG, 2, c.s), kRedBlocks, c.s, c.st);
     c.launches++;
-    vcycle<T>(c, *E.mg, 0, E.r, zc, halt);
-    launch_dot<T>(E.r, zc, E.r, zo, E.n, red(c, FIN_PCG_BETA, 2, c.s), kRedBlocks, halt, c.st);
+    const RedArgs fin = red(c, FIN_PCG_BETA_RZ, 1, c.s);
+    if (!vcycle<T>(c, *E.mg, 0, E.r, zc, halt, &fin)) {
+      launch_dot<T>(E.r, zc, E.r, zo, E.n, red(c, FIN_PCG_BETA, 2, c.s), kRedBlocks, halt, c.st);
+      c.launches++;
+    }
     launch_p_update<T>(E.p, zc, E.n, c.s, c.st);
-    c.launches += 2;
+    c.launches++;
   }
 }
 

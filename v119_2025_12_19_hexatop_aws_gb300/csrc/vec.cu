@@ -349,6 +349,63 @@ void launch_pcg_update(T* x, T* r, T* z, const T* p, const T* q, const T* dinv, 
   }
 }
 
+// Flexible-PCG update: x += alpha p, r -= alpha q, sums ||r||^2 and r.z_old
+// (the z of the previous iteration; its partner r.z_new comes from the
+// V-cycle's last smoothing step).
+template <typename T, bool VEC>
+__global__ void pcg_update_mg_kernel(T* __restrict__ x, T* __restrict__ r, const T* __restrict__ p,
+                                     const T* __restrict__ q, const T* __restrict__ zo, long long n, RedArgs red,
+                                     const PcgScalars* s) {
+  const ColMap cm = colmap(red.ncol);
+  if (*((volatile const int*)&s[cm.col].halt)) return;
+  const T alpha = (T)s[cm.col].alpha;
+  double acc[2] = {0.0, 0.0};
+  T part[2] = {T(0), T(0)};
+  int cnt = 0;
+  long long tail = 0;
+  if (VEC) {
+    constexpr int W = V16<T>::W;
+    const long long nv = n / W;
+    tail = nv * W;
+    for (long long i = cm.first; i < nv; i += cm.stride) {
+      T xv[W], rv[W], pv[W], qv[W], zv[W];
+      ldv(x, i, xv);
+      ldv(r, i, rv);
+      ldv(p, i, pv);
+      ldv(q, i, qv);
+      ldv(zo, i, zv);
+#pragma unroll
+      for (int w = 0; w < W; ++w) {
+        xv[w] = fma(alpha, pv[w], xv[w]);
+        rv[w] = fma(-alpha, qv[w], rv[w]);
+        part[0] = fma(rv[w], rv[w], part[0]);
+        part[1] = fma(rv[w], zv[w], part[1]);
+      }
+      stv(x, i, xv);
+      stv(r, i, rv);
+      if ((cnt += W) >= kChunk) flush_parts<T, 2>(acc, part, cnt);
+    }
+  }
+  for (long long i = tail + cm.first; i < n; i += cm.stride) {
+    x[i] = fma(alpha, p[i], x[i]);
+    const T ri = fma(-alpha, q[i], r[i]);
+    r[i] = ri;
+    part[0] = fma(ri, ri, part[0]);
+    part[1] = fma(ri, zo[i], part[1]);
+    if (++cnt == kChunk) flush_parts<T, 2>(acc, part, cnt);
+  }
+  flush_parts<T, 2>(acc, part, cnt);
+  block_reduce_finalize<2>(red, acc);
+}
+template <typename T>
+void launch_pcg_update_mg(T* x, T* r, const T* p, const T* q, const T* zo, long long n, const RedArgs& red,
+                          int nblocks, const PcgScalars* s, cudaStream_t st) {
+  if (vec_ok<T>(n, 1, {x, r, p, q, zo}))
+    pcg_update_mg_kernel<T, true><<<nblocks, 256, 0, st>>>(x, r, p, q, zo, n, red, s);
+  else
+    pcg_update_mg_kernel<T, false><<<nblocks, 256, 0, st>>>(x, r, p, q, zo, n, red, s);
+}
+
 template <typename T, bool VEC>
 __global__ void p_update_kernel(T* __restrict__ p, const T* __restrict__ z, long long n,
                                 const PcgScalars* s, int ncol) {
@@ -663,6 +720,8 @@ int vec_batch_plan(BatchInst* in, int n, int unit, int max_blocks) {
                                      const RedArgs&, int, const PcgScalars*, cudaStream_t);      \
   template void launch_p_update<T>(T*, const T*, long long, const PcgScalars*, cudaStream_t, int); \
   template void launch_scale_add_cols<T>(T*, const double*, const T*, long long, int, cudaStream_t); \
+  template void launch_pcg_update_mg<T>(T*, T*, const T*, const T*, const T*, long long, const RedArgs&, int,  \
+                                        const PcgScalars*, cudaStream_t);                                     \
   template void launch_jacobi_precond<T>(T*, const T*, const T*, long long, const RedArgs&, int, \
                                          const int*, cudaStream_t);                             \
   template void launch_axpby<T>(T*, T, const T*, T, long long, cudaStream_t);                    \
