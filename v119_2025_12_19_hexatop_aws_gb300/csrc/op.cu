@@ -62,11 +62,32 @@ __device__ __forceinline__ ColumnAddr<IX> column_addr(const Grid& g, int ie, int
 }
 
 // Corner values of the column at node layer kk; zeros outside the grid.
-template <typename T, typename IX>
+// INTERIOR: every corner of every column of the tile lies inside the grid in
+// x and y, so only the (CTA-uniform) layer test remains.
+template <typename T, typename IX, bool INTERIOR = false>
 __device__ __forceinline__ void load_corners(const Grid& g, const ColumnAddr<IX>& ca, const T* __restrict__ x, int kk,
                                              T (&v)[4][3]) {
   const bool kok = (kk >= 0) && (kk < g.NZ);
   const IX lb = ca.base + ca.plane3 * (IX)kk;
+  if (INTERIOR) {
+    if (kok) {
+      const T* __restrict__ p0 = x + lb;
+      const T* __restrict__ p2 = p0 + ca.row3;
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        v[0][c] = ldx(p0 + c);
+        v[1][c] = ldx(p0 + 3 + c);
+        v[2][c] = ldx(p2 + c);
+        v[3][c] = ldx(p2 + 3 + c);
+      }
+    } else {
+#pragma unroll
+      for (int cc = 0; cc < 4; ++cc)
+#pragma unroll
+        for (int c = 0; c < 3; ++c) v[cc][c] = T(0);
+    }
+    return;
+  }
 #pragma unroll
   for (int cc = 0; cc < 4; ++cc) {
     const bool ok = kok && ca.ok[cc];
@@ -76,9 +97,15 @@ __device__ __forceinline__ void load_corners(const Grid& g, const ColumnAddr<IX>
   }
 }
 
-// 1/d for the smoothers: correctly rounded in FP32; in FP64 a float seed and
-// two Newton steps (relative error far below 1e-15, deterministic).
-__device__ __forceinline__ float recip(float d) { return __frcp_rn(d); }
+// 1/d for the smoothers: in FP32 the hardware reciprocal approximation
+// (rcp.approx, about 1 ulp; the diagonal only scales a smoothing step); in
+// FP64 a float seed and two Newton steps (relative error far below 1e-15).
+// Both are deterministic.
+__device__ __forceinline__ float recip(float d) {
+  float r;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(d));
+  return r;
+}
 __device__ __forceinline__ double recip(double d) {
   double r = (double)__frcp_rn((float)d);
   r = r * fma(-d, r, 2.0);
@@ -286,7 +313,7 @@ __device__ __forceinline__ void load4(const double* p, double (&v)[4]) {
 // One work item: the node columns of tile (tx, ty) for node layers [k0, k1).
 // IX is the index type: int whenever 3 * nNodes fits, which halves the
 // integer work of the address arithmetic.
-template <typename T, int MODE, int TYW, typename IX, typename A>
+template <typename T, int MODE, int TYW, typename IX, typename A, bool INTERIOR = false>
 __device__ __forceinline__ void op_item(const A& a, int tx, int ty, int chunk,
                                         T (&xch)[2][TYW][32][4],
                                         double& acc0, long long co) {
@@ -301,11 +328,11 @@ __device__ __forceinline__ void op_item(const A& a, int tx, int ty, int chunk,
   const int k0 = chunk * a.kchunk;
   const int k1 = min(k0 + a.kchunk, g.NZ);
   const int ie = i0 - 1 + lane, je = j0 - 1 + wy;
-  const bool colv = (ie >= 0) && (ie < g.nx) && (je >= 0) && (je < g.ny);
+  const bool colv = INTERIOR || ((ie >= 0) && (ie < g.nx) && (je >= 0) && (je < g.ny));
   const IX ecol = colv ? ((IX)ie + (IX)g.nx * je) : (IX)0;
   const IX eplane = (IX)g.nx * g.ny;
   const int in = i0 + lane, jn = j0 + wy;
-  const bool own = (lane < NX_OWN) && (wy < NY_OWN) && (in < g.NX) && (jn < g.NY);
+  const bool own = (lane < NX_OWN) && (wy < NY_OWN) && (INTERIOR || ((in < g.NX) && (jn < g.NY)));
   // column co / ndof of a multi-column apply (the factors are shared)
   const T* __restrict__ x = a.x + co;
   const T* __restrict__ bv = a.b ? a.b + co : a.b;
@@ -316,8 +343,8 @@ __device__ __forceinline__ void op_item(const A& a, int tx, int ty, int chunk,
   // Dirichlet bits of this thread's node column: the x/y faces are fixed per
   // column, the z faces and the optional node mask are tested per layer
   const uint32_t F = a.m.faces;
-  const unsigned colfix = (((F & 1u) && in == 0) || ((F & 2u) && in == g.NX - 1) || ((F & 4u) && jn == 0) ||
-                           ((F & 8u) && jn == g.NY - 1)) ? 7u : 0u;
+  const unsigned colfix = (!INTERIOR && (((F & 1u) && in == 0) || ((F & 2u) && in == g.NX - 1) ||
+                                          ((F & 4u) && jn == 0) || ((F & 8u) && jn == g.NY - 1))) ? 7u : 0u;
   const IX nplane = (IX)g.NX * g.NY;
   const IX ncol = (IX)in + (IX)g.NX * jn;
 
@@ -328,10 +355,10 @@ __device__ __forceinline__ void op_item(const A& a, int tx, int ty, int chunk,
   T fprev;
   {
     T raw[4][3];
-    load_corners<T, IX>(g, ca, x, k0 - 1, raw);
+    load_corners<T, IX, INTERIOR>(g, ca, x, k0 - 1, raw);
     T Lprev[4][3];
     xy_forward<T>(raw, Lprev);
-    load_corners<T, IX>(g, ca, x, k0, raw);
+    load_corners<T, IX, INTERIOR>(g, ca, x, k0, raw);
 #pragma unroll
     for (int c = 0; c < 3; ++c) xown[c] = raw[3][c];
     xy_forward<T>(raw, Lm);
@@ -361,7 +388,7 @@ __device__ __forceinline__ void op_item(const A& a, int tx, int ty, int chunk,
   // FP64 arithmetic in the FP32 kernels would run at GB300's FP64 rate
   T accT = T(0);
   T nraw[4][3];
-  load_corners<T, IX>(g, ca, x, k0 + 1, nraw);
+  load_corners<T, IX, INTERIOR>(g, ca, x, k0 + 1, nraw);
   T fnext = facload(k0);
 
 #pragma unroll 2
@@ -376,7 +403,7 @@ __device__ __forceinline__ void op_item(const A& a, int tx, int ty, int chunk,
 #pragma unroll
     for (int c = 0; c < 3; ++c) bk[c] = bnext[c], pk3[c] = pnext[c];
     if (k + 1 < k1) {  // prefetch the next layer
-      load_corners<T, IX>(g, ca, x, k + 2, nraw);
+      load_corners<T, IX, INTERIOR>(g, ca, x, k + 2, nraw);
       fnext = facload(k + 1);
       if (NEED_B || NEED_P) load_bp(k + 1);
     }
@@ -462,6 +489,17 @@ __device__ __forceinline__ void op_item(const A& a, int tx, int ty, int chunk,
   __syncthreads();  // the next item reuses xch
 }
 
+// Whether every corner of every column of tile (tx, ty) lies inside the grid
+// in x and y (the predicate-free form of the item applies).
+#ifndef HEXA_OP_INTERIOR
+#define HEXA_OP_INTERIOR 1
+#endif
+template <int TYW>
+__device__ __forceinline__ bool tile_interior(const Grid& g, int tx, int ty) {
+  const int i0 = tx * 31, j0 = ty * (TYW - 1);
+  return i0 >= 1 && i0 + 31 <= g.NX - 1 && j0 >= 1 && j0 + TYW - 1 <= g.NY - 1;
+}
+
 template <typename T, int MODE, int TYW, typename IX, bool MULTI>
 __global__ void __launch_bounds__(32 * TYW, op_min_ctas<T>()) op_kernel(const OpArgs<T> a) {
   if (a.halt && *((volatile const int*)a.halt)) return;
@@ -476,6 +514,8 @@ __global__ void __launch_bounds__(32 * TYW, op_min_ctas<T>()) op_kernel(const Op
     const int ty = t / a.tiles_x, tx = t - ty * a.tiles_x;
     if (MULTI) {  // every column of a multi-column apply reuses the item's factors from L1
       for (int col = 0; col < a.ncol; ++col) op_item<T, MODE, TYW, IX>(a, tx, ty, chunk, xch, acc0, col * a.g.ndof());
+    } else if (HEXA_OP_INTERIOR && tile_interior<TYW>(a.g, tx, ty)) {
+      op_item<T, MODE, TYW, IX, OpArgs<T>, true>(a, tx, ty, chunk, xch, acc0, 0);
     } else {
       op_item<T, MODE, TYW, IX>(a, tx, ty, chunk, xch, acc0, 0);
     }
