@@ -55,6 +55,9 @@ def parse():
                     help="profiling run: the warm-up and timed mixed steps only (no plain FP64, e2e, roofline or "
                          "CPU legs), the timed steps bracketed by cudaProfilerStart/Stop for "
                          "ncu --profile-from-start off; used for the launch lists under profiles/")
+    ap.add_argument("--mg", default=None,
+                    help="levels,steps,ratio: fixed multigrid settings for the mixed solves instead of the "
+                         "autotuner (profile runs, where ncu's own overhead would distort the tuner's timings)")
     ap.add_argument("--kernel", default=None, choices=["apply", "apply_dot", "residual", "jacobi", "chebyshev",
                                                        "apply_fp64"],
                     help="time one operator mode alone on the config grid (--steps launches after --warmup) and "
@@ -165,6 +168,9 @@ def make_inputs(name, ctx):
     return grid, rho, fac, f
 
 
+MG_OVERRIDE = None
+
+
 def solver_params(name, precision):
     """The plain FP64 form uses the configuration's multigrid (4 levels at c2,
     5 at c3, V(2,2)); the mixed form is the autotuned one (level count and
@@ -172,6 +178,10 @@ def solver_params(name, precision):
     from v119_2025_12_19_hexatop_aws_gb300 import _lib, workloads as W
     # the reference's rel > 10 divergence stop (GPUSolver.jl:397) is off: CG residuals of these
     # high-contrast systems oscillate above it on the way to convergence
+    if precision == "mixed" and MG_OVERRIDE:
+        lv, nu, ratio = MG_OVERRIDE
+        return _lib.default_params(precision=precision, precond="multigrid", tol=1e-9, max_iter=60000, mg_levels=lv,
+                                   pre_smooth=nu, post_smooth=nu, cheb_ratio=ratio, divergence_check=0, autotune=0)
     return _lib.default_params(precision=precision, precond="multigrid", tol=1e-9, max_iter=60000,
                                mg_levels=W.MG_LEVELS.get(name, 0), pre_smooth=2, post_smooth=2,
                                divergence_check=0, autotune=1 if precision == "mixed" else 0)
@@ -591,8 +601,10 @@ def run_c5(a):
     R = W.helmholtz_R(1.5)
     pm = solver_params("c5", "mixed")
 
+    # the in-batch filter runs with the reference's own settings: Float32
+    # Jacobi-PCG, tolerance 1e-5, at most 200 iterations (GPUHelmholtz.jl:190-266)
     def batch():
-        filter_batch(grids, rho_d, R, tol=1e-9, max_iter=2000, quirk=False, out=filt_d, ctx=ctx)
+        filter_batch(grids, rho_d, R, tol=1e-5, max_iter=200, quirk=True, precision="fp32", out=filt_d, ctx=ctx)
         facs = [W.EMIN + r ** W.PENAL * (W.E0 - W.EMIN) for r in filt_d]
         _, st, rc = solve_batch(grids, facs, f_d, clamp_faces=1, params=pm, u_out=u_d, ctx=ctx)
         return st
@@ -600,7 +612,8 @@ def run_c5(a):
     def one_by_one():
         st = []
         for i, g in enumerate(grids):
-            fr, _ = filter_density(g, rho_d[i], R, tol=1e-9, max_iter=2000, quirk=False, out=filt_d[i], ctx=ctx)
+            fr, _ = filter_density(g, rho_d[i], R, tol=1e-5, max_iter=200, quirk=True, precision="fp32",
+                                   out=filt_d[i], ctx=ctx)
             fac = W.EMIN + filt_d[i] ** W.PENAL * (W.E0 - W.EMIN)
             _, s = solve(g, fac, f_d[i], clamp_faces=1, params=pm, u_out=u_d[i], ctx=ctx)
             st.append(s)
@@ -636,6 +649,8 @@ def run_c5(a):
 
 if __name__ == "__main__":
     args = parse()
+    if args.mg:
+        MG_OVERRIDE = tuple(int(v) for v in args.mg.split(","))
     if args.impl == "reference":
         run_reference(args)
     elif args.config == "c4":

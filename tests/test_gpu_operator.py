@@ -8,7 +8,9 @@ from v119_2025_12_19_hexatop_aws_gb300.solver import apply_operator, operator_di
 
 pytestmark = pytest.mark.gpu
 
-GRIDS = [(1, 1, 1), (2, 1, 1), (4, 2, 2), (5, 3, 7), (33, 17, 9), (62, 15, 20), (31, 7, 3)]
+# (62, 15, 20) and (64, 32, 12) have tiles whose columns all lie inside the
+# grid (the predicate-free item path of the kernel), besides boundary tiles
+GRIDS = [(1, 1, 1), (2, 1, 1), (4, 2, 2), (5, 3, 7), (33, 17, 9), (62, 15, 20), (31, 7, 3), (64, 32, 12)]
 
 
 def _case(oracle, rng, dims, h=(1.0, 1.0, 1.0), faces=1, nodemask=False):
@@ -33,7 +35,7 @@ def test_apply_fp64_matches_oracle(ctx, oracle, rng, dims, sigma):
     assert np.abs(y - y_ref).max() <= 1e-13 * scale
 
 
-@pytest.mark.parametrize("dims", [(5, 3, 7), (33, 17, 9)])
+@pytest.mark.parametrize("dims", [(5, 3, 7), (33, 17, 9), (64, 32, 6)])
 def test_apply_brick_nodemask_faces(ctx, oracle, rng, dims):
     h = (1.0, 2.0, 0.5)
     g, fac, x, fd, fixed = _case(oracle, rng, dims, h=h, faces=0b010110, nodemask=True)
@@ -43,7 +45,7 @@ def test_apply_brick_nodemask_faces(ctx, oracle, rng, dims):
     assert np.abs(y - y_ref).max() <= 1e-13 * np.abs(y_ref).max()
 
 
-@pytest.mark.parametrize("dims", [(4, 2, 2), (33, 17, 9)])
+@pytest.mark.parametrize("dims", [(4, 2, 2), (33, 17, 9), (64, 32, 12)])
 def test_apply_fp32_matches_oracle(ctx, oracle, rng, dims):
     g, fac, x, fd, fixed = _case(oracle, rng, dims, faces=1)
     K0 = oracle.canonical_stiffness(1, 1, 1, 0.3)

@@ -201,3 +201,21 @@ def test_autotuned_mixed_matches_fp64_and_caches(ctx, oracle, rng):
     assert s2["setup_ms"] < s1["setup_ms"]  # the second call reuses the tuned settings
     assert np.array_equal(um, um2)
     assert abs(s1["compliance"] - s64["compliance"]) <= 1e-8 * abs(s64["compliance"])
+
+
+def test_mixed_matches_fp64_on_a_grid_with_interior_tiles(ctx, oracle, rng):
+    """64x32x16: the FP32 smoothing, residual and PCG operator forms run both
+    their interior-tile and boundary-tile item paths."""
+    dims = (64, 32, 16)
+    g = oracle.Grid(*dims)
+    rho = np.clip(0.3 + 0.3 * rng.standard_normal(g.nelem), 0.001, 1.0)
+    fac = 1e-9 + rho ** 3 * (1 - 1e-9)
+    f = workloads.edge_load(*dims)
+    grid = _lib.make_grid(*dims)
+    u64, s64 = solve(grid, fac, f, clamp_faces=1, params=_lib.default_params(divergence_check=0, tol=1e-11), ctx=ctx)
+    um, sm = solve(grid, fac, f, clamp_faces=1, params=_lib.default_params(precision="mixed", divergence_check=0,
+                                                                           tol=1e-11), ctx=ctx)
+    assert s64["status"] == 0 and sm["status"] == 0
+    assert sm["true_relres"] <= 1e-11
+    assert np.linalg.norm(um - u64) <= 1e-7 * np.linalg.norm(u64)
+    assert abs(sm["compliance"] - s64["compliance"]) <= 1e-10 * abs(s64["compliance"])
