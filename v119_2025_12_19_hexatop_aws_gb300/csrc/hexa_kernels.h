@@ -57,7 +57,6 @@ ModalK<float> modal_to_f32(const ModalK<double>& K);
 // diagonal is shared by the columns).
 template <typename T>
 void launch_fill(T* v, T val, long long n, cudaStream_t st);
-void launch_fill_u32(unsigned* v, unsigned val, long long n, cudaStream_t st);
 template <typename T>
 void launch_copy(T* dst, const T* src, long long n, cudaStream_t st);
 // dst = src with fixed DOFs zeroed (expand/contract semantics)
@@ -85,9 +84,7 @@ void launch_p_update(T* p, const T* z, long long n, const PcgScalars* s, cudaStr
 template <typename T>
 void launch_pcg_update_mg(T* x, T* r, const T* p, const T* q, const T* zo, long long n, const RedArgs& red,
                           int nblocks, const PcgScalars* s, cudaStream_t st);
-// x = a[c] x + y per column c (a: ncol device doubles)
-template <typename T>
-void launch_scale_add_cols(T* x, const double* a, const T* y, long long n, int ncol, cudaStream_t st);
+
 // z = dinv * r (Jacobi) ; rz = r.z
 template <typename T>
 void launch_jacobi_precond(T* z, const T* r, const T* dinv, long long n, const RedArgs& red,

@@ -80,9 +80,6 @@ template <typename T>
 void launch_fill(T* v, T val, long long n, cudaStream_t st) {
   fill_kernel<T><<<vec_blocks(n), 256, 0, st>>>(v, val, n);
 }
-void launch_fill_u32(unsigned* v, unsigned val, long long n, cudaStream_t st) {
-  fill_kernel<unsigned><<<vec_blocks(n), 256, 0, st>>>(v, val, n);
-}
 
 template <typename T>
 __global__ void copy_kernel(T* __restrict__ d, const T* __restrict__ s, long long n) {
@@ -486,20 +483,6 @@ void launch_add_scaled_f32(double* u, const float* d, const double* scale, long 
   add_scaled_f32_kernel<<<col_blocks(vec_blocks(n), ncol), 256, 0, st>>>(u, d, scale, n, ncol);
 }
 
-// x = a[c] * x + y per column (a on the device)
-template <typename T>
-__global__ void scale_add_cols_kernel(T* __restrict__ x, const double* a, const T* __restrict__ y, long long n,
-                                      int ncol) {
-  const ColMap cm = colmap(ncol);
-  const T ac = (T)a[cm.col];
-  const long long off = (long long)cm.col * n;
-  for (long long i = cm.first; i < n; i += cm.stride) x[off + i] = fma(ac, x[off + i], y[off + i]);
-}
-template <typename T>
-void launch_scale_add_cols(T* x, const double* a, const T* y, long long n, int ncol, cudaStream_t st) {
-  scale_add_cols_kernel<T><<<col_blocks(vec_blocks(n), ncol), 256, 0, st>>>(x, a, y, n, ncol);
-}
-
 template <typename T>
 __global__ void axpby_kernel(T* __restrict__ x, T a, const T* __restrict__ y, T b, long long n) {
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
@@ -719,7 +702,6 @@ int vec_batch_plan(BatchInst* in, int n, int unit, int max_blocks) {
   template void launch_pcg_update<T>(T*, T*, T*, const T*, const T*, const T*, long long,        \
                                      const RedArgs&, int, const PcgScalars*, cudaStream_t);      \
   template void launch_p_update<T>(T*, const T*, long long, const PcgScalars*, cudaStream_t, int); \
-  template void launch_scale_add_cols<T>(T*, const double*, const T*, long long, int, cudaStream_t); \
   template void launch_pcg_update_mg<T>(T*, T*, const T*, const T*, const T*, long long, const RedArgs&, int,  \
                                         const PcgScalars*, cudaStream_t);                                     \
   template void launch_jacobi_precond<T>(T*, const T*, const T*, long long, const RedArgs&, int, \
