@@ -94,6 +94,7 @@ typedef struct hexa_solve_params {
   int32_t divergence_check;   /* 1: stop when rel > 10 or (k > 500 and rel > 100 best), GPUSolver.jl:397 */
   int32_t autotune;           /* mixed + multigrid: pick levels and smoother degree by short trial solves,
                                  cached per grid in the context (0: use mg_levels / pre_smooth / post_smooth) */
+  int32_t mg_cycle;           /* coarse-grid visits per level: 1 V-cycle (default), 2 W-cycle */
 } hexa_solve_params;
 
 typedef struct hexa_solve_stats {

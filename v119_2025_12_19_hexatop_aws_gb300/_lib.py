@@ -47,7 +47,7 @@ class SolveParams(C.Structure):
         ("smoother", C.c_int32), ("jacobi_omega", C.c_double), ("cheb_ratio", C.c_int32),
         ("coarse_iters", C.c_int32), ("inner_tol", C.c_double), ("max_outer", C.c_int32),
         ("use_graphs", C.c_int32), ("graph_iters", C.c_int32), ("true_residual", C.c_int32),
-        ("divergence_check", C.c_int32), ("autotune", C.c_int32),
+        ("divergence_check", C.c_int32), ("autotune", C.c_int32), ("mg_cycle", C.c_int32),
     ]
 
 

@@ -149,6 +149,7 @@ void hexa_default_params(hexa_solve_params* p) {
   p->true_residual = 1;
   p->divergence_check = 1;
   p->autotune = 0;
+  p->mg_cycle = 1;
 }
 
 int hexa_create(int32_t device, hexa_ctx** out) {

@@ -128,6 +128,7 @@ struct Lev {
   T* dinv = nullptr, *p = nullptr, *q = nullptr, *z = nullptr;  // coarsest-level PCG
   T* w = nullptr;  // element-product scratch of the single-CTA coarse solve
   T* ainv = nullptr;  // dense inverse of the coarsest operator (small coarse grids)
+  T* xw = nullptr, *bw = nullptr;  // W-cycle: second correction and its right-hand side
   T sigma = 0;
   int kchunk = 4;
 };
@@ -139,6 +140,7 @@ struct MG {
   int quirk = 0;
   T omega = T(0.6);
   int nu1 = 2, nu2 = 2, citers = 30;
+  int gamma = 1;  // coarse-grid visits per level (1: V-cycle, 2: W-cycle)
   int smoother = HEXA_SMOOTH_CHEBYSHEV;
   // Chebyshev on [lmax/ratio, lmax] of D^-1 A (ratio 10 by default): d_0 = D^-1 r / theta,
   // d_s = c1[s] d_{s-1} + c2[s] D^-1 r_s
@@ -239,6 +241,11 @@ bool build_mg(Ctx& c, MG<T>& mg, const Grid& g0, const Mask& m0, const T* fac0, 
     C.b = c.vec<T>(s + "b", n);
     C.r = c.vec<T>(s + "r", n);
     if (!C.fac || !C.xa || !C.xb || !C.b || !C.r) return false;
+    if (mg.gamma > 1) {
+      C.xw = c.vec<T>(s + "xw", n);
+      C.bw = c.vec<T>(s + "bw", n);
+      if (!C.xw || !C.bw) return false;
+    }
     launch_coarsen_factors<T>(F.g, F.fac, C.g, C.fac, c.st);
     c.launches++;
     C.kchunk = pick_kchunk<T>(C.g);
@@ -461,6 +468,15 @@ bool vcycle(Ctx& c, MG<T>& mg, int l, const T* b, T* xout, const int* halt, cons
   launch_restrict<T>(V.g, V.r, C.g, C.m, C.b, halt, c.st);
   c.launches++;
   vcycle<T>(c, mg, l + 1, C.b, C.xa, halt);
+  if (mg.gamma > 1 && C.xw && l + 2 < (int)mg.L.size()) {
+    // W-cycle: a second cycle on the coarse residual (its own right-hand side
+    // and output buffers: the cycle reuses the level's r and xb), added to the
+    // first correction
+    op<T>(c, OP_RESID, opargs<T>(C, mg.K, mg.quirk, C.xa, C.b, C.bw, T(0), halt, none));
+    vcycle<T>(c, mg, l + 1, C.bw, C.xw, halt);
+    launch_axpby<T>(C.xa, T(1), C.xw, T(1), C.g.ndof(), c.st);
+    c.launches++;
+  }
   launch_prolong_add<T>(C.g, C.xa, V.g, V.m, cur, halt, c.st);
   c.launches++;
   bool fused = false;
@@ -747,6 +763,7 @@ void configure_mg(MG<T>& mg, const Problem& P, const hexa_solve_params& prm) {
   mg.nu1 = prm.pre_smooth > 0 ? prm.pre_smooth : 1;
   mg.nu2 = prm.post_smooth >= 0 ? prm.post_smooth : 2;
   mg.citers = prm.coarse_iters >= 0 ? prm.coarse_iters : 30;
+  mg.gamma = prm.mg_cycle == 2 ? 2 : 1;
   mg.set_chebyshev(lmax, std::max(mg.nu1, mg.nu2) + 1, prm.cheb_ratio > 1 ? prm.cheb_ratio : 10.0);
   mg.ke.assign(576, 0.0);
   if (canonical_stiffness(P.dx, P.dy, P.dz, P.nu, mg.ke.data()) != 0) mg.ke.clear();
