@@ -97,14 +97,21 @@ __device__ __forceinline__ void load_corners(const Grid& g, const ColumnAddr<IX>
   }
 }
 
-// 1/d for the smoothers: in FP32 the hardware reciprocal approximation
-// (rcp.approx, about 1 ulp; the diagonal only scales a smoothing step); in
-// FP64 a float seed and two Newton steps (relative error far below 1e-15).
-// Both are deterministic.
+// 1/d for the smoothers: correctly rounded in FP32; in FP64 a float seed and
+// two Newton steps (relative error far below 1e-15).  Both are deterministic.
+// The FP32 hardware approximation (rcp.approx, HEXA_OP_RCP_APPROX=1) measured
+// slower in the Chebyshev step on the 384x192x192 grid (311 us against 251 us).
+#ifndef HEXA_OP_RCP_APPROX
+#define HEXA_OP_RCP_APPROX 0
+#endif
 __device__ __forceinline__ float recip(float d) {
+#if HEXA_OP_RCP_APPROX
   float r;
   asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(d));
   return r;
+#else
+  return __frcp_rn(d);
+#endif
 }
 __device__ __forceinline__ double recip(double d) {
   double r = (double)__frcp_rn((float)d);
@@ -490,9 +497,11 @@ __device__ __forceinline__ void op_item(const A& a, int tx, int ty, int chunk,
 }
 
 // Whether every corner of every column of tile (tx, ty) lies inside the grid
-// in x and y (the predicate-free form of the item applies).
+// in x and y (the predicate-free form of the item applies).  Off by default:
+// with both item forms inlined the kernels spill, and on the 384x192x192 grid
+// the residual gained 6 % while the plain apply lost 18 %.
 #ifndef HEXA_OP_INTERIOR
-#define HEXA_OP_INTERIOR 1
+#define HEXA_OP_INTERIOR 0
 #endif
 template <int TYW>
 __device__ __forceinline__ bool tile_interior(const Grid& g, int tx, int ty) {
