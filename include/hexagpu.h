@@ -245,6 +245,18 @@ int hexa_filter_batch(hexa_ctx* ctx, int32_t count, const hexa_grid* grids, cons
                       double radius, double tol, int32_t max_iter, int32_t quirk, int32_t precision,
                       double* const* rho_out, hexa_filter_stats* stats);
 
+/* ---- (f) stress post-processing ---------------------------------------- */
+/* Replaces Stress.compute_stress_field (src/Core/Stress.jl:286-339, kernel
+ * :159-285): per element at its centre the stress of E_loc = E * density,
+ * the principal stresses (descending) with the directions of the largest and
+ * smallest, von Mises, the L1 norm of the principal stresses and, when voigt
+ * is not NULL, the Voigt stress (xx, yy, zz, xy, yz, xz).  u is the FP64
+ * solution (3*nNodes), rounded to Float32 as the reference does; outputs are
+ * Float32, element-major (principal[3e+i], voigt[6e+i], dir_*[3e+i]);
+ * elements with density < 1e-6 get zeros.  Arrays host or device. */
+int hexa_stress_field(hexa_ctx* ctx, const hexa_grid* g, const double* u, const float* density, float E, float nu,
+                      float* principal, float* vonmises, float* voigt, float* l1, float* dir_max, float* dir_min);
+
 /* ---- (e) SIMP sensitivities and OC update ------------------------------ */
 /* dc_e = -penal * rho_e^(penal-1) * (E0 - Emin) * u_e^T K0 u_e and
  * compliance = sum_e (Emin + rho_e^penal (E0-Emin)) u_e^T K0 u_e. */

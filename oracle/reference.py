@@ -457,3 +457,140 @@ def wall(fn, *a, **k):
     t = time.perf_counter()
     r = fn(*a, **k)
     return r, time.perf_counter() - t
+
+
+# ------------------------------------------------------------------- stress
+def _jacobi_rotate(spp, sqq, spq, spr, sqr, v, p, q):
+    """One rotation of Stress.jl:89-140 on arrays of elements (float32), in place."""
+    f32 = np.float32
+    h = spq.copy()
+    g = f32(100.0) * np.abs(h)
+    act = (np.abs(spp) + g != np.abs(spp)) | (np.abs(sqq) + g != np.abs(sqq))
+    with np.errstate(divide="ignore", invalid="ignore"):
+        theta = f32(0.5) * (sqq - spp) / h
+        t = f32(1.0) / (np.abs(theta) + np.sqrt(theta * theta + f32(1.0)))
+    t = np.where(theta < 0, -t, t).astype(f32)
+    c = (f32(1.0) / np.sqrt(t * t + f32(1.0))).astype(f32)
+    s = (t * c).astype(f32)
+    tau = (s / (f32(1.0) + c)).astype(f32)
+    spp_n = spp - t * spq
+    sqq_n = sqq + t * spq
+    tmp = spr.copy()
+    spr_n = spr - s * (sqr + tau * spr)
+    sqr_n = sqr + s * (tmp - tau * sqr)
+    for arr, new in ((spp, spp_n), (sqq, sqq_n), (spr, spr_n), (sqr, sqr_n)):
+        arr[act] = new[act]
+    spq[act] = 0.0
+    for r in range(3):
+        vp = v[r][p].copy()
+        vp_n = vp - s * (v[r][q] + tau * vp)
+        vq_n = v[r][q] + s * (vp - tau * v[r][q])
+        v[r][p][act] = vp_n[act]
+        v[r][q][act] = vq_n[act]
+
+
+def stress_field(g: Grid, u, density, E, nu):
+    """Stress.stress_kernel! (Stress.jl:159-285) restated in numpy, Float32, all
+    elements at once: centre-point strain/stress with E_loc = E*density, von
+    Mises, principal stresses by 12 cyclic Jacobi sweeps (sorted descending),
+    directions of the largest/smallest, L1 norm, Voigt stress.  Element-major
+    arrays (principal[e, i])."""
+    f32 = np.float32
+    ne = g.nelem
+    e = np.arange(ne)
+    i = e % g.nx
+    j = (e // g.nx) % g.ny
+    k = e // (g.nx * g.ny)
+    NX, NY = g.nx + 1, g.ny + 1
+    dens = np.asarray(density, dtype=f32)
+    uf = np.asarray(u).astype(f32)
+    DI = [0, 1, 1, 0, 0, 1, 1, 0]
+    DJ = [0, 0, 1, 1, 0, 0, 1, 1]
+    DK = [0, 0, 0, 0, 1, 1, 1, 1]
+    dx, dy, dz = f32(g.dx), f32(g.dy), f32(g.dz)
+    J = [[np.zeros(ne, f32) for _ in range(3)] for _ in range(3)]
+    for a in range(8):
+        x = (i + DI[a]).astype(f32) * dx
+        y = (j + DJ[a]).astype(f32) * dy
+        z = (k + DK[a]).astype(f32) * dz
+        w = [f32(0.125) if DI[a] else f32(-0.125), f32(0.125) if DJ[a] else f32(-0.125),
+             f32(0.125) if DK[a] else f32(-0.125)]
+        for r in range(3):
+            J[r][0] += w[r] * x
+            J[r][1] += w[r] * y
+            J[r][2] += w[r] * z
+    (j11, j12, j13), (j21, j22, j23), (j31, j32, j33) = J
+    det = j11 * (j22 * j33 - j23 * j32) - j12 * (j21 * j33 - j23 * j31) + j13 * (j21 * j32 - j22 * j31)
+    det = np.where(det <= f32(1e-12), f32(1.0), det).astype(f32)
+    idt = f32(1.0) / det
+    A = [[(j22 * j33 - j23 * j32) * idt, -(j12 * j33 - j13 * j32) * idt, (j12 * j23 - j13 * j22) * idt],
+         [-(j21 * j33 - j23 * j31) * idt, (j11 * j33 - j13 * j31) * idt, -(j11 * j23 - j13 * j21) * idt],
+         [(j21 * j32 - j22 * j31) * idt, -(j11 * j32 - j12 * j31) * idt, (j11 * j22 - j12 * j21) * idt]]
+    exx, eyy, ezz, gxy, gyz, gxz = (np.zeros(ne, f32) for _ in range(6))
+    for a in range(8):
+        n = (i + DI[a]) + NX * ((j + DJ[a]) + NY * (k + DK[a]))
+        ux, uy, uz = uf[3 * n], uf[3 * n + 1], uf[3 * n + 2]
+        w = [f32(0.125) if DI[a] else f32(-0.125), f32(0.125) if DJ[a] else f32(-0.125),
+             f32(0.125) if DK[a] else f32(-0.125)]
+        ddx = w[0] * A[0][0] + w[1] * A[1][0] + w[2] * A[2][0]
+        ddy = w[0] * A[0][1] + w[1] * A[1][1] + w[2] * A[2][1]
+        ddz = w[0] * A[0][2] + w[1] * A[1][2] + w[2] * A[2][2]
+        exx += ddx * ux
+        eyy += ddy * uy
+        ezz += ddz * uz
+        gxy += ddy * ux + ddx * uy
+        gyz += ddz * uy + ddy * uz
+        gxz += ddz * ux + ddx * uz
+    E, nu = f32(E), f32(nu)
+    fact = (E * dens) / ((f32(1.0) + nu) * (f32(1.0) - f32(2.0) * nu))
+    c1, c2, c3 = (f32(1.0) - nu) * fact, nu * fact, (f32(0.5) - nu) * fact
+    sxx = c1 * exx + c2 * eyy + c2 * ezz
+    syy = c2 * exx + c1 * eyy + c2 * ezz
+    szz = c2 * exx + c2 * eyy + c1 * ezz
+    sxy, syz, sxz = c3 * gxy, c3 * gyz, c3 * gxz
+    voigt = np.stack([sxx, syy, szz, sxy, syz, sxz], axis=1)
+    vm = np.sqrt(np.maximum(f32(0.0), f32(0.5) * ((sxx - syy) ** 2 + (syy - szz) ** 2 + (szz - sxx) ** 2)
+                            + f32(3.0) * (sxy ** 2 + syz ** 2 + sxz ** 2)))
+    s11, s22, s33, s12, s23, s13 = (a.astype(f32).copy() for a in (sxx, syy, szz, sxy, syz, sxz))
+    v = [[np.full(ne, f32(1.0 if r == c else 0.0)) for c in range(3)] for r in range(3)]
+    done = np.zeros(ne, bool)
+    for _ in range(12):
+        done |= np.maximum(np.abs(s12), np.maximum(np.abs(s23), np.abs(s13))) < f32(1e-9)
+        live = ~done
+        if not live.any():
+            break
+        sub = [a[live] for a in (s11, s22, s33, s12, s23, s13)]
+        vs = [[v[r][c][live] for c in range(3)] for r in range(3)]
+        a11, a22, a33, a12, a23, a13 = sub
+        _jacobi_rotate(a11, a22, a12, a13, a23, vs, 0, 1)
+        _jacobi_rotate(a11, a33, a13, a12, a23, vs, 0, 2)
+        _jacobi_rotate(a22, a33, a23, a12, a13, vs, 1, 2)
+        for arr, new in zip((s11, s22, s33, s12, s23, s13), (a11, a22, a33, a12, a23, a13)):
+            arr[live] = new
+        for r in range(3):
+            for c in range(3):
+                v[r][c][live] = vs[r][c]
+
+    def swap(ma, mb, ca, cb):
+        m = ma < mb
+        ta = ma.copy()
+        ma[m] = mb[m]
+        mb[m] = ta[m]
+        for r in range(3):
+            t = v[r][ca].copy()
+            v[r][ca][m] = v[r][cb][m]
+            v[r][cb][m] = t[m]
+    swap(s11, s22, 0, 1)
+    swap(s22, s33, 1, 2)
+    swap(s11, s22, 0, 1)
+    principal = np.stack([s11, s22, s33], axis=1)
+    dmax = np.stack([v[0][0], v[1][0], v[2][0]], axis=1)
+    dmin = np.stack([v[0][2], v[1][2], v[2][2]], axis=1)
+    l1 = np.abs(s11) + np.abs(s22) + np.abs(s33)
+    zero = dens < f32(1e-6)
+    for arr in (principal, dmax, dmin, voigt):
+        arr[zero] = 0.0
+    for arr in (vm, l1):
+        arr[zero] = 0.0
+    return dict(principal=principal, vonmises=vm.astype(f32), voigt=voigt.astype(f32), l1=l1.astype(f32),
+                dir_max=dmax, dir_min=dmin)

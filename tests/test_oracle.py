@@ -115,3 +115,23 @@ def test_cpu_baseline_skips_soft_elements(oracle):
     dens2[:4] = 0.0
     u2, *_ = oracle.cpu_matrix_free_cg(g, 1.0, dens2, f, fixed, max_iter=5, tol=1e-30, nthreads=1)
     assert np.array_equal(u1, u2)
+
+
+def test_stress_oracle_principal_stresses_are_eigenvalues(oracle, rng):
+    g = oracle.Grid(5, 4, 3, 1.0, 2.0, 0.5)
+    u = 1e-2 * rng.standard_normal(g.ndof)
+    dens = rng.uniform(0.0, 1.0, g.nelem).astype(np.float32)
+    out = oracle.stress_field(g, u, dens, 1.0, 0.3)
+    v = out["voigt"].astype(np.float64)
+    S = np.zeros((g.nelem, 3, 3))
+    S[:, 0, 0], S[:, 1, 1], S[:, 2, 2] = v[:, 0], v[:, 1], v[:, 2]
+    S[:, 0, 1] = S[:, 1, 0] = v[:, 3]
+    S[:, 1, 2] = S[:, 2, 1] = v[:, 4]
+    S[:, 0, 2] = S[:, 2, 0] = v[:, 5]
+    w, vec = np.linalg.eigh(S)
+    assert np.abs(out["principal"] - w[:, ::-1]).max() <= 1e-5 * np.abs(w).max()
+    # the directions are unit eigenvectors of the largest and smallest
+    for key, col in (("dir_max", 2), ("dir_min", 0)):
+        d = out[key].astype(np.float64)
+        assert np.allclose(np.linalg.norm(d, axis=1), 1.0, atol=1e-5)
+        assert np.all(np.abs(np.sum(d * vec[:, :, col], axis=1)) >= 1 - 1e-4)

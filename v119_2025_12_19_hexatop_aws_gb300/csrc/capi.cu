@@ -686,6 +686,38 @@ int hexa_filter_batch(hexa_ctx* h, int32_t count, const hexa_grid* grids, const 
   return rc;
 }
 
+int hexa_stress_field(hexa_ctx* h, const hexa_grid* g, const double* u, const float* density, float E, float nu,
+                      float* principal, float* vonmises, float* voigt, float* l1, float* dir_max, float* dir_min) {
+  if (!h) return HEXA_ERR_ARG;
+  if (!valid_grid(g) || !u || !density || !principal || !vonmises || !l1 || !dir_max || !dir_min)
+    return set_err(h, HEXA_ERR_ARG, "invalid grid or null array");
+  Ctx& c = h->c;
+  c.err.clear();
+  cudaSetDevice(c.device);
+  const Grid G = make_grid(g->nx, g->ny, g->nz);
+  const long long ne = G.nelem();
+  const double* ud = stage_in<double>(c, u, G.ndof(), "st_u");
+  const float* rd = stage_in<float>(c, density, ne, "st_rho");
+  float* pd = out_buf<float>(c, principal, 3 * ne, "st_p");
+  float* vd = out_buf<float>(c, vonmises, ne, "st_vm");
+  float* wd = voigt ? out_buf<float>(c, voigt, 6 * ne, "st_w") : nullptr;
+  float* ld = out_buf<float>(c, l1, ne, "st_l1");
+  float* xd = out_buf<float>(c, dir_max, 3 * ne, "st_dmax");
+  float* nd = out_buf<float>(c, dir_min, 3 * ne, "st_dmin");
+  if (!ud || !rd || !pd || !vd || (voigt && !wd) || !ld || !xd || !nd) return set_err(h, HEXA_ERR_NOMEM, c.err);
+  launch_stress<double>(G, ud, rd, E, nu, (float)g->dx, (float)g->dy, (float)g->dz, voigt ? 1 : 0, pd, vd, wd, ld, xd,
+                        nd, c.st);
+  c.launches++;
+  stage_out<float>(c, principal, pd, 3 * ne);
+  stage_out<float>(c, vonmises, vd, ne);
+  if (voigt) stage_out<float>(c, voigt, wd, 6 * ne);
+  stage_out<float>(c, l1, ld, ne);
+  stage_out<float>(c, dir_max, xd, 3 * ne);
+  stage_out<float>(c, dir_min, nd, 3 * ne);
+  if (cudaStreamSynchronize(c.st) != cudaSuccess || !c.cuda_ok("stress")) return set_err(h, HEXA_ERR_CUDA, c.err);
+  return HEXA_OK;
+}
+
 int hexa_simp_factors(hexa_ctx* h, int64_t n, const double* rho, double Emin, double E0, double penal,
                       double* factor_out) {
   if (!h) return HEXA_ERR_ARG;

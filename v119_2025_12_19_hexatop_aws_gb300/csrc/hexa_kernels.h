@@ -154,6 +154,12 @@ void launch_oc_apply(const double* x, const double* dc, const double* dv, long l
                      double move, double* xout, cudaStream_t st);
 
 
+// ---- stress post-processing (stress.cu) ----------------------------------
+template <typename TU>
+void launch_stress(const Grid& g, const TU* u, const float* density, float E, float nu, float dx, float dy, float dz,
+                   int save_voigt, float* principal, float* vonmises, float* voigt, float* l1, float* dmax,
+                   float* dmin, cudaStream_t st);
+
 // ---- block PCG over k <= kMaxBlockCols columns (block.cu) ----------------
 constexpr int kMaxBlockCols = 16;
 constexpr int kBlockRedBlocks = 608;  // grid of the reducing block passes

@@ -108,3 +108,21 @@ def run_simp(S: SimpSetup, x0: np.ndarray, n_iter: int = 10, keep=True, ctx=None
                                xphys.copy() if keep else None))
         x, _ = oc_update(x, dcx, dv, S.volfrac, S.move, ctx=ctx)
     return hist
+
+
+def stress_field(grid, u, density, *, E=1.0, nu=0.3, voigt=True, ctx=None):
+    """Stress.compute_stress_field (Stress.jl:286-339) on the GPU: per element
+    principal stresses (descending), von Mises, Voigt stress, L1 norm of the
+    principal stresses and the directions of the largest and smallest.
+    Returns a dict of float32 arrays, element-major (principal[e, i])."""
+    ctx = ctx or context()
+    ne = grid.nx * grid.ny * grid.nz
+    out = dict(principal=np.empty((ne, 3), np.float32), vonmises=np.empty(ne, np.float32),
+               voigt=np.empty((ne, 6), np.float32) if voigt else None, l1=np.empty(ne, np.float32),
+               dir_max=np.empty((ne, 3), np.float32), dir_min=np.empty((ne, 3), np.float32))
+    rc = ctx.lib.hexa_stress_field(ctx.h, C.byref(grid), _lib.ptr(np.ascontiguousarray(u, dtype=np.float64)),
+                                   _lib.ptr(np.ascontiguousarray(density, dtype=np.float32)), float(E), float(nu),
+                                   _lib.ptr(out["principal"]), _lib.ptr(out["vonmises"]), _lib.ptr(out["voigt"]),
+                                   _lib.ptr(out["l1"]), _lib.ptr(out["dir_max"]), _lib.ptr(out["dir_min"]))
+    ctx.check(rc, allow=(_lib.HEXA_OK,))
+    return out
