@@ -1,0 +1,82 @@
+"""The on-disk formats either side of the loop (host code): the HEXA v2 web
+binary (Postprocessing.jl:370-471) and the .vti result file
+(ExportVTK.jl:16-110), written and parsed back byte by byte."""
+import struct
+
+import numpy as np
+
+from v119_2025_12_19_hexatop_aws_gb300 import _lib
+from v119_2025_12_19_hexatop_aws_gb300.exporters import (export_indices, read_hexa_binary, read_vti_arrays,
+                                                         signed_l1, write_hexa_binary, write_vti)
+
+
+def test_export_indices_threshold_and_fractional_stride():
+    dens = np.array([0.1, 0.6, 0.7, 0.2, 0.9, 0.95, 0.5, 0.8, 0.99, 0.51, 0.52, 0.3], dtype=np.float32)
+    act = np.nonzero(dens >= 0.5)[0]  # 9 cells
+    assert np.array_equal(export_indices(dens, 0.5), act)
+    # 9 active, at most 4: stride 2.25 -> 1-based picks 1, 3.25, 5.5, 7.75 -> floor 1, 3, 5, 7
+    assert np.array_equal(export_indices(dens, 0.5, 4), act[[0, 2, 4, 6]])
+
+
+def test_signed_l1_takes_the_sign_of_the_largest_principal():
+    p = np.array([[3.0, 1.0, -5.0], [4.0, 0.0, -4.0], [-1.0, -2.0, -0.5]], dtype=np.float32)
+    l1 = np.abs(p).sum(axis=1).astype(np.float32)
+    assert np.array_equal(signed_l1(l1, p), np.array([-9.0, 8.0, -3.5], dtype=np.float32))
+
+
+def test_hexa_binary_layout_and_round_trip(tmp_path):
+    grid = _lib.make_grid(4, 3, 2, 1.0, 2.0, 0.5)
+    ne = 24
+    rng = np.random.default_rng(3)
+    dens = rng.uniform(0, 1, ne).astype(np.float32)
+    principal = rng.standard_normal((ne, 3)).astype(np.float32)
+    l1 = np.abs(principal).sum(axis=1).astype(np.float32)
+    cfg = {"geometry": {"hole": {"type": "sphere", "stiffness_ratio": 0.0}}, "external_forces": [{"F": [0, 0, -1]}],
+           "boundary_conditions": [{"location": [0, ":", ":"]}], "optimization_parameters": {"volfrac": 0.3}}
+    path = tmp_path / "iter.bin"
+    n = write_hexa_binary(path, grid, dens, l1, principal, iteration=7, radius=1.5, threshold=0.3, config=cfg)
+    idx = np.nonzero(dens >= 0.3)[0]
+    assert n == idx.size
+    raw = path.read_bytes()
+    magic, ver, it, rad, thr, cnt, dx, dy, dz = struct.unpack_from("<IIiffIfff", raw, 0)
+    assert (magic, ver, it, cnt) == (0x48455841, 2, 7, idx.size)
+    assert raw[:4] == b"AXEH"  # the UInt32 magic as a little-endian file writes it
+    assert (rad, thr, dx, dy, dz) == (1.5, np.float32(0.3), 1.0, 2.0, 0.5)
+    back = read_hexa_binary(path)
+    i, j, k = idx % 4, (idx // 4) % 3, idx // 12
+    assert np.allclose(back["centroids"], np.stack([(i + 0.5) * 1.0, (j + 0.5) * 2.0, (k + 0.5) * 0.5], 1), atol=1e-6)
+    assert np.array_equal(back["density"], dens[idx])
+    assert np.array_equal(back["signed_l1"], signed_l1(l1[idx], principal[idx]))
+    meta = back["meta"]
+    assert meta["iteration"] == 7 and meta["loads"] == cfg["external_forces"] and meta["bcs"] == cfg["boundary_conditions"]
+    assert meta["settings"] == {"volfrac": 0.3} and meta["geometry"]["hole"]["action"] == "remove"
+    assert len(raw) == 36 + 20 * idx.size + 4 + struct.unpack_from("<I", raw, 36 + 20 * idx.size)[0]
+
+
+def test_hexa_binary_writes_nothing_without_active_cells(tmp_path):
+    grid = _lib.make_grid(2, 2, 2)
+    path = tmp_path / "none.bin"
+    n = write_hexa_binary(path, grid, np.zeros(8, np.float32), np.zeros(8, np.float32), np.zeros((8, 3), np.float32),
+                          iteration=1, radius=1.0, threshold=0.5)
+    assert n == 0 and not path.exists()
+
+
+def test_vti_header_and_arrays(tmp_path):
+    rng = np.random.default_rng(4)
+    dims = (3, 2, 2)
+    n = 12
+    dens, l1, vm = (rng.uniform(0, 1, n).astype(np.float32) for _ in range(3))
+    pv, dmax, dmin = (rng.standard_normal((n, 3)).astype(np.float32) for _ in range(3))
+    for vectors in ("no", "yes"):
+        path = write_vti(tmp_path / f"res_{vectors}", dims, (1.0, 2.0, 0.5), (0.0, 0.0, 0.0), dens, l1, vm, pv, dmax,
+                         dmin, config={"output_settings": {"save_principal_stress_vectors": vectors}})
+        text = open(path, "rb").read().split(b"<AppendedData")[0].decode()
+        assert '<ImageData WholeExtent="0 3 0 2 0 2" Origin="0.0 0.0 0.0" Spacing="1.0 2.0 0.5">' in text
+        assert 'Name="L1_Stress" format="appended" offset="52"' in text  # 4 + 12 * 4 after Density
+        arrs = read_vti_arrays(path)
+        assert np.array_equal(arrs["Density"], dens) and np.array_equal(arrs["VonMises"], vm)
+        if vectors == "yes":
+            assert np.array_equal(arrs["PrincipalValues"], pv) and np.array_equal(arrs["MinPrincipalDirection"], dmin)
+        else:
+            assert "PrincipalValues" not in arrs
+        assert open(path, "rb").read().endswith(b"\n  </AppendedData>\n</VTKFile>\n")
