@@ -257,6 +257,17 @@ int hexa_filter_batch(hexa_ctx* ctx, int32_t count, const hexa_grid* grids, cons
 int hexa_stress_field(hexa_ctx* ctx, const hexa_grid* g, const double* u, const float* density, float E, float nu,
                       float* principal, float* vonmises, float* voigt, float* l1, float* dir_max, float* dir_min);
 
+/* Replaces the field mapping of MeshRefiner.refine_mesh_and_fields
+ * (src/Mesh/MeshRefiner.jl:188-240): the old cell-centred density (old grid
+ * old_g, element order x fastest) interpolated trilinearly at the centroids
+ * of the new grid new_g spanning the same box (lengths lx, ly, lz), projected
+ * (> 0.4 -> 1, < 0.2 -> 1e-4) when projection is 1 ("hard" update); alpha
+ * (nullable) is carried by nearest lower-corner cell into new_alpha
+ * (nullable).  Float32 throughout; arrays host or device. */
+int hexa_remap_fields(hexa_ctx* ctx, const hexa_grid* old_g, const hexa_grid* new_g, double lx, double ly, double lz,
+                      const float* density, const float* alpha, int32_t projection, float* new_density,
+                      float* new_alpha);
+
 /* ---- (e) SIMP sensitivities and OC update ------------------------------ */
 /* dc_e = -penal * rho_e^(penal-1) * (E0 - Emin) * u_e^T K0 u_e and
  * compliance = sum_e (Emin + rho_e^penal (E0-Emin)) u_e^T K0 u_e. */

@@ -594,3 +594,50 @@ def stress_field(g: Grid, u, density, E, nu):
         arr[zero] = 0.0
     return dict(principal=principal, vonmises=vm.astype(f32), voigt=voigt.astype(f32), l1=l1.astype(f32),
                 dir_max=dmax, dir_min=dmin)
+
+
+# -------------------------------------------------------------- refinement
+def remap_fields(old, new_dims, new_h, lengths, density, alpha=None, projection=True):
+    """MeshRefiner.jl:188-240 restated in numpy (Float32): trilinear transfer
+    of the cell-centred density to the new grid's centroids, projected in the
+    "hard" update, and the lower-corner cell's alpha."""
+    f32 = np.float32
+    onx, ony, onz = old
+    nnx, nny, nnz = new_dims
+    e = np.arange(nnx * nny * nnz, dtype=np.int64)
+    ix = e % nnx + 1
+    iy = (e // nnx) % nny + 1
+    iz = e // (nnx * nny) + 1
+    cx = (ix.astype(f32) - f32(0.5)) * f32(new_h[0])
+    cy = (iy.astype(f32) - f32(0.5)) * f32(new_h[1])
+    cz = (iz.astype(f32) - f32(0.5)) * f32(new_h[2])
+    u = np.clip((cx / f32(lengths[0])) * f32(onx), f32(0.5), f32(onx) - f32(0.5)).astype(f32)
+    v = np.clip((cy / f32(lengths[1])) * f32(ony), f32(0.5), f32(ony) - f32(0.5)).astype(f32)
+    w = np.clip((cz / f32(lengths[2])) * f32(onz), f32(0.5), f32(onz) - f32(0.5)).astype(f32)
+    u0 = np.floor(u - f32(0.5)).astype(np.int64)
+    v0 = np.floor(v - f32(0.5)).astype(np.int64)
+    w0 = np.floor(w - f32(0.5)).astype(np.int64)
+    tx = np.clip((u - f32(0.5)) - u0.astype(f32), 0, 1).astype(f32)
+    ty = np.clip((v - f32(0.5)) - v0.astype(f32), 0, 1).astype(f32)
+    tz = np.clip((w - f32(0.5)) - w0.astype(f32), 0, 1).astype(f32)
+    i0, i1 = np.clip(u0, 0, onx - 1), np.clip(u0 + 1, 0, onx - 1)
+    j0, j1 = np.clip(v0, 0, ony - 1), np.clip(v0 + 1, 0, ony - 1)
+    k0, k1 = np.clip(w0, 0, onz - 1), np.clip(w0 + 1, 0, onz - 1)
+    d = np.asarray(density, dtype=f32)
+
+    def at(i, j, k):
+        return d[i + onx * j + onx * ony * k]
+    one = f32(1.0)
+    c00 = at(i0, j0, k0) * (one - tx) + at(i1, j0, k0) * tx
+    c10 = at(i0, j1, k0) * (one - tx) + at(i1, j1, k0) * tx
+    c01 = at(i0, j0, k1) * (one - tx) + at(i1, j0, k1) * tx
+    c11 = at(i0, j1, k1) * (one - tx) + at(i1, j1, k1) * tx
+    c0 = c00 * (one - ty) + c10 * ty
+    c1 = c01 * (one - ty) + c11 * ty
+    val = (c0 * (one - tz) + c1 * tz).astype(f32)
+    raw = val.copy()
+    if projection:
+        val = np.where(val > f32(0.4), f32(1.0), np.where(val < f32(0.2), f32(0.0001), val)).astype(f32)
+    na = None if alpha is None else np.asarray(alpha, dtype=f32)[i0 + onx * j0 + onx * ony * k0]
+    return val, na, raw
+

@@ -101,6 +101,7 @@ SIGNATURES = {
     "hexa_filter_batch": (I32, [P, I32, C.POINTER(Grid), C.POINTER(P), D, D, I32, I32, I32, C.POINTER(P),
                                 C.POINTER(FilterStats)]),
     "hexa_filter_noalloc": (I32, [C.POINTER(Grid), P, D, D, I32, I32, P, P, C.POINTER(FilterStats)]),
+    "hexa_remap_fields": (I32, [P, C.POINTER(Grid), C.POINTER(Grid), D, D, D, P, P, I32, P, P]),
     "hexa_stress_field": (I32, [P, C.POINTER(Grid), P, P, C.c_float, C.c_float, P, P, P, P, P, P]),
     "hexa_sensitivities": (I32, [P, C.POINTER(Grid), D, P, P, D, D, D, P, C.POINTER(D)]),
     "hexa_simp_factors": (I32, [P, I64, P, D, D, D, P]),

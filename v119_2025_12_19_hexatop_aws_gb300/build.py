@@ -19,7 +19,7 @@ CSRC = PKG / "csrc"
 BUILD = PKG / "_build"
 LIB = PKG / "libhexagpu.so"
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
-SOURCES = ["op.cu", "vec.cu", "mg.cu", "helm.cu", "topo.cu", "block.cu", "batch.cu", "stress.cu", "solver.cu", "capi.cu", "noalloc.cu", "element.cpp"]
+SOURCES = ["op.cu", "vec.cu", "mg.cu", "helm.cu", "topo.cu", "block.cu", "batch.cu", "stress.cu", "remap.cu", "solver.cu", "capi.cu", "noalloc.cu", "element.cpp"]
 
 
 def nvcc() -> str:

@@ -718,6 +718,30 @@ int hexa_stress_field(hexa_ctx* h, const hexa_grid* g, const double* u, const fl
   return HEXA_OK;
 }
 
+int hexa_remap_fields(hexa_ctx* h, const hexa_grid* og, const hexa_grid* ng, double lx, double ly, double lz,
+                      const float* density, const float* alpha, int32_t projection, float* new_density,
+                      float* new_alpha) {
+  if (!h) return HEXA_ERR_ARG;
+  if (!valid_grid(og) || !valid_grid(ng) || !density || !new_density || !(lx > 0 && ly > 0 && lz > 0))
+    return set_err(h, HEXA_ERR_ARG, "invalid grids, lengths or null array");
+  Ctx& c = h->c;
+  c.err.clear();
+  cudaSetDevice(c.device);
+  const long long no = (long long)og->nx * og->ny * og->nz, nn = (long long)ng->nx * ng->ny * ng->nz;
+  const float* dd = stage_in<float>(c, density, no, "rm_d");
+  const float* ad = alpha ? stage_in<float>(c, alpha, no, "rm_a") : nullptr;
+  float* ndd = out_buf<float>(c, new_density, nn, "rm_nd");
+  float* nad = new_alpha ? out_buf<float>(c, new_alpha, nn, "rm_na") : nullptr;
+  if (!dd || (alpha && !ad) || !ndd || (new_alpha && !nad)) return set_err(h, HEXA_ERR_NOMEM, c.err);
+  launch_remap(og->nx, og->ny, og->nz, ng->nx, ng->ny, ng->nz, (float)ng->dx, (float)ng->dy, (float)ng->dz, (float)lx,
+               (float)ly, (float)lz, projection ? 1 : 0, dd, ad, ndd, nad, c.st);
+  c.launches++;
+  stage_out<float>(c, new_density, ndd, nn);
+  if (new_alpha) stage_out<float>(c, new_alpha, nad, nn);
+  if (cudaStreamSynchronize(c.st) != cudaSuccess || !c.cuda_ok("remap")) return set_err(h, HEXA_ERR_CUDA, c.err);
+  return HEXA_OK;
+}
+
 int hexa_simp_factors(hexa_ctx* h, int64_t n, const double* rho, double Emin, double E0, double penal,
                       double* factor_out) {
   if (!h) return HEXA_ERR_ARG;

@@ -160,6 +160,11 @@ void launch_stress(const Grid& g, const TU* u, const float* density, float E, fl
                    int save_voigt, float* principal, float* vonmises, float* voigt, float* l1, float* dmax,
                    float* dmin, cudaStream_t st);
 
+// ---- density transfer onto a refined grid (remap.cu) ----------------------
+void launch_remap(int onx, int ony, int onz, int nnx, int nny, int nnz, float ndx, float ndy, float ndz, float lx,
+                  float ly, float lz, int projection, const float* dens, const float* alpha, float* nd, float* na,
+                  cudaStream_t st);
+
 // ---- block PCG over k <= kMaxBlockCols columns (block.cu) ----------------
 constexpr int kMaxBlockCols = 16;
 constexpr int kBlockRedBlocks = 608;  // grid of the reducing block passes
