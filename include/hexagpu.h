@@ -268,6 +268,62 @@ int hexa_remap_fields(hexa_ctx* ctx, const hexa_grid* old_g, const hexa_grid* ne
                       const float* density, const float* alpha, int32_t projection, float* new_density,
                       float* new_alpha);
 
+/* ---- density update between solves (TopOpt.jl:211-482) ---------------- */
+/* The scalars update_density! reads from its arguments and its config;
+ * defaults are the reference's get(...) defaults. */
+typedef struct hexa_density_update_params {
+  float E;                                 /* Young's modulus (argument E) */
+  float l1_stress_allowable;               /* argument l1_stress_allowable */
+  int32_t iter;                            /* argument iter */
+  int32_t number_of_iterations;            /* argument number_of_iterations */
+  float min_density;                       /* argument min_density (1e-3) */
+  float max_density;                       /* argument max_density (1.0) */
+  float max_domain_dim;                    /* geometry.max_domain_dim (Float32) */
+  float filter_R_init_perc;                /* optimization_parameters..., 0 */
+  float filter_R_interm_perc;              /* 0 */
+  float filter_R_final_perc;               /* 0 */
+  float filter_R_interm_iter_perc;         /* 50 */
+  float minimum_filter_radius_as_elements; /* 2.5 */
+  float filter_tolerance;                  /* solver_parameters.filter_tolerance, 1e-5 */
+  float final_density_threshold;           /* 0.95 */
+  float max_culling_ratio;                 /* 0.1 */
+  int32_t hard_update;                     /* density_update_method == "hard" (default "soft") */
+  int32_t filter_max_iter;                 /* 200, as apply_gpu_filter! */
+  int32_t filter_precision;                /* HEXA_PREC_FP32 (the reference's Float32 filter) or FP64 */
+} hexa_density_update_params;
+
+/* update_density!'s return tuple (mean_change, R_length, current_threshold,
+ * filter_time, filter_iters, filter_res) and the counts behind it. */
+typedef struct hexa_density_update_stats {
+  int32_t status;              /* 0 updated; 1 skipped: NaN in the stress field (TopOpt.jl:230-236) */
+  int32_t filter_used;         /* R_effective > 1e-4 */
+  int32_t filter_nan_fallback; /* the filtered field held a NaN: the proposal was used (TopOpt.jl:360-363) */
+  int32_t filter_iters;
+  float mean_change;
+  float R_length;
+  float current_threshold;
+  float R_effective;           /* R_length / 2.5, the radius given to the filter */
+  double filter_time;          /* seconds of filter PCG (device time) */
+  double filter_res;
+  int64_t active_count;        /* after the clamp; protected elements by their original density */
+  int64_t candidates;          /* unprotected elements with min_density < rho < current_threshold */
+  int64_t culled;              /* candidates set to min_density */
+} hexa_density_update_stats;
+
+void hexa_default_density_update_params(hexa_density_update_params* p);
+
+/* Replaces TopologyOptimization.update_density!(density, l1_stress_norm_field,
+ * protected_elements_mask, E, l1_stress_allowable, iter,
+ * number_of_iterations, original_density, min_density, max_density, config,
+ * elements) (src/Optimization/TopOpt.jl:211-482) on the structured grid g:
+ * density (Float32, in/out) is updated in place, the filter is this
+ * library's (the GPU path of TopOpt.jl:310-327).  protected_mask (one byte
+ * per element, nonzero = protected) may be NULL (none protected); arrays host
+ * or device; at most 2^32 - 1 elements (HEXA_ERR_TOO_LARGE beyond). */
+int hexa_update_density(hexa_ctx* ctx, const hexa_grid* g, float* density, const float* l1_stress,
+                        const uint8_t* protected_mask, const float* original_density,
+                        const hexa_density_update_params* p, hexa_density_update_stats* stats);
+
 /* ---- (e) SIMP sensitivities and OC update ------------------------------ */
 /* dc_e = -penal * rho_e^(penal-1) * (E0 - Emin) * u_e^T K0 u_e and
  * compliance = sum_e (Emin + rho_e^penal (E0-Emin)) u_e^T K0 u_e. */

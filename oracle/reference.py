@@ -641,3 +641,90 @@ def remap_fields(old, new_dims, new_h, lengths, density, alpha=None, projection=
     na = None if alpha is None else np.asarray(alpha, dtype=f32)[i0 + onx * j0 + onx * ony * k0]
     return val, na, raw
 
+
+# ---------------------------------------------------------- density update
+def density_filter_radius(p, dx, dy, dz):
+    """The radius schedule of TopOpt.jl:265-298 in Float32: (R_length, R_effective)."""
+    f32 = np.float32
+    interm_frac = f32(p["filter_R_interm_iter_perc"]) / f32(100.0)
+    dim = f32(p["max_domain_dim"])
+    r_init = f32(p["filter_R_init_perc"]) / f32(100.0) * dim
+    r_interm = f32(p["filter_R_interm_perc"]) / f32(100.0) * dim
+    r_final = f32(p["filter_R_final_perc"]) / f32(100.0) * dim
+    n = int(p["number_of_iterations"])
+    interm = max(1, int(np.rint(interm_frac * f32(n))))  # Julia's round: ties to even
+    calc = min(int(p["iter"]), n)
+    if calc <= interm:
+        t = f32(calc - 1) / f32(interm - 1) if interm > 1 else f32(0.0)
+        r = r_init * (f32(1.0) - t) + r_interm * t
+    else:
+        t = f32(calc - interm) / f32(n - interm) if n > interm else f32(0.0)
+        r = r_interm * (f32(1.0) - t) + r_final * t
+    safe = f32(p["minimum_filter_radius_as_elements"]) * ((f32(dx) + f32(dy) + f32(dz)) / f32(3.0))
+    r = safe if r < safe else r
+    return f32(r), f32(r) / f32(2.5)
+
+
+def update_density(density, l1, protected, original, p, h, filter_fn=None):
+    """TopologyOptimization.update_density! (TopOpt.jl:211-482) restated in
+    numpy Float32.  p holds the scalars update_density! reads (the field
+    names of hexa_density_update_params); h = (dx, dy, dz); filter_fn(proposal,
+    R_effective) stands for the GPU filter (None: no filter).  Returns the
+    new density and the statistics; the change sum is taken in FP64 and
+    rounded once (the reference's Float32 chunk sums depend on its thread
+    count)."""
+    f32 = np.float32
+    dens = np.asarray(density, dtype=f32)
+    l1 = np.asarray(l1, dtype=f32)
+    orig = np.asarray(original, dtype=f32)
+    prot = np.zeros(dens.size, bool) if protected is None else np.asarray(protected).astype(bool)
+    free = ~prot
+    stats = dict(status=0, filter_used=0, filter_nan_fallback=0, mean_change=f32(0), R_length=f32(0),
+                 current_threshold=f32(0), R_effective=f32(0), active_count=0, candidates=0, culled=0)
+    if np.isnan(l1).any():  # TopOpt.jl:230-236
+        stats["status"] = 1
+        return dens.copy(), stats
+    min_d, max_d = f32(p["min_density"]), f32(p["max_density"])
+    with np.errstate(over="ignore", invalid="ignore"):
+        val = (l1 / f32(p["l1_stress_allowable"])) / f32(p["E"])
+    prop = np.where(prot, orig, np.maximum(val, min_d)).astype(f32)  # TopOpt.jl:254-263
+    R, Reff = density_filter_radius(p, *h)
+    stats["R_length"], stats["R_effective"] = R, Reff
+    filt = prop
+    if float(Reff) > 1e-4 and filter_fn is not None:
+        stats["filter_used"] = 1
+        filt = np.asarray(filter_fn(prop, Reff), dtype=f32)
+        if np.isnan(filt).any():  # TopOpt.jl:360-363
+            stats["filter_nan_fallback"] = 1
+            filt = prop
+    new = dens.copy()
+    with np.errstate(invalid="ignore"):
+        raw = np.maximum(filt, min_d)
+        eff = np.minimum(raw, max_d)
+        diff = np.abs(eff - dens)  # TopOpt.jl:376-393
+    change = float(diff[free].astype(np.float64).sum())
+    act1 = int(np.count_nonzero(raw[free] > min_d))
+    stats["mean_change"] = f32(f32(change) / f32(act1)) if act1 > 0 else f32(0)
+    new[free] = raw[free]
+    it, n = int(p["iter"]), int(p["number_of_iterations"])  # TopOpt.jl:420-428
+    if it > n:
+        thr = f32(p["final_density_threshold"])
+    else:
+        thr = f32(p["final_density_threshold"]) * f32(min(max(f32(it) / f32(n), f32(0)), f32(1)))
+    stats["current_threshold"] = f32(thr)
+    new[free] = np.minimum(new[free], max_d)  # TopOpt.jl:430-447
+    live = free & (new > min_d)
+    active = int(np.count_nonzero(live)) + int(np.count_nonzero(prot & (orig > min_d)))
+    cands = np.nonzero(live & (new < thr))[0]
+    allowed = int(np.floor(f32(active) * f32(p["max_culling_ratio"])))
+    if cands.size > allowed:  # TopOpt.jl:449-460: stable sort by density
+        cull = cands[np.argsort(new[cands], kind="stable")[:allowed]]
+    else:
+        cull = cands
+    new[cull] = min_d
+    if p.get("hard_update", 0):  # TopOpt.jl:464-472
+        new[free & (new > min_d)] = f32(1.0)
+    new[prot] = orig[prot]  # TopOpt.jl:474-479
+    stats.update(active_count=active, candidates=int(cands.size), culled=int(cull.size))
+    return new, stats
+

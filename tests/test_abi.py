@@ -66,6 +66,15 @@ def test_default_params(built_lib):
         _lib.default_params(not_a_key=1)
 
 
+def test_default_density_update_params(built_lib):
+    p = _lib.DensityUpdateParams()
+    _lib.load(built_lib).hexa_default_density_update_params(C.byref(p))
+    assert p.min_density == np.float32(1e-3) and p.max_density == 1.0 and p.filter_R_interm_iter_perc == 50.0
+    assert p.minimum_filter_radius_as_elements == 2.5 and p.filter_tolerance == np.float32(1e-5)
+    assert p.final_density_threshold == np.float32(0.95) and p.max_culling_ratio == np.float32(0.1)
+    assert p.hard_update == 0 and p.filter_max_iter == 200 and p.filter_precision == 2
+
+
 def test_struct_sizes_match_header_layout(built_lib):
     # 8-byte aligned doubles after int32 pairs: sizes computed by the C compiler
     assert C.sizeof(_lib.Grid) == 40
@@ -77,7 +86,9 @@ def test_ctypes_layout_matches_c_compiler(tmp_path):
     """offsetof/sizeof of every public struct, from gcc on include/hexagpu.h."""
     import subprocess
     structs = {"hexa_grid": _lib.Grid, "hexa_bc": _lib.BC, "hexa_solve_params": _lib.SolveParams,
-               "hexa_solve_stats": _lib.SolveStats, "hexa_filter_stats": _lib.FilterStats}
+               "hexa_solve_stats": _lib.SolveStats, "hexa_filter_stats": _lib.FilterStats,
+               "hexa_density_update_params": _lib.DensityUpdateParams,
+               "hexa_density_update_stats": _lib.DensityUpdateStats}
     lines = ['#include <stdio.h>', '#include <stddef.h>', f'#include "{HEADER}"', "int main(void){"]
     for cname, py in structs.items():
         lines.append(f'printf("{cname} %zu\\n", sizeof({cname}));')

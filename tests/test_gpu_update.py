@@ -1,0 +1,122 @@
+"""hexa_update_density (TopOpt.jl:211-482 on the GPU) against the oracle's
+restatement: densities, counts and the culled set bit-exact, the mean change
+to FP32 rounding of the same FP64 sum."""
+import numpy as np
+import pytest
+import torch
+
+from v119_2025_12_19_hexatop_aws_gb300 import _lib
+from v119_2025_12_19_hexatop_aws_gb300.helmholtz import filter_density
+from v119_2025_12_19_hexatop_aws_gb300.topopt import density_update_params, update_density, update_density_gpu
+
+pytestmark = pytest.mark.gpu
+F32 = np.float32
+KEYS = ("E", "l1_stress_allowable", "iter", "number_of_iterations", "min_density", "max_density", "max_domain_dim",
+        "filter_R_init_perc", "filter_R_interm_perc", "filter_R_final_perc", "filter_R_interm_iter_perc",
+        "minimum_filter_radius_as_elements", "filter_tolerance", "final_density_threshold", "max_culling_ratio",
+        "hard_update")
+
+
+def as_dict(p):
+    return {k: getattr(p, k) for k in KEYS}
+
+
+def fields(rng, ne, ties=True):
+    dens = rng.uniform(0.0, 1.0, ne).astype(F32)
+    l1 = rng.uniform(0.0, 1.5, ne).astype(F32) * F32(200.0)
+    if ties:  # repeated stress values give equal proposals: the cull order falls back to the index
+        pick = rng.uniform(size=ne) < 0.3
+        l1[pick] = rng.choice(np.array([2.0, 4.0, 6.0, 10.0], F32), pick.sum())
+    prot = rng.uniform(size=ne) < 0.05
+    orig = np.where(rng.uniform(size=ne) < 0.5, F32(1.0), F32(0.0)).astype(F32)
+    return dens, l1, prot, orig
+
+
+def check(grid, dens, l1, prot, orig, p, ctx, oracle, filter_fn=None):
+    d_gpu = dens.copy()
+    st = update_density_gpu(grid, d_gpu, l1, prot, orig, p, ctx=ctx)
+    ref, rs = oracle.update_density(dens, l1, prot, orig, as_dict(p), (F32(grid.dx), F32(grid.dy), F32(grid.dz)),
+                                    filter_fn=filter_fn)
+    assert st["status"] == rs["status"]
+    assert np.array_equal(d_gpu, ref), np.nonzero(d_gpu != ref)[0][:10]
+    for k in ("active_count", "candidates", "culled", "filter_used", "filter_nan_fallback"):
+        assert st[k] == rs[k], k
+    for k in ("R_length", "R_effective", "current_threshold"):
+        assert F32(st[k]) == rs[k], k
+    assert abs(st["mean_change"] - rs["mean_change"]) <= 1e-6 * abs(rs["mean_change"]) + 1e-30
+    return st
+
+
+@pytest.mark.parametrize("dims", [(16, 8, 8), (96, 48, 48)])
+@pytest.mark.parametrize("it,hard", [(5, 0), (30, 1), (40, 0)])
+def test_update_without_filter_matches_oracle(ctx, oracle, rng, dims, it, hard):
+    grid = _lib.make_grid(*dims, 0.05, 0.05, 0.05)
+    ne = dims[0] * dims[1] * dims[2]
+    dens, l1, prot, orig = fields(rng, ne)
+    p = density_update_params(E=200.0, l1_stress_allowable=1.0, iter=it, number_of_iterations=30,
+                              minimum_filter_radius_as_elements=0.0, hard_update=hard, max_culling_ratio=0.05,
+                              final_density_threshold=0.95, max_domain_dim=dims[0] * 0.05)
+    st = check(grid, dens, l1, prot, orig, p, ctx, oracle)
+    assert st["filter_used"] == 0
+    if it >= 30:
+        assert st["candidates"] > st["culled"] > 0  # the selection path ran
+
+
+def test_update_with_filter_matches_oracle(ctx, oracle, rng):
+    dims = (48, 24, 24)
+    grid = _lib.make_grid(*dims, 0.05, 0.05, 0.05)
+    dens, l1, prot, orig = fields(rng, dims[0] * dims[1] * dims[2], ties=False)
+    p = density_update_params(E=200.0, l1_stress_allowable=1.0, iter=12, number_of_iterations=30,
+                              filter_R_init_perc=8.0, filter_R_interm_perc=4.0, filter_R_final_perc=2.0,
+                              max_domain_dim=dims[0] * 0.05, max_culling_ratio=0.1)
+
+    def gpu_filter(prop, reff):
+        out, _ = filter_density(grid, prop.astype(np.float64), float(reff), tol=float(F32(1e-5)), max_iter=200,
+                                quirk=True, precision="fp32", ctx=ctx)
+        return out.astype(F32)
+
+    st = check(grid, dens, l1, prot, orig, p, ctx, oracle, filter_fn=gpu_filter)
+    assert st["filter_used"] == 1 and st["filter_iters"] > 0
+
+
+def test_update_nan_stress_skips_and_inf_falls_back(ctx, oracle, rng):
+    dims = (16, 8, 8)
+    grid = _lib.make_grid(*dims, 0.05, 0.05, 0.05)
+    dens, l1, prot, orig = fields(rng, 1024)
+    p = density_update_params(E=200.0, iter=10, filter_R_init_perc=10.0, filter_R_interm_perc=10.0,
+                              filter_R_final_perc=10.0, max_domain_dim=0.8)
+    bad = l1.copy()
+    bad[17] = np.nan
+    d = dens.copy()
+    st = update_density_gpu(grid, d, bad, prot, orig, p, ctx=ctx)
+    assert st["status"] == 1 and np.array_equal(d, dens)
+    # an infinite stress makes the filtered field NaN: the proposal is used
+    inf = l1.copy()
+    inf[~prot] = np.where(np.arange((~prot).sum()) == 3, np.inf, inf[~prot])
+
+    def gpu_filter(prop, reff):
+        out, _ = filter_density(grid, prop.astype(np.float64), float(reff), tol=float(F32(1e-5)), max_iter=200,
+                                quirk=True, precision="fp32", ctx=ctx)
+        return out.astype(F32)
+
+    st = check(grid, dens, inf, prot, orig, p, ctx, oracle, filter_fn=gpu_filter)
+    assert st["filter_nan_fallback"] == 1
+
+
+def test_update_device_arrays_and_dropin(ctx, oracle, rng):
+    dims = (24, 12, 12)
+    grid = _lib.make_grid(*dims, 0.05, 0.05, 0.05)
+    ne = dims[0] * dims[1] * dims[2]
+    dens, l1, prot, orig = fields(rng, ne)
+    p = density_update_params(E=200.0, iter=30, minimum_filter_radius_as_elements=0.0, max_domain_dim=1.2)
+    host = dens.copy()
+    update_density_gpu(grid, host, l1, prot, orig, p, ctx=ctx)
+    dev = torch.from_numpy(dens.copy()).cuda()
+    update_density_gpu(grid, dev, torch.from_numpy(l1).cuda(), prot, torch.from_numpy(orig).cuda(), p, ctx=ctx)
+    assert np.array_equal(dev.cpu().numpy(), host)
+    config = {"optimization_parameters": {"minimum_filter_radius_as_elements": 0.0},
+              "geometry": {"nElem_x_computed": dims[0], "nElem_y_computed": dims[1], "nElem_z_computed": dims[2],
+                           "dx_computed": 0.05, "dy_computed": 0.05, "dz_computed": 0.05, "max_domain_dim": 1.2}}
+    d2 = dens.copy()
+    out = update_density(d2, l1, prot, F32(200.0), F32(1.0), 30, 30, orig, F32(1e-3), F32(1.0), config, ctx=ctx)
+    assert np.array_equal(d2, host) and len(out) == 6

@@ -1,0 +1,75 @@
+"""The density update between solves (TopOpt.jl:211-482): the oracle's
+restatement checked on hand-worked cases, without a GPU."""
+import numpy as np
+import pytest
+
+F32 = np.float32
+
+
+def params(**kw):
+    p = dict(E=1.0, l1_stress_allowable=1.0, iter=1, number_of_iterations=30, min_density=1e-3, max_density=1.0,
+             max_domain_dim=2.0, filter_R_init_perc=0.0, filter_R_interm_perc=0.0, filter_R_final_perc=0.0,
+             filter_R_interm_iter_perc=50.0, minimum_filter_radius_as_elements=0.0, filter_tolerance=1e-5,
+             final_density_threshold=0.95, max_culling_ratio=0.1, hard_update=0)
+    p.update(kw)
+    return p
+
+
+def test_radius_schedule_follows_the_reference(oracle):
+    # R from 10 % to 5 % of 2.0 over the first half (iterations 1..15), then to 2 %
+    p = params(filter_R_init_perc=10.0, filter_R_interm_perc=5.0, filter_R_final_perc=2.0)
+    r1, e1 = oracle.density_filter_radius(dict(p, iter=1), 0.01, 0.01, 0.01)
+    assert r1 == F32(0.2) and e1 == F32(0.2) / F32(2.5)
+    r15, _ = oracle.density_filter_radius(dict(p, iter=15), 0.01, 0.01, 0.01)
+    assert r15 == F32(F32(5.0) / F32(100.0) * F32(2.0))
+    r30, _ = oracle.density_filter_radius(dict(p, iter=30), 0.01, 0.01, 0.01)
+    assert abs(float(r30) - 0.04) < 1e-7
+    r99, _ = oracle.density_filter_radius(dict(p, iter=99), 0.01, 0.01, 0.01)
+    assert r99 == r30  # iterations past the schedule keep the final radius
+    # the floor at minimum_filter_radius_as_elements x mean element size
+    rmin, _ = oracle.density_filter_radius(dict(p, iter=30, minimum_filter_radius_as_elements=2.5), 0.1, 0.1, 0.1)
+    assert rmin == F32(2.5) * ((F32(0.1) + F32(0.1) + F32(0.1)) / F32(3.0))
+
+
+def test_update_proposal_cull_and_projection(oracle):
+    # 10 elements, none protected; proposal = l1 / allowable / E, floored at min_density
+    l1 = np.array([0.0, 0.3, 0.5, 0.02, 0.9, 0.01, 0.6, 0.05, 2.0, 0.04], F32)
+    dens = np.full(10, 0.5, F32)
+    p = params(iter=30, max_culling_ratio=0.25, final_density_threshold=0.1)
+    new, st = oracle.update_density(dens, l1, None, np.ones(10, F32), p, (0.1, 0.1, 0.1))
+    # threshold 0.1 * 30/30; live: all but element 0 (0.001); candidates 0.02, 0.01, 0.05, 0.04
+    assert st["current_threshold"] == F32(0.1) and st["active_count"] == 9 and st["candidates"] == 4
+    # floor(9 * 0.25) = 2 culls: the two smallest, 0.01 (e5) and 0.02 (e3)
+    assert st["culled"] == 2
+    assert new[5] == F32(1e-3) and new[3] == F32(1e-3) and new[7] == F32(0.05) and new[9] == F32(0.04)
+    assert new[8] == F32(1.0)  # clamped to max_density
+    change = np.abs(np.minimum(np.maximum(l1, F32(1e-3)), F32(1.0)) - dens).astype(np.float64).sum()
+    assert st["mean_change"] == F32(F32(change) / F32(9))
+    hard, _ = oracle.update_density(dens, l1, None, np.ones(10, F32), dict(p, hard_update=1), (0.1, 0.1, 0.1))
+    assert set(np.unique(hard)) == {F32(1e-3), F32(1.0)}
+
+
+def test_update_ties_cull_lowest_index_first(oracle):
+    l1 = np.array([0.05, 0.05, 0.5, 0.05, 0.05, 0.5, 0.5, 0.5], F32)
+    p = params(iter=30, final_density_threshold=0.1, max_culling_ratio=0.3)
+    new, st = oracle.update_density(np.full(8, 0.5, F32), l1, None, np.ones(8, F32), p, (0.1, 0.1, 0.1))
+    assert st["candidates"] == 4 and st["culled"] == 2  # floor(8 * 0.3)
+    assert list(np.nonzero(new == F32(1e-3))[0]) == [0, 1]
+
+
+def test_update_protected_and_nan_paths(oracle):
+    l1 = np.array([0.5, 0.5, 0.5, 0.5], F32)
+    prot = np.array([1, 0, 0, 1], bool)
+    orig = np.array([0.7, 1.0, 1.0, 0.0005], F32)
+    new, st = oracle.update_density(np.full(4, 0.3, F32), l1, prot, orig, params(), (0.1, 0.1, 0.1))
+    assert new[0] == F32(0.7) and new[3] == F32(0.0005) and new[1] == F32(0.5)
+    assert st["active_count"] == 3  # protected counted by their original density
+    bad = l1.copy()
+    bad[2] = np.nan
+    same, st = oracle.update_density(np.full(4, 0.3, F32), bad, prot, orig, params(), (0.1, 0.1, 0.1))
+    assert st["status"] == 1 and np.all(same == F32(0.3))
+    # a filter that returns NaN: the proposal is used instead
+    p = params(filter_R_init_perc=10.0, filter_R_interm_perc=10.0, filter_R_final_perc=10.0)
+    new2, st2 = oracle.update_density(np.full(4, 0.3, F32), l1, prot, orig, p, (0.1, 0.1, 0.1),
+                                      filter_fn=lambda x, r: np.full_like(x, np.nan))
+    assert st2["filter_used"] == 1 and st2["filter_nan_fallback"] == 1 and np.array_equal(new2, new)

@@ -69,6 +69,27 @@ class FilterStats(C.Structure):
     _fields_ = [("status", C.c_int32), ("iterations", C.c_int32), ("relres", C.c_double), ("solve_ms", C.c_double)]
 
 
+class DensityUpdateParams(C.Structure):
+    _fields_ = [("E", C.c_float), ("l1_stress_allowable", C.c_float), ("iter", C.c_int32),
+                ("number_of_iterations", C.c_int32), ("min_density", C.c_float), ("max_density", C.c_float),
+                ("max_domain_dim", C.c_float), ("filter_R_init_perc", C.c_float), ("filter_R_interm_perc", C.c_float),
+                ("filter_R_final_perc", C.c_float), ("filter_R_interm_iter_perc", C.c_float),
+                ("minimum_filter_radius_as_elements", C.c_float), ("filter_tolerance", C.c_float),
+                ("final_density_threshold", C.c_float), ("max_culling_ratio", C.c_float), ("hard_update", C.c_int32),
+                ("filter_max_iter", C.c_int32), ("filter_precision", C.c_int32)]
+
+
+class DensityUpdateStats(C.Structure):
+    _fields_ = [("status", C.c_int32), ("filter_used", C.c_int32), ("filter_nan_fallback", C.c_int32),
+                ("filter_iters", C.c_int32), ("mean_change", C.c_float), ("R_length", C.c_float),
+                ("current_threshold", C.c_float), ("R_effective", C.c_float), ("filter_time", C.c_double),
+                ("filter_res", C.c_double), ("active_count", C.c_int64), ("candidates", C.c_int64),
+                ("culled", C.c_int64)]
+
+    def as_dict(self) -> dict:
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
 P = C.c_void_p
 D = C.c_double
 I32 = C.c_int32
@@ -102,6 +123,9 @@ SIGNATURES = {
                                 C.POINTER(FilterStats)]),
     "hexa_filter_noalloc": (I32, [C.POINTER(Grid), P, D, D, I32, I32, P, P, C.POINTER(FilterStats)]),
     "hexa_remap_fields": (I32, [P, C.POINTER(Grid), C.POINTER(Grid), D, D, D, P, P, I32, P, P]),
+    "hexa_default_density_update_params": (None, [C.POINTER(DensityUpdateParams)]),
+    "hexa_update_density": (I32, [P, C.POINTER(Grid), P, P, P, P, C.POINTER(DensityUpdateParams),
+                                  C.POINTER(DensityUpdateStats)]),
     "hexa_stress_field": (I32, [P, C.POINTER(Grid), P, P, C.c_float, C.c_float, P, P, P, P, P, P]),
     "hexa_sensitivities": (I32, [P, C.POINTER(Grid), D, P, P, D, D, D, P, C.POINTER(D)]),
     "hexa_simp_factors": (I32, [P, I64, P, D, D, D, P]),

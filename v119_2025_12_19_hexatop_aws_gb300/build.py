@@ -19,7 +19,7 @@ CSRC = PKG / "csrc"
 BUILD = PKG / "_build"
 LIB = PKG / "libhexagpu.so"
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
-SOURCES = ["op.cu", "vec.cu", "mg.cu", "helm.cu", "topo.cu", "block.cu", "batch.cu", "stress.cu", "remap.cu", "solver.cu", "capi.cu", "noalloc.cu", "element.cpp"]
+SOURCES = ["op.cu", "vec.cu", "mg.cu", "helm.cu", "topo.cu", "block.cu", "batch.cu", "stress.cu", "remap.cu", "update.cu", "solver.cu", "capi.cu", "noalloc.cu", "element.cpp"]
 
 
 def nvcc() -> str:
@@ -30,7 +30,9 @@ def nvcc() -> str:
 
 
 def _flags(src: str, ptxas_verbose: bool) -> list[str]:
-    f = ["-O3", "-std=c++17", "-Xcompiler", "-fPIC", "-lineinfo", "--expt-relaxed-constexpr"]
+    # host code without FMA contraction: the same roundings on x86-64 and aarch64
+    f = ["-O3", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off", "-lineinfo",
+         "--expt-relaxed-constexpr"]
     if src.endswith(".cu"):
         f += [ARCH]
         if ptxas_verbose:

@@ -5,6 +5,7 @@
 // buffers, device arrays are used in place.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <chrono>
 #include <cmath>
 #include <cstring>
@@ -521,14 +522,17 @@ int hexa_solve_multi_rhs(hexa_ctx* h, const hexa_grid* g, const hexa_bc* bc, con
 
 }  // extern "C"
 
+// The filter's PCG on a device density of type T (GPUHelmholtz.jl:180-260):
+// writes the filtered element field into outT, or sets *zero and leaves outT
+// alone when the right-hand side is zero (the reference returns its input
+// unchanged, GPUHelmholtz.jl:203-206).
 template <typename T>
-static int filter_t(hexa_ctx* h, const Grid& G, const double* rho_d, const HelmK& K, double tol, int max_iter,
-                    double* out_d, hexa_filter_stats* st) {
+static int filter_run(hexa_ctx* h, const Grid& G, const T* rho, const HelmK& K, double tol, int max_iter, T* outT,
+                      hexa_filter_stats* st, bool* zero) {
   Ctx& c = h->c;
-  const long long nn = G.nnode(), ne = G.nelem();
+  const long long nn = G.nnode();
   const char* tg = sizeof(T) == 8 ? "h64_" : "h32_";
   auto nm = [&](const char* s) { return std::string(tg) + s; };
-  T* rho = c.vec<T>(nm("rho"), ne);
   T* b = c.vec<T>(nm("b"), nn);
   T* x = c.vec<T>(nm("x"), nn);
   T* r = c.vec<T>(nm("r"), nn);
@@ -536,13 +540,11 @@ static int filter_t(hexa_ctx* h, const Grid& G, const double* rho_d, const HelmK
   T* p = c.vec<T>(nm("p"), nn);
   T* q = c.vec<T>(nm("q"), nn);
   T* dinv = c.vec<T>(nm("dinv"), nn);
-  T* outT = c.vec<T>(nm("out"), ne);
-  if (!rho || !b || !x || !r || !z || !p || !q || !dinv || !outT) return HEXA_ERR_NOMEM;
-  if constexpr (sizeof(T) == 8) cudaMemcpyAsync(rho, rho_d, ne * sizeof(double), cudaMemcpyDeviceToDevice, c.st);
-  else launch_convert<float, double>(rho, rho_d, ne, c.st);
+  if (!b || !x || !r || !z || !p || !q || !dinv) return HEXA_ERR_NOMEM;
+  *zero = false;
   launch_helm_rhs<T>(G, rho, (T)K.rhs_scale, b, c.st);
   launch_helm_dinv<T>(G, K, dinv, c.st);
-  c.launches += 3;
+  c.launches += 2;
   RedArgs rd;
   rd.partials = c.partials;
   rd.ticket = c.ticket;
@@ -555,10 +557,11 @@ static int filter_t(hexa_ctx* h, const Grid& G, const double* rho_d, const HelmK
   cudaMemcpyAsync(c.hscal + 20, c.dscal + 20, sizeof(double), cudaMemcpyDeviceToHost, c.st);
   cudaStreamSynchronize(c.st);
   const double bnorm = std::sqrt(c.hscal[20]);
-  if (bnorm == 0.0) {  // GPUHelmholtz.jl:203-206 returns the input unchanged
-    cudaMemcpyAsync(out_d, rho_d, ne * sizeof(double), cudaMemcpyDeviceToDevice, c.st);
+  if (bnorm == 0.0) {
+    *zero = true;
     st->iterations = 0;
     st->relres = 0.0;
+    st->solve_ms = 0.0;
     return HEXA_OK;
   }
   PcgScalars hs;
@@ -600,11 +603,6 @@ static int filter_t(hexa_ctx* h, const Grid& G, const double* rho_d, const HelmK
   }
   launch_helm_extract<T>(G, x, outT, c.st);
   c.launches++;
-  if constexpr (sizeof(T) == 8) cudaMemcpyAsync(out_d, outT, ne * sizeof(double), cudaMemcpyDeviceToDevice, c.st);
-  else {
-    launch_convert<double, float>(out_d, outT, ne, c.st);
-    c.launches++;
-  }
   cudaEventRecord(c.ev[1], c.st);
   cudaEventSynchronize(c.ev[1]);
   float ms = 0;
@@ -615,6 +613,33 @@ static int filter_t(hexa_ctx* h, const Grid& G, const double* rho_d, const HelmK
   return HEXA_OK;
 }
 
+template <typename T>
+static int filter_t(hexa_ctx* h, const Grid& G, const double* rho_d, const HelmK& K, double tol, int max_iter,
+                    double* out_d, hexa_filter_stats* st) {
+  Ctx& c = h->c;
+  const long long ne = G.nelem();
+  const char* tg = sizeof(T) == 8 ? "h64_" : "h32_";
+  T* rho = c.vec<T>(std::string(tg) + "rho", ne);
+  T* outT = c.vec<T>(std::string(tg) + "out", ne);
+  if (!rho || !outT) return HEXA_ERR_NOMEM;
+  if constexpr (sizeof(T) == 8) cudaMemcpyAsync(rho, rho_d, ne * sizeof(double), cudaMemcpyDeviceToDevice, c.st);
+  else {
+    launch_convert<float, double>(rho, rho_d, ne, c.st);
+    c.launches++;
+  }
+  bool zero = false;
+  const int rc = filter_run<T>(h, G, rho, K, tol, max_iter, outT, st, &zero);
+  if (rc != HEXA_OK) return rc;
+  if (zero) {
+    cudaMemcpyAsync(out_d, rho_d, ne * sizeof(double), cudaMemcpyDeviceToDevice, c.st);
+  } else if constexpr (sizeof(T) == 8) {
+    cudaMemcpyAsync(out_d, outT, ne * sizeof(double), cudaMemcpyDeviceToDevice, c.st);
+  } else {
+    launch_convert<double, float>(out_d, outT, ne, c.st);
+    c.launches++;
+  }
+  return HEXA_OK;
+}
 
 extern "C" {
 
@@ -645,6 +670,161 @@ int hexa_filter(hexa_ctx* h, const hexa_grid* g, const double* rho_in, double ra
   c.last_ms = st.solve_ms;
   if (stats) *stats = st;
   return rc;
+}
+
+void hexa_default_density_update_params(hexa_density_update_params* p) {
+  if (!p) return;
+  std::memset(p, 0, sizeof(*p));
+  p->E = 1.0f;
+  p->l1_stress_allowable = 1.0f;
+  p->iter = 1;
+  p->number_of_iterations = 30;  // config number_of_iterations (Main.jl:316)
+  p->min_density = 1.0e-3f;
+  p->max_density = 1.0f;
+  p->filter_R_interm_iter_perc = 50.0f;
+  p->minimum_filter_radius_as_elements = 2.5f;
+  p->filter_tolerance = 1.0e-5f;
+  p->final_density_threshold = 0.95f;
+  p->max_culling_ratio = 0.1f;
+  p->hard_update = 0;
+  p->filter_max_iter = 200;
+  p->filter_precision = HEXA_PREC_FP32;
+}
+
+// The filter radius schedule of TopOpt.jl:265-298 in Float32: linear from
+// the initial to the intermediate radius up to the intermediate iteration,
+// then to the final radius, floored at minimum_filter_radius_as_elements
+// times the mean element size.  Host code is built without FMA contraction,
+// so each product and sum rounds once as in the reference.
+static float density_filter_radius(const hexa_density_update_params& p, float dx, float dy, float dz) {
+  const float interm_frac = p.filter_R_interm_iter_perc / 100.0f;
+  const float r_init = p.filter_R_init_perc / 100.0f * p.max_domain_dim;
+  const float r_interm = p.filter_R_interm_perc / 100.0f * p.max_domain_dim;
+  const float r_final = p.filter_R_final_perc / 100.0f * p.max_domain_dim;
+  const int n = p.number_of_iterations;
+  const int interm = std::max(1, (int)std::nearbyint(interm_frac * (float)n));  // round(Int, .): ties to even
+  const int calc = std::min(p.iter, n);
+  float r;
+  if (calc <= interm) {
+    const float t = interm > 1 ? (float)(calc - 1) / (float)(interm - 1) : 0.0f;
+    r = r_init * (1.0f - t) + r_interm * t;
+  } else {
+    const float t = n > interm ? (float)(calc - interm) / (float)(n - interm) : 0.0f;
+    r = r_interm * (1.0f - t) + r_final * t;
+  }
+  const float safe = p.minimum_filter_radius_as_elements * ((dx + dy + dz) / 3.0f);
+  return r < safe ? safe : r;
+}
+
+// The culling threshold of TopOpt.jl:420-428.
+static float density_cull_threshold(const hexa_density_update_params& p) {
+  if (p.iter > p.number_of_iterations) return p.final_density_threshold;
+  float prog = (float)p.iter / (float)p.number_of_iterations;
+  prog = prog > 1.0f ? 1.0f : (prog < 0.0f ? 0.0f : prog);
+  return p.final_density_threshold * prog;
+}
+
+int hexa_update_density(hexa_ctx* h, const hexa_grid* g, float* density, const float* l1_stress,
+                        const uint8_t* protected_mask, const float* original_density,
+                        const hexa_density_update_params* p, hexa_density_update_stats* stats) {
+  if (!h) return HEXA_ERR_ARG;
+  if (!valid_grid(g) || !density || !l1_stress || !original_density || !p)
+    return set_err(h, HEXA_ERR_ARG, "invalid grid or null array");
+  if (p->number_of_iterations < 1 || !(p->E > 0.0f) || !(p->l1_stress_allowable > 0.0f) || !std::isfinite(p->E) ||
+      !std::isfinite(p->l1_stress_allowable) || !(p->filter_tolerance > 0.0f) || p->filter_max_iter < 1 ||
+      !(p->min_density <= p->max_density))
+    return set_err(h, HEXA_ERR_ARG, "invalid density update parameters");
+  Ctx& c = h->c;
+  c.err.clear();
+  cudaSetDevice(c.device);
+  const Grid G = make_grid(g->nx, g->ny, g->nz);
+  const long long ne = G.nelem();
+  if (ne >= (1LL << 32)) return set_err(h, HEXA_ERR_TOO_LARGE, "density update: more than 2^32 - 1 elements");
+  hexa_density_update_stats st;
+  std::memset(&st, 0, sizeof(st));
+  const float* l1d = stage_in<float>(c, l1_stress, ne, "ud_l1");
+  const float* od = stage_in<float>(c, original_density, ne, "ud_orig");
+  const uint8_t* pd = protected_mask ? stage_in<uint8_t>(c, protected_mask, ne, "ud_prot") : nullptr;
+  const float* dd = stage_in<float>(c, (const float*)density, ne, "ud_rho");  // the user's array is written last
+  float* prop = c.vec<float>("ud_prop", ne);
+  float* work = c.vec<float>("ud_new", ne);
+  UpdateState* s = c.vec<UpdateState>("ud_state", 1);
+  double* part = c.vec<double>("ud_part", update_partials_doubles());
+  unsigned long long* hist = c.vec<unsigned long long>("ud_hist", update_hist_bins());
+  if (!l1d || !od || (protected_mask && !pd) || !dd || !prop || !work || !s || !part || !hist)
+    return set_err(h, HEXA_ERR_NOMEM, c.err.empty() ? "density update: out of device memory" : c.err);
+  static_assert(sizeof(UpdateState) <= 16 * sizeof(double), "UpdateState exceeds its host landing slots");
+  UpdateState* hs = reinterpret_cast<UpdateState*>(c.hscal + 48);
+  auto fetch = [&]() {
+    cudaMemcpyAsync(hs, s, sizeof(UpdateState), cudaMemcpyDeviceToHost, c.st);
+    return cudaStreamSynchronize(c.st) == cudaSuccess && c.cuda_ok("update_density");
+  };
+  cudaMemsetAsync(s, 0, sizeof(UpdateState), c.st);
+  launch_propose(ne, l1d, pd, od, p->l1_stress_allowable, p->E, p->min_density, prop, s, c.st);
+  c.launches++;
+  if (!fetch()) return set_err(h, HEXA_ERR_CUDA, c.err);
+  if (hs->nan_stress) {  // TopOpt.jl:230-236: no update, zero statistics
+    st.status = 1;
+    if (stats) *stats = st;
+    return HEXA_OK;
+  }
+  st.R_length = density_filter_radius(*p, (float)g->dx, (float)g->dy, (float)g->dz);
+  st.R_effective = st.R_length / 2.5f;
+  st.current_threshold = density_cull_threshold(*p);
+  const float* src = prop;
+  if ((double)st.R_effective > 1e-4) {
+    st.filter_used = 1;
+    double Ke[64], Me[64];
+    if (scalar_matrices(g->dx, g->dy, g->dz, 1, Ke, Me) != 0) return set_err(h, HEXA_ERR_ARG, "invalid element size");
+    HelmK K;
+    helm_corner_matrix(Ke, Me, (double)st.R_effective, K.A);
+    K.rhs_scale = g->dx * g->dy * g->dz / 8.0;  // GPUHelmholtz.jl:198-199
+    hexa_filter_stats fs;
+    std::memset(&fs, 0, sizeof(fs));
+    bool zero = false;
+    int rc;
+    if (p->filter_precision == HEXA_PREC_FP64) {
+      double* p64 = c.vec<double>("h64_rho", ne);
+      double* o64 = c.vec<double>("h64_out", ne);
+      float* filt = c.vec<float>("ud_filt", ne);
+      if (!p64 || !o64 || !filt) return set_err(h, HEXA_ERR_NOMEM, "density update: out of device memory");
+      launch_convert<double, float>(p64, prop, ne, c.st);
+      c.launches++;
+      rc = filter_run<double>(h, G, p64, K, p->filter_tolerance, p->filter_max_iter, o64, &fs, &zero);
+      if (rc == HEXA_OK && !zero) {
+        launch_convert<float, double>(filt, o64, ne, c.st);
+        c.launches++;
+        src = filt;
+      }
+    } else {
+      float* filt = c.vec<float>("h32_out", ne);
+      if (!filt) return set_err(h, HEXA_ERR_NOMEM, "density update: out of device memory");
+      rc = filter_run<float>(h, G, prop, K, p->filter_tolerance, p->filter_max_iter, filt, &fs, &zero);
+      if (rc == HEXA_OK && !zero) src = filt;
+    }
+    if (rc != HEXA_OK) return set_err(h, rc, c.err.empty() ? "density update: filter failed" : c.err);
+    st.filter_time = fs.solve_ms / 1e3;
+    st.filter_iters = fs.iterations;
+    st.filter_res = fs.relres;
+  }
+  c.launches += launch_update_cull(ne, dd, src, pd, od, p->min_density, p->max_density, st.current_threshold,
+                                   p->max_culling_ratio, p->hard_update ? 1 : 0, work, part, hist, s, c.st);
+  if (!fetch()) return set_err(h, HEXA_ERR_CUDA, c.err);
+  if (hs->nan_filtered && src != prop) {  // TopOpt.jl:360-363: the unfiltered proposal instead
+    st.filter_nan_fallback = 1;
+    c.launches += launch_update_cull(ne, dd, prop, pd, od, p->min_density, p->max_density, st.current_threshold,
+                                     p->max_culling_ratio, p->hard_update ? 1 : 0, work, part, hist, s, c.st);
+    if (!fetch()) return set_err(h, HEXA_ERR_CUDA, c.err);
+  }
+  st.mean_change = hs->mean_change;
+  st.active_count = (int64_t)hs->active;
+  st.candidates = (int64_t)hs->candidates;
+  st.culled = (int64_t)hs->culled;
+  cudaMemcpyAsync(density, work, ne * sizeof(float),
+                  is_device_ptr(density) ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, c.st);
+  if (cudaStreamSynchronize(c.st) != cudaSuccess || !c.cuda_ok("update_density")) return set_err(h, HEXA_ERR_CUDA, c.err);
+  if (stats) *stats = st;
+  return HEXA_OK;
 }
 
 int hexa_solve_batch(hexa_ctx* h, int32_t count, const hexa_grid* grids, const hexa_bc* bcs, double nu,

@@ -165,6 +165,23 @@ void launch_remap(int onx, int ony, int onz, int nnx, int nny, int nnz, float nd
                   float ly, float lz, int projection, const float* dens, const float* alpha, float* nd, float* na,
                   cudaStream_t st);
 
+// ---- density update between solves (update.cu) -----------------------------
+struct UpdateState {
+  int nan_stress, nan_filtered, mode, pad;  // mode: 0 cull none, 1 every candidate, 2 the `allowed` smallest
+  double change;                            // sum of |min(raw, max) - old| over unprotected elements
+  unsigned long long active_updated;        // unprotected raw > min_density (the mean's divisor)
+  unsigned long long active, candidates, allowed, culled;
+  unsigned long long prefix, remaining;     // radix select: key of the last culled candidate
+  float mean_change, pad2;
+};
+void launch_propose(long long n, const float* l1, const uint8_t* prot, const float* orig, float allow, float E,
+                    float min_d, float* prop, UpdateState* s, cudaStream_t st);
+int launch_update_cull(long long n, const float* old, const float* src, const uint8_t* prot, const float* orig,
+                       float min_d, float max_d, float thr, float ratio, int hard, float* out, double* part,
+                       unsigned long long* hist, UpdateState* s, cudaStream_t st);
+size_t update_partials_doubles();
+int update_hist_bins();
+
 // ---- block PCG over k <= kMaxBlockCols columns (block.cu) ----------------
 constexpr int kMaxBlockCols = 16;
 constexpr int kBlockRedBlocks = 608;  // grid of the reducing block passes

@@ -126,3 +126,67 @@ def stress_field(grid, u, density, *, E=1.0, nu=0.3, voigt=True, ctx=None):
                                    _lib.ptr(out["l1"]), _lib.ptr(out["dir_max"]), _lib.ptr(out["dir_min"]))
     ctx.check(rc, allow=(_lib.HEXA_OK,))
     return out
+
+
+def density_update_params(**kw) -> _lib.DensityUpdateParams:
+    """hexa_density_update_params with the library defaults, fields overridden by keyword."""
+    p = _lib.DensityUpdateParams()
+    _lib.load().hexa_default_density_update_params(C.byref(p))
+    names = {f for f, _ in p._fields_}
+    for k, v in kw.items():
+        if k not in names:
+            raise KeyError(k)
+        setattr(p, k, v)
+    return p
+
+
+def update_density_gpu(grid, density, l1, protected, original, params, *, ctx=None):
+    """hexa_update_density: density (float32 numpy array or device tensor) is
+    updated in place; returns the statistics as a dict."""
+    ctx = ctx or context()
+    if isinstance(density, np.ndarray) and (density.dtype != np.float32 or not density.flags.c_contiguous):
+        raise TypeError("density must be a contiguous float32 array (it is updated in place)")
+    def f32(a):  # numpy arrays are converted; tensors (host or device) are passed as they are
+        return a if hasattr(a, "data_ptr") else np.ascontiguousarray(a, dtype=np.float32)
+
+    prot = None if protected is None else np.ascontiguousarray(np.asarray(protected, dtype=bool).view(np.uint8))
+    st = _lib.DensityUpdateStats()
+    l1a, oa = f32(l1), f32(original)
+    rc = ctx.lib.hexa_update_density(ctx.h, C.byref(grid), _lib.ptr(density), _lib.ptr(l1a), _lib.ptr(prot),
+                                     _lib.ptr(oa), C.byref(params), C.byref(st))
+    ctx.check(rc, allow=(_lib.HEXA_OK,))
+    return st.as_dict()
+
+
+def update_density(density, l1_stress_norm_field, protected_elements_mask, E, l1_stress_allowable, iter,
+                   number_of_iterations, original_density, min_density, max_density, config, elements=None,
+                   is_annealing=False, *, ctx=None):
+    """Drop-in for TopologyOptimization.update_density! (TopOpt.jl:211-482):
+    same arguments and config keys, density (float32) updated in place,
+    returns (mean_change, R_length, current_threshold, filter_time,
+    filter_iters, filter_res).  The structured grid comes from the config's
+    geometry.{nElem,d}{x,y,z}_computed; `elements` is not needed."""
+    opt = config["optimization_parameters"]
+    geom = config["geometry"]
+    solver = config.get("solver_parameters", {})
+    grid = _lib.make_grid(int(geom["nElem_x_computed"]), int(geom["nElem_y_computed"]), int(geom["nElem_z_computed"]),
+                          float(np.float32(geom["dx_computed"])), float(np.float32(geom["dy_computed"])),
+                          float(np.float32(geom["dz_computed"])))
+    p = density_update_params(
+        E=float(E), l1_stress_allowable=float(l1_stress_allowable), iter=int(iter),
+        number_of_iterations=int(number_of_iterations), min_density=float(min_density),
+        max_density=float(max_density), max_domain_dim=float(geom["max_domain_dim"]),
+        filter_R_init_perc=float(opt.get("filter_R_init_perc", 0.0)),
+        filter_R_interm_perc=float(opt.get("filter_R_interm_perc", 0.0)),
+        filter_R_final_perc=float(opt.get("filter_R_final_perc", 0.0)),
+        filter_R_interm_iter_perc=float(opt.get("filter_R_interm_iter_perc", 50.0)),
+        minimum_filter_radius_as_elements=float(opt.get("minimum_filter_radius_as_elements", 2.5)),
+        filter_tolerance=float(solver.get("filter_tolerance", 1.0e-5)),
+        final_density_threshold=float(opt.get("final_density_threshold", 0.95)),
+        max_culling_ratio=float(opt.get("max_culling_ratio", 0.1)),
+        hard_update=int(opt.get("density_update_method", "soft") == "hard"))
+    st = update_density_gpu(grid, density, l1_stress_norm_field, protected_elements_mask, original_density, p, ctx=ctx)
+    if st["status"] == 1:
+        return np.float32(0), np.float32(0), np.float32(0), 0.0, 0, 0.0
+    return (np.float32(st["mean_change"]), np.float32(st["R_length"]), np.float32(st["current_threshold"]),
+            st["filter_time"], st["filter_iters"], st["filter_res"])
