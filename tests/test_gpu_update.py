@@ -90,7 +90,8 @@ def test_update_nan_stress_skips_and_inf_falls_back(ctx, oracle, rng):
     d = dens.copy()
     st = update_density_gpu(grid, d, bad, prot, orig, p, ctx=ctx)
     assert st["status"] == 1 and np.array_equal(d, dens)
-    # an infinite stress makes the filtered field NaN: the proposal is used
+    # an infinite stress breaks the filter's PCG (NaN p.Ap); as the reference's
+    # loop, the filter returns a NaN field and the update uses the proposal
     inf = l1.copy()
     inf[~prot] = np.where(np.arange((~prot).sum()) == 3, np.inf, inf[~prot])
 

@@ -9,6 +9,7 @@
 #include <chrono>
 #include <cmath>
 #include <cstring>
+#include <limits>
 #include <new>
 #include <string>
 #include <vector>
@@ -601,7 +602,14 @@ static int filter_run(hexa_ctx* h, const Grid& G, const T* rho, const HelmK& K, 
     if (cudaStreamSynchronize(c.st) != cudaSuccess) return HEXA_ERR_CUDA;
     if (c.hs->halt) break;
   }
-  launch_helm_extract<T>(G, x, outT, c.st);
+  if (c.hs->status == 2 || c.hs->status == 4) {
+    // a NaN residual or a breakdown of p.Ap: the reference's loop goes on with
+    // alpha = rho / p.Ap non-finite and returns a NaN field (its callers test
+    // for that, TopOpt.jl:360-363), so the output is NaN here too
+    launch_fill<T>(outT, std::numeric_limits<T>::quiet_NaN(), G.nelem(), c.st);
+  } else {
+    launch_helm_extract<T>(G, x, outT, c.st);
+  }
   c.launches++;
   cudaEventRecord(c.ev[1], c.st);
   cudaEventSynchronize(c.ev[1]);

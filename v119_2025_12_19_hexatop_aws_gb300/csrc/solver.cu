@@ -1042,11 +1042,12 @@ Ctx::Tuned autotune_mixed(Ctx& c, const Problem& P, const hexa_solve_params& prm
     const double t = trial(best_l, nu, r0);
     if (t < best) best = t, best_nu = nu;
   }
-  for (int r : {5, 10, 20, 40}) {  // the lower end of the Chebyshev interval
-    if (r == r0) continue;
-    const double t = trial(best_l, best_nu, r);
-    if (t < best) best = t, best_r = r;
-  }
+  // The lower end of the Chebyshev interval (lambda_max / ratio) stays the
+  // caller's: a short trial does not predict its effect on the full count.
+  // On the 384x192x192 cantilever with 7 levels and V(3,3), whole solves took
+  // 4421 iterations at ratio 10 against 5173 at 5 and 5381 at 30, and a solve
+  // whose 120-iteration trials had picked a ratio other than 10 took 6116
+  // where ratio 10 takes 3996.
   Ctx::Tuned tu;
   tu.a = best_l;
   tu.b = best_nu;
