@@ -466,7 +466,7 @@ def _jacobi_rotate(spp, sqq, spq, spr, sqr, v, p, q):
     h = spq.copy()
     g = f32(100.0) * np.abs(h)
     act = (np.abs(spp) + g != np.abs(spp)) | (np.abs(sqq) + g != np.abs(sqq))
-    with np.errstate(divide="ignore", invalid="ignore"):
+    with np.errstate(divide="ignore", invalid="ignore", over="ignore"):  # inactive lanes; the GPU overflows alike
         theta = f32(0.5) * (sqq - spp) / h
         t = f32(1.0) / (np.abs(theta) + np.sqrt(theta * theta + f32(1.0)))
     t = np.where(theta < 0, -t, t).astype(f32)
