@@ -447,6 +447,7 @@ def next_rows(ctx, grid, u_d, rho, dev, reps=3):
     remap 12 B per new element (8 out + about 4 in)."""
     import ctypes as C
     import torch
+    from v119_2025_12_19_hexatop_aws_gb300 import _lib
     from v119_2025_12_19_hexatop_aws_gb300.refine import element_distribution
     from v119_2025_12_19_hexatop_aws_gb300.topopt import density_update_params
     ne = grid.nx * grid.ny * grid.nz
