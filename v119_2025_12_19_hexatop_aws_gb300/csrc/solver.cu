@@ -984,9 +984,10 @@ int solve_plain(Ctx& c, const Problem& P, const hexa_solve_params& prm, const do
 // iteration.  The choice is cached in the context per grid.
 Ctx::Tuned autotune_mixed(Ctx& c, const Problem& P, const hexa_solve_params& prm, float* fac32,
                           const ModalK<float>& K32, double sigma, PcgEnv<float>& E, float* b32, double bnorm,
-                          MG<float>& mg) {
+                          MG<float>& mg, bool search_ratio = false) {
   char key[96];
-  std::snprintf(key, sizeof(key), "%d,%d,%d,%d,%g,%g", P.g.nx, P.g.ny, P.g.nz, prm.diag_quirk, P.nu, prm.tol);
+  std::snprintf(key, sizeof(key), "%d,%d,%d,%d,%g,%g,%d", P.g.nx, P.g.ny, P.g.nz, prm.diag_quirk, P.nu, prm.tol,
+                search_ratio ? 1 : 0);
   auto it = c.tuned.find(key);
   if (it != c.tuned.end()) return it->second;
   const long long n = P.g.ndof();
@@ -1043,11 +1044,19 @@ Ctx::Tuned autotune_mixed(Ctx& c, const Problem& P, const hexa_solve_params& prm
     if (t < best) best = t, best_nu = nu;
   }
   // The lower end of the Chebyshev interval (lambda_max / ratio) stays the
-  // caller's: a short trial does not predict its effect on the full count.
-  // On the 384x192x192 cantilever with 7 levels and V(3,3), whole solves took
-  // 4421 iterations at ratio 10 against 5173 at 5 and 5381 at 30, and a solve
-  // whose 120-iteration trials had picked a ratio other than 10 took 6116
-  // where ratio 10 takes 3996.
+  // caller's for single solves: a short trial does not predict its effect on
+  // the full count.  On the 384x192x192 cantilever with 7 levels and V(3,3),
+  // whole solves took 4421 iterations at ratio 10 against 5173 at 5 and 5381
+  // at 30, and a solve whose 120-iteration trials had picked a ratio other
+  // than 10 took 6116 where ratio 10 takes 3996.  The block solve keeps the
+  // search: on 8 load cases of the 256x128x128 cantilever it took 1283 block
+  // iterations with the searched ratio and 1387 with ratio 10.
+  if (search_ratio)
+    for (int r : {5, 10, 20, 40}) {
+      if (r == r0) continue;
+      const double t = trial(best_l, best_nu, r);
+      if (t < best) best = t, best_r = r;
+    }
   Ctx::Tuned tu;
   tu.a = best_l;
   tu.b = best_nu;
@@ -1358,7 +1367,7 @@ int solve_block(Ctx& c, const Problem& P, int k, const hexa_solve_params& prm, d
         if (k == 1) E.q = qbuf;
         MG<float> tmg;
         const Ctx::Tuned t =
-            autotune_mixed(c, P0, prm, const_cast<float*>(fac), K, sigma, E, b32, fnorm[j0], tmg);
+            autotune_mixed(c, P0, prm, const_cast<float*>(fac), K, sigma, E, b32, fnorm[j0], tmg, true);
         prm2.mg_levels = t.a;
         prm2.pre_smooth = prm2.post_smooth = t.b;
         prm2.cheb_ratio = t.c;
