@@ -1049,7 +1049,7 @@ Ctx::Tuned autotune_mixed(Ctx& c, const Problem& P, const hexa_solve_params& prm
   // whole solves took 4421 iterations at ratio 10 against 5173 at 5 and 5381
   // at 30, and a solve whose 120-iteration trials had picked a ratio other
   // than 10 took 6116 where ratio 10 takes 3996.  The block solve keeps the
-  // search: on 8 load cases of the 256x128x128 cantilever it took 1283 block
+  // search: on 8 load cases of the 256x128x128 cantilever it took 1264 block
   // iterations with the searched ratio and 1387 with ratio 10.
   if (search_ratio)
     for (int r : {5, 10, 20, 40}) {
