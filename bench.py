@@ -317,6 +317,22 @@ def run_ours(a):
                  "compliance": sp["compliance"], "mixed_over_plain": ms / plain_ms,
                  "compliance_rel_diff_mixed": abs(comp_mixed - sp["compliance"]) / abs(sp["compliance"]),
                  "u_rel_diff_mixed": du}
+        try:  # sensitivities of both solutions, SIMP p=3 on the same density
+            from v119_2025_12_19_hexatop_aws_gb300 import workloads as W
+            rho_t = torch.from_numpy(np.asarray(rho, dtype=np.float64)).to(dev)
+            dcs = []
+            for uu in (u_d, u64):
+                dc = torch.empty_like(rho_t)
+                cv = C.c_double()
+                ctx.check(ctx.lib.hexa_sensitivities(ctx.h, C.byref(grid), 0.3, rho_t.data_ptr(), uu.data_ptr(),
+                                                     W.EMIN, W.E0, W.PENAL, dc.data_ptr(), C.byref(cv)),
+                          allow=(_lib.HEXA_OK,))
+                dcs.append(dc)
+            plain["dc_rel_diff_mixed"] = (torch.linalg.vector_norm(dcs[0] - dcs[1]) /
+                                          torch.linalg.vector_norm(dcs[1])).item()
+            del dcs, rho_t
+        except Exception as e:  # never voids the line
+            plain["dc_rel_diff_mixed"] = f"error: {e}"[:160]
         del u64
 
     # e2e: the same step through the C ABI with pinned host buffers
