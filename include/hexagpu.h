@@ -268,6 +268,15 @@ int hexa_remap_fields(hexa_ctx* ctx, const hexa_grid* old_g, const hexa_grid* ne
                       const float* density, const float* alpha, int32_t projection, float* new_density,
                       float* new_alpha);
 
+/* Warm start across a refinement: the nodal displacement field u_old
+ * (3 per node, node-major xyz, grid old_g) interpolated trilinearly onto the
+ * nodes of new_g spanning the same box, in FP64.  The reference resets U to
+ * zero after MeshRefiner grows the grid (src/Main.jl:412-413); passing u_new
+ * as the next solve's u_guess changes only where that solve starts.  Arrays
+ * host or device. */
+int hexa_remap_displacement(hexa_ctx* ctx, const hexa_grid* old_g, const hexa_grid* new_g, const double* u_old,
+                            double* u_new);
+
 /* ---- density update between solves (TopOpt.jl:211-482) ---------------- */
 /* The scalars update_density! reads from its arguments and its config;
  * defaults are the reference's get(...) defaults. */

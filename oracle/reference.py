@@ -642,6 +642,32 @@ def remap_fields(old, new_dims, new_h, lengths, density, alpha=None, projection=
     return val, na, raw
 
 
+def remap_displacement(old, new, u):
+    """Trilinear transfer of nodal xyz displacements from grid `old` to grid
+    `new` (element counts per axis, same box): new node i sits at old node
+    coordinate i * old_n / new_n.  No reference counterpart (the reference
+    restarts from zero after a refinement, Main.jl:412-413)."""
+    onx, ony, onz = old
+    nnx, nny, nnz = new
+    U = np.asarray(u, dtype=np.float64).reshape(onz + 1, ony + 1, onx + 1, 3)
+
+    def axis(nn, on):
+        s = np.clip(np.arange(nn + 1) * on / nn, 0.0, on)  # (i * on) / nn, as the kernel
+        i0 = np.clip(np.floor(s).astype(np.int64), 0, on - 1)
+        return i0, s - i0
+    i0, tx = axis(nnx, onx)
+    j0, ty = axis(nny, ony)
+    k0, tz = axis(nnz, onz)
+    K, J, I = np.meshgrid(np.arange(nnz + 1), np.arange(nny + 1), np.arange(nnx + 1), indexing="ij")
+    a, b, c = i0[I], j0[J], k0[K]
+    x, y, z = tx[I][..., None], ty[J][..., None], tz[K][..., None]
+    out = ((U[c, b, a] * (1 - x) + U[c, b, a + 1] * x) * (1 - y) +
+           (U[c, b + 1, a] * (1 - x) + U[c, b + 1, a + 1] * x) * y) * (1 - z) + \
+          ((U[c + 1, b, a] * (1 - x) + U[c + 1, b, a + 1] * x) * (1 - y) +
+           (U[c + 1, b + 1, a] * (1 - x) + U[c + 1, b + 1, a + 1] * x) * y) * z
+    return out.reshape(-1)
+
+
 # ---------------------------------------------------------- density update
 def density_filter_radius(p, dx, dy, dz):
     """The radius schedule of TopOpt.jl:265-298 in Float32: (R_length, R_effective)."""

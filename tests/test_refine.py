@@ -45,3 +45,18 @@ def test_oracle_remap_preserves_constant_and_linear_fields(oracle):
     # projection thresholds
     pv, _, raw = oracle.remap_fields(old, (16, 8, 8), (0.5, 0.5, 0.5), (8.0, 4.0, 4.0), lin, projection=True)
     assert np.all(pv[raw > 0.4] == 1.0) and np.all(pv[raw < 0.2] == np.float32(1e-4))
+
+
+def test_oracle_displacement_transfer_is_exact_on_trilinear_fields(oracle):
+    old, new = (4, 2, 3), (7, 5, 4)
+
+    def field(dims):
+        nx, ny, nz = dims
+        k, j, i = np.meshgrid(np.arange(nz + 1) / nz, np.arange(ny + 1) / ny, np.arange(nx + 1) / nx, indexing="ij")
+        # trilinear in the box coordinates, one combination per component
+        return np.stack([1 + 2 * i - j + 0.5 * i * j * k, 3 * k - i * k, j * k + 0.25], axis=-1).reshape(-1)
+    out = oracle.remap_displacement(old, new, field(old))
+    assert np.allclose(out, field(new), rtol=0, atol=1e-13)
+    same = oracle.remap_displacement(old, old, field(old))
+    assert np.array_equal(same, field(old))
+

@@ -122,6 +122,7 @@ SIGNATURES = {
     "hexa_filter_batch": (I32, [P, I32, C.POINTER(Grid), C.POINTER(P), D, D, I32, I32, I32, C.POINTER(P),
                                 C.POINTER(FilterStats)]),
     "hexa_filter_noalloc": (I32, [C.POINTER(Grid), P, D, D, I32, I32, P, P, C.POINTER(FilterStats)]),
+    "hexa_remap_displacement": (I32, [P, C.POINTER(Grid), C.POINTER(Grid), P, P]),
     "hexa_remap_fields": (I32, [P, C.POINTER(Grid), C.POINTER(Grid), D, D, D, P, P, I32, P, P]),
     "hexa_default_density_update_params": (None, [C.POINTER(DensityUpdateParams)]),
     "hexa_update_density": (I32, [P, C.POINTER(Grid), P, P, P, P, C.POINTER(DensityUpdateParams),

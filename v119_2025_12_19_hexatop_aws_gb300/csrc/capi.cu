@@ -930,6 +930,25 @@ int hexa_remap_fields(hexa_ctx* h, const hexa_grid* og, const hexa_grid* ng, dou
   return HEXA_OK;
 }
 
+int hexa_remap_displacement(hexa_ctx* h, const hexa_grid* og, const hexa_grid* ng, const double* u_old,
+                            double* u_new) {
+  if (!h) return HEXA_ERR_ARG;
+  if (!valid_grid(og) || !valid_grid(ng) || !u_old || !u_new) return set_err(h, HEXA_ERR_ARG, "invalid grids or null array");
+  Ctx& c = h->c;
+  c.err.clear();
+  cudaSetDevice(c.device);
+  const long long no = 3LL * (og->nx + 1) * (og->ny + 1) * (og->nz + 1);
+  const long long nn = 3LL * (ng->nx + 1) * (ng->ny + 1) * (ng->nz + 1);
+  const double* ud = stage_in<double>(c, u_old, no, "rm_u");
+  double* und = out_buf<double>(c, u_new, nn, "rm_un");
+  if (!ud || !und) return set_err(h, HEXA_ERR_NOMEM, c.err);
+  launch_remap_nodal(og->nx, og->ny, og->nz, ng->nx, ng->ny, ng->nz, ud, und, c.st);
+  c.launches++;
+  stage_out<double>(c, u_new, und, nn);
+  if (cudaStreamSynchronize(c.st) != cudaSuccess || !c.cuda_ok("remap_displacement")) return set_err(h, HEXA_ERR_CUDA, c.err);
+  return HEXA_OK;
+}
+
 int hexa_simp_factors(hexa_ctx* h, int64_t n, const double* rho, double Emin, double E0, double penal,
                       double* factor_out) {
   if (!h) return HEXA_ERR_ARG;

@@ -164,6 +164,8 @@ void launch_stress(const Grid& g, const TU* u, const float* density, float E, fl
 void launch_remap(int onx, int ony, int onz, int nnx, int nny, int nnz, float ndx, float ndy, float ndz, float lx,
                   float ly, float lz, int projection, const float* dens, const float* alpha, float* nd, float* na,
                   cudaStream_t st);
+void launch_remap_nodal(int onx, int ony, int onz, int nnx, int nny, int nnz, const double* u, double* un,
+                        cudaStream_t st);
 
 // ---- density update between solves (update.cu) -----------------------------
 struct UpdateState {

@@ -55,7 +55,52 @@ __global__ void remap_kernel(int onx, int ony, int onz, int nnx, int nny, int nn
   }
 }
 
+// Nodal displacements carried onto the grown grid as a warm start: new node
+// (i, j, k) sits at old node-index coordinates (i * onx / nnx, ...), both
+// grids spanning the same box; the three components are interpolated
+// trilinearly from the 8 surrounding old nodes in FP64.  The reference resets
+// U to zero after a refinement (Main.jl:412-413); this transfer only changes
+// the first guess of the next solve, not its answer.
+__global__ void remap_nodal_kernel(int onx, int ony, int onz, int nnx, int nny, int nnz, const double* __restrict__ u,
+                                   double* __restrict__ un) {
+  const long long NX = nnx + 1, NY = nny + 1, n = NX * NY * (long long)(nnz + 1);
+  const long long OX = onx + 1, OXY = (long long)(onx + 1) * (ony + 1);
+  for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n; q += (long long)gridDim.x * blockDim.x) {
+    const long long i = q % NX, rem = q / NX, j = rem % NY, k = rem / NY;
+    auto axis = [](long long idx, int on, int nn, int* i0, double* t) {
+      const double sc = fmin(fmax((double)idx * (double)on / (double)nn, 0.0), (double)on);
+      int a = (int)floor(sc);
+      a = a > on - 1 ? on - 1 : (a < 0 ? 0 : a);
+      *i0 = a;
+      *t = sc - (double)a;
+    };
+    int i0, j0, k0;
+    double tx, ty, tz;
+    axis(i, onx, nnx, &i0, &tx);
+    axis(j, ony, nny, &j0, &ty);
+    axis(k, onz, nnz, &k0, &tz);
+    const long long base = i0 + OX * j0 + OXY * k0;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      auto at = [&](int di, int dj, int dk) { return u[3 * (base + di + OX * dj + OXY * dk) + c]; };
+      const double c00 = at(0, 0, 0) * (1.0 - tx) + at(1, 0, 0) * tx;
+      const double c10 = at(0, 1, 0) * (1.0 - tx) + at(1, 1, 0) * tx;
+      const double c01 = at(0, 0, 1) * (1.0 - tx) + at(1, 0, 1) * tx;
+      const double c11 = at(0, 1, 1) * (1.0 - tx) + at(1, 1, 1) * tx;
+      const double c0 = c00 * (1.0 - ty) + c10 * ty, c1 = c01 * (1.0 - ty) + c11 * ty;
+      un[3 * q + c] = c0 * (1.0 - tz) + c1 * tz;
+    }
+  }
+}
+
 }  // namespace
+
+void launch_remap_nodal(int onx, int ony, int onz, int nnx, int nny, int nnz, const double* u, double* un,
+                        cudaStream_t st) {
+  const long long n = (long long)(nnx + 1) * (nny + 1) * (nnz + 1);
+  const int blocks = (int)std::max<long long>(1, std::min<long long>((n + 255) / 256, 152LL * 16));
+  remap_nodal_kernel<<<blocks, 256, 0, st>>>(onx, ony, onz, nnx, nny, nnz, u, un);
+}
 
 void launch_remap(int onx, int ony, int onz, int nnx, int nny, int nnz, float ndx, float ndy, float ndz, float lx,
                   float ly, float lz, int projection, const float* dens, const float* alpha, float* nd, float* na,

@@ -84,6 +84,18 @@ def remap_fields(old_grid, new_grid, lengths, density, alpha=None, *, projection
     return nd, na
 
 
+def remap_displacement(old_grid, new_grid, u, *, ctx=None):
+    """Nodal displacements of old_grid interpolated onto new_grid (same box)
+    as a warm start for the next solve (hexa_remap_displacement); float64."""
+    ctx = ctx or context()
+    nn = 3 * (new_grid.nx + 1) * (new_grid.ny + 1) * (new_grid.nz + 1)
+    out = np.empty(nn, np.float64)
+    rc = ctx.lib.hexa_remap_displacement(ctx.h, C.byref(old_grid), C.byref(new_grid),
+                                         _lib.ptr(np.ascontiguousarray(u, dtype=np.float64)), _lib.ptr(out))
+    ctx.check(rc, allow=(_lib.HEXA_OK,))
+    return out
+
+
 def refine_mesh_and_fields(grid, density, alpha, target_active, lengths, *, max_growth_rate=1.2,
                            hard_element_limit=800_000_000, update_method="hard", memory_limit=None, ctx=None):
     """Returns (grid, density, alpha, plan): the old ones when no refinement."""
