@@ -1,4 +1,7 @@
-"""CPU restatement of the reference's FE-solve path (numpy/scipy + hexa_oracle.c).
+"""CPU restatement of the reference's FE-solve path (numpy/scipy + hexa_oracle.c):
+the operator, the PCG control flow with its Jacobi and two-level multigrid
+preconditioners, the filter, SIMP/OC, and the rows either side of the solve
+(stress, density update, refiner transfer).
 
 TEST INFRASTRUCTURE ONLY -- the parity checker and the timed CPU baseline.
 Every function names the reference file:lines it restates (paths relative
@@ -163,9 +166,84 @@ class PcgInfo:
     name: str
 
 
+class ReferenceMG:
+    """The reference's two-level additive preconditioner, restated in numpy:
+    setup_multigrid and apply_mg_vcycle! (GPUGeometricMultigrid.jl:252-346)
+    with the restriction / prolongation kernels (:60-204), in Float32 as the
+    reference's workspace.  z = D^-1 r (fine Jacobi) + P (r_c ./ (D_c + 1e-9)),
+    r_c = P^T r: P interpolates trilinearly from the nodes of a grid of
+    max(1, n/2) elements per axis (element size 2h) at the fine nodes'
+    coordinates, D_c is 1 plus the x-diagonal of the unit-modulus coarse K0
+    (nu fixed at 0.3) summed over the coarse elements that hold a fine node
+    (modulus 1, the rest 0.001).  Atomic sums run in a fixed order here."""
+
+    def __init__(self, g: Grid, free):
+        f32 = np.float32
+        self.g, self.free = g, np.asarray(free)
+        nxc, nyc, nzc = max(1, g.nx // 2), max(1, g.ny // 2), max(1, g.nz // 2)
+        self.nc = (nxc, nyc, nzc)
+        hc = [f32(f32(h) * f32(2.0)) for h in (g.dx, g.dy, g.dz)]
+        NX, NY, NZ = g.nx + 1, g.ny + 1, g.nz + 1
+        k, j, i = np.meshgrid(np.arange(NZ), np.arange(NY), np.arange(NX), indexing="ij")
+        # node coordinates (i-1)*dx in Float32 (Mesh.jl:36), normalised by the coarse size (:206-214)
+        coords = [(a.ravel().astype(f32) * f32(h)) / hcc for a, h, hcc in zip((i, j, k), (g.dx, g.dy, g.dz), hc)]
+        lo = [np.floor(c).astype(np.int64) for c in coords]
+        t = [(c - l.astype(f32)).astype(f32) for c, l in zip(coords, lo)]
+        one = f32(1.0)
+        self.corners = []
+        for dk in (0, 1):
+            for dj in (0, 1):
+                for di in (0, 1):
+                    ci, cj, ck = lo[0] + di, lo[1] + dj, lo[2] + dk
+                    wx = t[0] if di else one - t[0]
+                    wy = t[1] if dj else one - t[1]
+                    wz = t[2] if dk else one - t[2]
+                    w = ((wx * wy) * wz).astype(f32)
+                    ok = (ci >= 0) & (cj >= 0) & (ck >= 0) & (ci <= nxc) & (cj <= nyc) & (ck <= nzc)
+                    self.corners.append((np.nonzero(ok)[0], (ci + cj * (nxc + 1) + ck * (nxc + 1) * (nyc + 1))[ok],
+                                         w[ok]))
+        # corner order of the kernels: (0,0,0) (1,0,0) (0,1,0) (1,1,0) (0,0,1) (1,0,1) (0,1,1) (1,1,1)
+        # coarse modulus: 1 where a fine node's floor lands inside, else 0.001 (:218-229)
+        ex, ey, ez = lo
+        inside = (ex >= 0) & (ey >= 0) & (ez >= 0) & (ex < nxc) & (ey < nyc) & (ez < nzc)
+        rho_c = np.full(nxc * nyc * nzc, f32(0.001))
+        rho_c[(ex + ey * nxc + ez * nxc * nyc)[inside]] = f32(1.0)
+        kd = np.diag(canonical_stiffness(float(hc[0]), float(hc[1]), float(hc[2]), 0.3, fp32=True)).astype(f32)
+        gc = Grid(nxc, nyc, nzc)
+        en = element_nodes(gc)
+        self.nnc = gc.nnode
+        Dc = np.ones(3 * gc.nnode, f32)  # fill!(diag_coarse, 1.0f0), then the atomic adds (:47-58)
+        for a in range(8):
+            kv = (kd[3 * a] * rho_c).astype(f32)
+            for c in range(3):
+                np.add.at(Dc, 3 * en[:, a] + c, kv)
+        self.Dc = Dc
+
+    def apply(self, r_free, Minv):
+        f32 = np.float32
+        z = r_free * Minv
+        rf = np.zeros(self.g.ndof, f32)
+        rf[self.free] = np.asarray(r_free).astype(f32)
+        rc = np.zeros(3 * self.nnc, f32)
+        for nodes, cidx, w in self.corners:
+            for c in range(3):
+                np.add.at(rc, 3 * cidx + c, (rf[3 * nodes + c] * w).astype(f32))
+        xc = (rc / (self.Dc + f32(1e-9))).astype(f32)
+        zf = np.zeros(self.g.ndof, f32)
+        for nodes, cidx, w in self.corners:
+            for c in range(3):
+                zf[3 * nodes + c] = (zf[3 * nodes + c] + (xc[3 * cidx + c] * w).astype(f32)).astype(f32)
+        return z + zf[self.free].astype(np.float64)
+
+
 def pcg_reference(g: Grid, K0, factor, f, fixed, *, tol, max_iter, shift_factor, stagnation_tol=0.0,
-                  max_shift_attempts=3, shift_multiplier=10.0, u_guess=None, diag_quirk=True, cadence=10):
-    """Jacobi branch of gpu_matrix_free_cg_solve (GPUSolver.jl:182-465) on free DOFs."""
+                  max_shift_attempts=3, shift_multiplier=10.0, u_guess=None, diag_quirk=True, cadence=10,
+                  precond="jacobi"):
+    """gpu_matrix_free_cg_solve (GPUSolver.jl:182-465) on the free DOFs, FP64:
+    shift attempts, the NaN/divergence tests, stagnation acceptance, the
+    best-iterate return and, with precond="multigrid", the reference's
+    two-level preconditioner (ReferenceMG) with its fall-back to Jacobi on a
+    NaN or divergence (:389-437).  Returns (u, final relres, PcgInfo)."""
     free = ~fixed
     d = diag_K(g, K0, factor, quirk=diag_quirk)[free]
     max_diag = d.max()
@@ -180,69 +258,84 @@ def pcg_reference(g: Grid, K0, factor, f, fixed, *, tol, max_iter, shift_factor,
         full[free] = v
         return apply_K(g, K0, factor, full)[free]
 
+    want_mg = precond == "multigrid"
+    mg = ReferenceMG(g, free) if want_mg else None
+    use_mg = want_mg
     x = np.zeros(n)
     best_x = np.zeros(n)
     final_rel = 0.0
-    cur_shift = shift_factor
     success = False
     iters, shifts = [], []
-    for attempt in range(1, max_shift_attempts + 1):
-        real_shift = cur_shift * max_diag
-        shifts.append(real_shift)
-        diverged = False
-        if u_guess is not None and attempt == 1:
-            x = np.asarray(u_guess, dtype=np.float64)[free].copy()
-        elif attempt > 1:
-            x = np.zeros(n)
-        Minv = 1.0 / (d + real_shift)
-        r = b - (A(x) + real_shift * x)
-        z = r * Minv
-        p = z.copy()
-        rz = r @ z
-        best_rel = np.inf
-        solve_ok = False
-        k = 0
-        for k in range(1, max_iter + 1):
-            Ap = A(p) + real_shift * p
-            denom = p @ Ap
-            if abs(denom) < 1e-20:
+    while True:
+        cur_shift = shift_factor
+        fallback = False
+        for attempt in range(1, max_shift_attempts + 1):
+            real_shift = cur_shift * max_diag
+            shifts.append(real_shift)
+            diverged = False
+            if u_guess is not None and attempt == 1 and use_mg == want_mg:
+                x = np.asarray(u_guess, dtype=np.float64)[free].copy()
+            elif attempt > 1 or use_mg != want_mg:
+                x = np.zeros(n)
+            Minv = 1.0 / (d + real_shift)
+            M = (lambda v: mg.apply(v, Minv)) if use_mg else (lambda v: v * Minv)
+            r = b - (A(x) + real_shift * x)
+            z = M(r)
+            p = z.copy()
+            rz = r @ z
+            best_rel = np.inf
+            solve_ok = False
+            k = 0
+            for k in range(1, max_iter + 1):
+                Ap = A(p) + real_shift * p
+                denom = p @ Ap
+                if abs(denom) < 1e-20:
+                    break
+                alpha = rz / denom
+                x = x + alpha * p
+                r = r - alpha * Ap
+                if k == 1 or (cadence <= 1) or k % cadence == 0:
+                    rel = np.linalg.norm(r) / norm_b
+                    final_rel = rel
+                    if rel < best_rel:
+                        best_rel = rel
+                        best_x = x.copy()
+                    if rel < tol:
+                        solve_ok = True
+                        break
+                    if np.isnan(rel) or np.isinf(rel) or rel > 10.0 or (k > 500 and rel > best_rel * 100.0):
+                        if use_mg:
+                            fallback = True
+                        else:
+                            diverged = True
+                        break
+                z = M(r)
+                rz_new = r @ z
+                p = z + (rz_new / rz) * p
+                rz = rz_new
+            iters.append(k)
+            if fallback:
                 break
-            alpha = rz / denom
-            x = x + alpha * p
-            r = r - alpha * Ap
-            if k == 1 or (cadence <= 1) or k % cadence == 0:
-                rel = np.linalg.norm(r) / norm_b
-                final_rel = rel
-                if rel < best_rel:
-                    best_rel = rel
-                    best_x = x.copy()
-                if rel < tol:
-                    solve_ok = True
-                    break
-                if np.isnan(rel) or np.isinf(rel) or rel > 10.0 or (k > 500 and rel > best_rel * 100.0):
-                    diverged = True
-                    break
-            z = r * Minv
-            rz_new = r @ z
-            p = z + (rz_new / rz) * p
-            rz = rz_new
-        iters.append(k)
-        if solve_ok:
-            success = True
-            break
-        if diverged and attempt < max_shift_attempts:
+            if solve_ok:
+                success = True
+                break
+            if diverged and attempt < max_shift_attempts:
+                cur_shift *= shift_multiplier
+                continue
+            if stagnation_tol > 0.0 and best_rel < stagnation_tol:
+                success = True
+                x = best_x
+                break
             cur_shift *= shift_multiplier
+        if fallback:  # restart every attempt with the Jacobi preconditioner
+            use_mg = False
             continue
-        if stagnation_tol > 0.0 and best_rel < stagnation_tol:
-            success = True
-            x = best_x
-            break
-        cur_shift *= shift_multiplier
+        break
     if not success:
         x = best_x
     u = np.zeros(g.ndof)
     u[free] = x
-    return u, final_rel, PcgInfo(iters, shifts, final_rel, success, "Jacobi_GPU")
+    return u, final_rel, PcgInfo(iters, shifts, final_rel, success, "GMG_GPU" if use_mg else "Jacobi_GPU")
 
 
 def cg_tight(g: Grid, K0, factor, f, fixed, sigma=0.0, tol=1e-13, max_iter=200000, x0=None):

@@ -71,6 +71,71 @@ def test_reference_pcg_failure_paths(oracle, rng):
     assert i3.name == "Failed_Corrupt_Input" and np.isnan(r3)
 
 
+def test_reference_multigrid_preconditioner(oracle, rng):
+    """The restated two-level preconditioner of GPUGeometricMultigrid.jl."""
+    g = oracle.Grid(8, 4, 4)
+    fixed = oracle.fixed_mask(g, 1)
+    free = ~fixed
+    mg = oracle.ReferenceMG(g, free)
+    assert mg.nc == (4, 2, 2)
+    # even grids: every fine node's trilinear weights sum to 1 (nothing falls outside)
+    wsum = np.zeros(g.nnode, np.float32)
+    for nodes, _, w in mg.corners:
+        np.add.at(wsum, nodes, w)
+    assert np.allclose(wsum, 1.0, atol=1e-7)
+    # D_c = 1 + (adjacent coarse elements) x the x-diagonal of the unit coarse K0
+    kd = np.diag(oracle.canonical_stiffness(2, 2, 2, 0.3, fp32=True))[0]
+    assert mg.Dc[0] == np.float32(1.0) + np.float32(kd)  # a corner node: one element
+    # symmetric positive (additive Jacobi + P D_c^-1 P^T), to Float32 rounding
+    n = int(free.sum())
+    Minv = rng.uniform(0.5, 1.0, n)
+    a, b = rng.standard_normal(n), rng.standard_normal(n)
+    Ma, Mb = mg.apply(a, Minv), mg.apply(b, Minv)
+    assert abs(b @ Ma - a @ Mb) <= 1e-5 * abs(b @ Ma) and a @ Ma > 0
+    # odd grids drop the weight of coarse nodes beyond the coarse grid, as the reference's range test does
+    g3 = oracle.Grid(5, 3, 3)
+    mg3 = oracle.ReferenceMG(g3, ~oracle.fixed_mask(g3, 1))
+    w3 = np.zeros(g3.nnode, np.float32)
+    for nodes, _, w in mg3.corners:
+        np.add.at(w3, nodes, w)
+    assert w3.min() < 1.0 and w3.max() == np.float32(1.0)
+
+
+def test_reference_multigrid_pcg_matches_direct(oracle, rng):
+    g = oracle.Grid(8, 4, 4)
+    K0 = oracle.canonical_stiffness(1, 1, 1, 0.3)
+    fac = rng.uniform(0.2, 1, g.nelem)
+    fixed = oracle.fixed_mask(g, 1)
+    f = workloads.edge_load(8, 4, 4)
+    # the preconditioned residual of this unit load meets the reference's absolute
+    # |p.Ap| < 1e-20 breakdown test near relres 2e-8 (GPUSolver.jl:374), so 1e-7 here
+    u, rel, info = oracle.pcg_reference(g, K0, fac, f, fixed, tol=1e-7, max_iter=10000, shift_factor=1e-10,
+                                        precond="multigrid")
+    assert info.success and info.name == "GMG_GPU" and rel < 1e-7
+    ud = oracle.direct_solve(g, K0, fac, f, fixed, info.shifts[0])
+    assert np.linalg.norm(u - ud) < 1e-5 * np.linalg.norm(ud)
+    _, rel9, i9 = oracle.pcg_reference(g, K0, fac, f, fixed, tol=1e-9, max_iter=10000, shift_factor=1e-10,
+                                       precond="multigrid")
+    assert not i9.success and len(i9.shifts) == 3 and rel9 < 1e-7  # every attempt ends in that test
+    _, _, ij = oracle.pcg_reference(g, K0, fac, f, fixed, tol=1e-9, max_iter=10000, shift_factor=1e-10)
+    assert ij.name == "Jacobi_GPU"
+
+
+def test_reference_multigrid_falls_back_to_jacobi(oracle, rng, monkeypatch):
+    """A NaN from the multigrid preconditioner restarts every attempt with
+    Jacobi (GPUSolver.jl:389-437); the fault is planted in the oracle's MG."""
+    g = oracle.Grid(8, 4, 4)
+    K0 = oracle.canonical_stiffness(1, 1, 1, 0.3)
+    fac = rng.uniform(0.2, 1, g.nelem)
+    fixed = oracle.fixed_mask(g, 1)
+    f = workloads.edge_load(8, 4, 4)
+    monkeypatch.setattr(oracle.ReferenceMG, "apply", lambda self, r, Minv: np.full_like(r, np.nan))
+    u, rel, info = oracle.pcg_reference(g, K0, fac, f, fixed, tol=1e-9, max_iter=10000, shift_factor=1e-10,
+                                        precond="multigrid")
+    assert info.success and info.name == "Jacobi_GPU" and rel < 1e-9
+    assert len(info.iterations) == 2 and info.iterations[0] == 1  # MG stopped at the first check
+
+
 def test_helmholtz_reference_vs_direct(oracle, rng):
     g = oracle.Grid(10, 6, 4)
     rho = rng.uniform(0, 1, g.nelem)
