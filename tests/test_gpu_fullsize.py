@@ -1,0 +1,91 @@
+"""Parity at the full 256x128x128 grid (12.8 M DOF) through properties that
+do not need the oracle to solve it: the operator's symmetry, its rigid-body
+null space and determinism, the FP32 operator against the FP64 one, the
+mixed solve's true residual recomputed through a separate operator call and
+its energy identity, and the element-wise rows (density update, refiner
+transfer) bit-exact against the oracle at this size."""
+import numpy as np
+import pytest
+
+from v119_2025_12_19_hexatop_aws_gb300 import _lib, workloads as W
+from v119_2025_12_19_hexatop_aws_gb300.helmholtz import filter_density
+from v119_2025_12_19_hexatop_aws_gb300.refine import domain_lengths, element_distribution, remap_fields
+from v119_2025_12_19_hexatop_aws_gb300.solver import apply_operator, solve
+from v119_2025_12_19_hexatop_aws_gb300.topopt import density_update_params, update_density_gpu
+
+pytestmark = pytest.mark.gpu
+DIMS = W.SIZES["c2"]
+
+
+@pytest.fixture(scope="module")
+def c2(ctx):
+    grid = _lib.make_grid(*DIMS)
+
+    def filt(g, R):
+        out, _ = filter_density(grid, np.ascontiguousarray(g), R, tol=1e-10, max_iter=20000, quirk=False, ctx=ctx)
+        return out
+
+    rho = W.smooth_density(*DIMS, filt)
+    fac = W.EMIN + rho ** W.PENAL * (W.E0 - W.EMIN)
+    return grid, rho, fac, W.edge_load(*DIMS)
+
+
+def test_operator_properties_at_full_size(ctx, c2):
+    grid, _, fac, _ = c2
+    rng = np.random.default_rng(7)
+    n = W.ndof(*DIMS)
+    x, y = rng.standard_normal(n), rng.standard_normal(n)
+    Kx = apply_operator(grid, fac, x, ctx=ctx)
+    Ky = apply_operator(grid, fac, y, ctx=ctx)
+    assert abs(y @ Kx - x @ Ky) <= 1e-12 * np.linalg.norm(y) * np.linalg.norm(Kx)
+    assert np.array_equal(Kx, apply_operator(grid, fac, x, ctx=ctx))  # bitwise deterministic
+    for c in range(3):  # rigid translations are in the null space
+        t = np.zeros(n)
+        t[c::3] = 1.0
+        assert np.abs(apply_operator(grid, fac, t, ctx=ctx)).max() <= 1e-12 * np.abs(Kx).max()
+    K32 = apply_operator(grid, fac.astype(np.float32), x.astype(np.float32), ctx=ctx, fp32=True)
+    assert np.abs(K32 - Kx).max() <= 2e-6 * np.abs(Kx).max()
+
+
+def test_mixed_solve_true_residual_and_energy_at_full_size(ctx, c2):
+    grid, _, fac, f = c2
+    p = _lib.default_params(precision="mixed", divergence_check=0, tol=1e-9, max_iter=60000)
+    u, st = solve(grid, fac, f, clamp_faces=1, params=p, ctx=ctx)
+    assert st["status"] == 0 and st["true_relres"] <= 1e-9
+    # the residual again, through a separate operator call (f and the operator's
+    # output are both zero at the clamped DOFs)
+    Au = apply_operator(grid, fac, u, sigma=st["shift"], clamp_faces=1, ctx=ctx)
+    r = f - Au
+    assert np.linalg.norm(r) <= 1.05e-9 * np.linalg.norm(f)
+    comp = f @ u
+    assert abs(st["compliance"] - comp) <= 1e-12 * abs(comp)
+    # energy: u.(K + sigma I)u = f.u - u.r, and |u.r| <= |u| |r| (Cauchy-Schwarz)
+    assert abs(u @ Au - comp) <= 1.1e-9 * np.linalg.norm(u) * np.linalg.norm(f) + 1e-12 * abs(comp)
+
+
+def test_elementwise_rows_bit_exact_at_full_size(ctx, oracle, c2):
+    grid, rho, _, _ = c2
+    ne = DIMS[0] * DIMS[1] * DIMS[2]
+    rng = np.random.default_rng(11)
+    dens = rho.astype(np.float32)
+    l1 = (rng.uniform(0.0, 1.5, ne) * 200.0).astype(np.float32)
+    prot = rng.uniform(size=ne) < 0.02
+    orig = np.ones(ne, np.float32)
+    p = density_update_params(E=200.0, iter=30, number_of_iterations=30, minimum_filter_radius_as_elements=0.0,
+                              max_domain_dim=float(DIMS[0]), hard_update=1)
+    d_gpu = dens.copy()
+    st = update_density_gpu(grid, d_gpu, l1, prot, orig, p, ctx=ctx)
+    keys = ("E", "l1_stress_allowable", "iter", "number_of_iterations", "min_density", "max_density",
+            "max_domain_dim", "filter_R_init_perc", "filter_R_interm_perc", "filter_R_final_perc",
+            "filter_R_interm_iter_perc", "minimum_filter_radius_as_elements", "filter_tolerance",
+            "final_density_threshold", "max_culling_ratio", "hard_update")
+    ref, rs = oracle.update_density(dens, l1, prot, orig, {k: getattr(p, k) for k in keys}, (1.0, 1.0, 1.0))
+    assert np.array_equal(d_gpu, ref)
+    assert (st["active_count"], st["candidates"], st["culled"]) == (rs["active_count"], rs["candidates"], rs["culled"])
+    assert st["candidates"] > st["culled"] > 0
+    L = domain_lengths(grid)
+    nx, ny, nz, dx, dy, dz, cnt = element_distribution(*L, int(ne * 1.2))
+    ng = _lib.make_grid(nx, ny, nz, dx, dy, dz)
+    nd, na = remap_fields(grid, ng, L, dens, orig, projection=True, ctx=ctx)
+    rd, ra, _ = oracle.remap_fields(DIMS, (nx, ny, nz), (ng.dx, ng.dy, ng.dz), L, dens, orig, True)
+    assert np.array_equal(nd, rd) and np.array_equal(na, ra)
