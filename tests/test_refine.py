@@ -1,6 +1,7 @@
 """Mesh growth: the refinement decision (host, MeshRefiner.jl:101-146,
 Helpers.calculate_element_distribution) and the oracle's field transfer."""
 import numpy as np
+import pytest
 
 from v119_2025_12_19_hexatop_aws_gb300.refine import element_distribution, plan_refinement
 
@@ -60,3 +61,57 @@ def test_oracle_displacement_transfer_is_exact_on_trilinear_fields(oracle):
     same = oracle.remap_displacement(old, old, field(old))
     assert np.array_equal(same, field(old))
 
+
+
+def _remap_loops(old, new, new_h, lengths, density, alpha, projection):
+    """MeshRefiner.jl:201-237 transcribed with its 1-based indices, one
+    element at a time in Float32: a cross-check of the vectorised oracle."""
+    f32 = np.float32
+    onx, ony, onz = old
+    nnx, nny, nnz = new
+    nd, na = [], []
+    for e_new in range(1, nnx * nny * nnz + 1):
+        iz = (e_new - 1) // (nnx * nny) + 1
+        rem = (e_new - 1) % (nnx * nny)
+        iy = rem // nnx + 1
+        ix = rem % nnx + 1
+        cx = (f32(ix) - f32(0.5)) * f32(new_h[0])
+        cy = (f32(iy) - f32(0.5)) * f32(new_h[1])
+        cz = (f32(iz) - f32(0.5)) * f32(new_h[2])
+        u = min(max((cx / f32(lengths[0])) * f32(onx), f32(0.5)), f32(onx) - f32(0.5))
+        v = min(max((cy / f32(lengths[1])) * f32(ony), f32(0.5)), f32(ony) - f32(0.5))
+        w = min(max((cz / f32(lengths[2])) * f32(onz), f32(0.5)), f32(onz) - f32(0.5))
+        u0, v0, w0 = int(np.floor(u - f32(0.5))), int(np.floor(v - f32(0.5))), int(np.floor(w - f32(0.5)))
+        tx, ty, tz = (u - f32(0.5)) - f32(u0), (v - f32(0.5)) - f32(v0), (w - f32(0.5)) - f32(w0)
+        i0, i1 = min(max(u0 + 1, 1), onx), min(max(u0 + 2, 1), onx)
+        j0, j1 = min(max(v0 + 1, 1), ony), min(max(v0 + 2, 1), ony)
+        k0, k1 = min(max(w0 + 1, 1), onz), min(max(w0 + 2, 1), onz)
+
+        def d(i, j, k):
+            return f32(density[i + (j - 1) * onx + (k - 1) * onx * ony - 1])
+        ctx, cty, ctz = (min(max(t, f32(0)), f32(1)) for t in (tx, ty, tz))
+        one = f32(1)
+        c00 = d(i0, j0, k0) * (one - ctx) + d(i1, j0, k0) * ctx
+        c10 = d(i0, j1, k0) * (one - ctx) + d(i1, j1, k0) * ctx
+        c01 = d(i0, j0, k1) * (one - ctx) + d(i1, j0, k1) * ctx
+        c11 = d(i0, j1, k1) * (one - ctx) + d(i1, j1, k1) * ctx
+        c0 = c00 * (one - cty) + c10 * cty
+        c1 = c01 * (one - cty) + c11 * cty
+        val = c0 * (one - ctz) + c1 * ctz
+        if projection:
+            val = f32(1.0) if val > f32(0.4) else (f32(0.0001) if val < f32(0.2) else val)
+        nd.append(val)
+        na.append(f32(alpha[i0 + (j0 - 1) * onx + (k0 - 1) * onx * ony - 1]))
+    return np.array(nd, np.float32), np.array(na, np.float32)
+
+
+@pytest.mark.parametrize("projection", [False, True])
+def test_vectorised_remap_matches_the_loop_transcription(oracle, projection):
+    rng = np.random.default_rng(5)
+    old, new, L = (7, 4, 3), (9, 5, 4), (7.0, 4.0, 3.0)
+    h = tuple(float(np.float32(np.float32(Li) / np.float32(n))) for Li, n in zip(L, new))
+    dens = rng.uniform(0, 1, 84).astype(np.float32)
+    alpha = rng.uniform(-1, 1, 84).astype(np.float32)
+    nd, na, _ = oracle.remap_fields(old, new, h, L, dens, alpha, projection)
+    rd, ra = _remap_loops(old, new, h, L, dens, alpha, projection)
+    assert np.array_equal(nd, rd) and np.array_equal(na, ra)

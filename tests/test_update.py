@@ -73,3 +73,68 @@ def test_update_protected_and_nan_paths(oracle):
     new2, st2 = oracle.update_density(np.full(4, 0.3, F32), l1, prot, orig, p, (0.1, 0.1, 0.1),
                                       filter_fn=lambda x, r: np.full_like(x, np.nan))
     assert st2["filter_used"] == 1 and st2["filter_nan_fallback"] == 1 and np.array_equal(new2, new)
+
+
+def _update_loops(density, l1, prot, E, allow, it, n_it, orig, min_d, max_d, opt, h):
+    """update_density! (TopOpt.jl:211-482) transcribed statement by statement
+    in pure-Python loops over Float32 scalars, without a filter (R_effective
+    at or below 1e-4): a cross-check of the vectorised restatement."""
+    f32 = np.float32
+    dens = [f32(v) for v in density]
+    ne = len(dens)
+    prop = [orig[e] if prot[e] else max((f32(l1[e]) / f32(allow)) / f32(E), f32(min_d)) for e in range(ne)]
+    change, active1 = 0.0, 0
+    for e in range(ne):
+        if not prot[e]:
+            old = dens[e]
+            raw = max(prop[e], f32(min_d))
+            dens[e] = raw
+            change += float(abs(min(raw, f32(max_d)) - old))
+            if dens[e] > f32(min_d):
+                active1 += 1
+    mean = f32(f32(change) / f32(active1)) if active1 > 0 else f32(0)
+    if it > n_it:
+        thr = f32(opt["final_density_threshold"])
+    else:
+        thr = f32(opt["final_density_threshold"]) * min(max(f32(it) / f32(n_it), f32(0)), f32(1))
+    cands, active = [], 0
+    for e in range(ne):
+        if not prot[e]:
+            if dens[e] > f32(max_d):
+                dens[e] = f32(max_d)
+            if dens[e] > f32(min_d):
+                active += 1
+                if dens[e] < thr:
+                    cands.append(e)
+        elif orig[e] > f32(min_d):
+            active += 1
+    allowed = int(np.floor(f32(active) * f32(opt["max_culling_ratio"])))
+    if len(cands) > allowed:
+        cands = sorted(cands, key=lambda e: dens[e])[:allowed]  # Python's sort is stable, as Julia's
+    for e in cands:
+        dens[e] = f32(min_d)
+    if opt.get("hard_update"):
+        for e in range(ne):
+            if not prot[e] and dens[e] > f32(min_d):
+                dens[e] = f32(1.0)
+    for e in range(ne):
+        if prot[e]:
+            dens[e] = orig[e]
+    return np.array(dens, np.float32), mean, active, len(cands)
+
+
+@pytest.mark.parametrize("it,hard", [(3, 0), (30, 1), (45, 0)])
+def test_vectorised_update_matches_the_loop_transcription(oracle, it, hard):
+    rng = np.random.default_rng(it)
+    ne = 600
+    dens = rng.uniform(0, 1, ne).astype(F32)
+    l1 = (rng.uniform(0, 1.5, ne) * 50).astype(F32)
+    l1[rng.uniform(size=ne) < 0.3] = F32(0.5)  # ties
+    prot = rng.uniform(size=ne) < 0.1
+    orig = np.where(rng.uniform(size=ne) < 0.5, F32(1.0), F32(0.0)).astype(F32)
+    p = params(E=50.0, iter=it, number_of_iterations=30, hard_update=hard, max_culling_ratio=0.2)
+    new, st = oracle.update_density(dens, l1, prot, orig, p, (0.1, 0.1, 0.1))
+    ref, mean, active, culled = _update_loops(dens, l1, prot, 50.0, 1.0, it, 30, orig, p["min_density"],
+                                              p["max_density"], p, (0.1, 0.1, 0.1))
+    assert np.array_equal(new, ref)
+    assert st["active_count"] == active and st["culled"] == culled and st["mean_change"] == mean
