@@ -582,6 +582,52 @@ def _jacobi_rotate(spp, sqq, spq, spr, sqr, v, p, q):
         v[r][q][act] = vq_n[act]
 
 
+def eigen3x3(sxx, syy, szz, sxy, syz, sxz):
+    """eigen3x3_device (Stress.jl:95-157) on arrays of symmetric tensors,
+    Float32: at most 12 sweeps of the (1,2), (1,3), (2,3) Jacobi rotations,
+    stopped per tensor once every off-diagonal is below 1e-9, then sorted
+    descending.  Returns (eigenvalues (n, 3), direction of the largest (n, 3),
+    direction of the smallest (n, 3))."""
+    f32 = np.float32
+    n = np.asarray(sxx).size
+    s11, s22, s33, s12, s23, s13 = (np.asarray(a, dtype=f32).reshape(-1).copy() for a in (sxx, syy, szz, sxy, syz, sxz))
+    v = [[np.full(n, f32(1.0 if r == c else 0.0)) for c in range(3)] for r in range(3)]
+    done = np.zeros(n, bool)
+    for _ in range(12):
+        done |= np.maximum(np.abs(s12), np.maximum(np.abs(s23), np.abs(s13))) < f32(1e-9)
+        live = ~done
+        if not live.any():
+            break
+        sub = [a[live] for a in (s11, s22, s33, s12, s23, s13)]
+        vs = [[v[r][c][live] for c in range(3)] for r in range(3)]
+        a11, a22, a33, a12, a23, a13 = sub
+        _jacobi_rotate(a11, a22, a12, a13, a23, vs, 0, 1)
+        _jacobi_rotate(a11, a33, a13, a12, a23, vs, 0, 2)
+        _jacobi_rotate(a22, a33, a23, a12, a13, vs, 1, 2)
+        for arr, new in zip((s11, s22, s33, s12, s23, s13), (a11, a22, a33, a12, a23, a13)):
+            arr[live] = new
+        for r in range(3):
+            for c in range(3):
+                v[r][c][live] = vs[r][c]
+
+    def swap(ma, mb, ca, cb):
+        m = ma < mb
+        ta = ma.copy()
+        ma[m] = mb[m]
+        mb[m] = ta[m]
+        for r in range(3):
+            t = v[r][ca].copy()
+            v[r][ca][m] = v[r][cb][m]
+            v[r][cb][m] = t[m]
+    swap(s11, s22, 0, 1)
+    swap(s22, s33, 1, 2)
+    swap(s11, s22, 0, 1)
+    principal = np.stack([s11, s22, s33], axis=1)
+    dmax = np.stack([v[0][0], v[1][0], v[2][0]], axis=1)
+    dmin = np.stack([v[0][2], v[1][2], v[2][2]], axis=1)
+    return principal, dmax, dmin
+
+
 def stress_field(g: Grid, u, density, E, nu):
     """Stress.stress_kernel! (Stress.jl:159-285) restated in numpy, Float32, all
     elements at once: centre-point strain/stress with E_loc = E*density, von
@@ -644,41 +690,8 @@ def stress_field(g: Grid, u, density, E, nu):
     voigt = np.stack([sxx, syy, szz, sxy, syz, sxz], axis=1)
     vm = np.sqrt(np.maximum(f32(0.0), f32(0.5) * ((sxx - syy) ** 2 + (syy - szz) ** 2 + (szz - sxx) ** 2)
                             + f32(3.0) * (sxy ** 2 + syz ** 2 + sxz ** 2)))
-    s11, s22, s33, s12, s23, s13 = (a.astype(f32).copy() for a in (sxx, syy, szz, sxy, syz, sxz))
-    v = [[np.full(ne, f32(1.0 if r == c else 0.0)) for c in range(3)] for r in range(3)]
-    done = np.zeros(ne, bool)
-    for _ in range(12):
-        done |= np.maximum(np.abs(s12), np.maximum(np.abs(s23), np.abs(s13))) < f32(1e-9)
-        live = ~done
-        if not live.any():
-            break
-        sub = [a[live] for a in (s11, s22, s33, s12, s23, s13)]
-        vs = [[v[r][c][live] for c in range(3)] for r in range(3)]
-        a11, a22, a33, a12, a23, a13 = sub
-        _jacobi_rotate(a11, a22, a12, a13, a23, vs, 0, 1)
-        _jacobi_rotate(a11, a33, a13, a12, a23, vs, 0, 2)
-        _jacobi_rotate(a22, a33, a23, a12, a13, vs, 1, 2)
-        for arr, new in zip((s11, s22, s33, s12, s23, s13), (a11, a22, a33, a12, a23, a13)):
-            arr[live] = new
-        for r in range(3):
-            for c in range(3):
-                v[r][c][live] = vs[r][c]
-
-    def swap(ma, mb, ca, cb):
-        m = ma < mb
-        ta = ma.copy()
-        ma[m] = mb[m]
-        mb[m] = ta[m]
-        for r in range(3):
-            t = v[r][ca].copy()
-            v[r][ca][m] = v[r][cb][m]
-            v[r][cb][m] = t[m]
-    swap(s11, s22, 0, 1)
-    swap(s22, s33, 1, 2)
-    swap(s11, s22, 0, 1)
-    principal = np.stack([s11, s22, s33], axis=1)
-    dmax = np.stack([v[0][0], v[1][0], v[2][0]], axis=1)
-    dmin = np.stack([v[0][2], v[1][2], v[2][2]], axis=1)
+    principal, dmax, dmin = eigen3x3(sxx, syy, szz, sxy, syz, sxz)
+    s11, s22, s33 = principal[:, 0], principal[:, 1], principal[:, 2]
     l1 = np.abs(s11) + np.abs(s22) + np.abs(s33)
     zero = dens < f32(1e-6)
     for arr in (principal, dmax, dmin, voigt):

@@ -200,3 +200,62 @@ def test_stress_oracle_principal_stresses_are_eigenvalues(oracle, rng):
         d = out[key].astype(np.float64)
         assert np.allclose(np.linalg.norm(d, axis=1), 1.0, atol=1e-5)
         assert np.all(np.abs(np.sum(d * vec[:, :, col], axis=1)) >= 1 - 1e-4)
+
+
+def _eigen3x3_loops(s11, s22, s33, s12, s23, s13):
+    """eigen3x3_device (Stress.jl:95-157) transcribed statement by statement
+    on Float32 scalars: a cross-check of the vectorised restatement."""
+    f = np.float32
+    s11, s22, s33, s12, s23, s13 = (f(x) for x in (s11, s22, s33, s12, s23, s13))
+    v = [[f(1), f(0), f(0)], [f(0), f(1), f(0)], [f(0), f(0), f(1)]]
+
+    def rot(spp, sqq, spq, spr, sqr, p, q):
+        h = spq
+        g = f(100) * abs(h)
+        if abs(spp) + g != abs(spp) or abs(sqq) + g != abs(sqq):
+            theta = f(0.5) * (sqq - spp) / h
+            t = f(1) / (abs(theta) + np.sqrt(theta * theta + f(1)))
+            if theta < f(0):
+                t = -t
+            c = f(1) / np.sqrt(t * t + f(1))
+            s = t * c
+            tau = s / (f(1) + c)
+            spp, sqq = spp - t * spq, sqq + t * spq
+            spq = f(0)
+            tmp = spr
+            spr = spr - s * (sqr + tau * spr)
+            sqr = sqr + s * (tmp - tau * sqr)
+            for r in range(3):
+                vp = v[r][p]
+                v[r][p] = vp - s * (v[r][q] + tau * vp)
+                v[r][q] = v[r][q] + s * (vp - tau * v[r][q])
+        return spp, sqq, spq, spr, sqr
+
+    with np.errstate(over="ignore"):
+        for _ in range(12):
+            if max(abs(s12), abs(s23), abs(s13)) < f(1e-9):
+                break
+            s11, s22, s12, s13, s23 = rot(s11, s22, s12, s13, s23, 0, 1)
+            s11, s33, s13, s12, s23 = rot(s11, s33, s13, s12, s23, 0, 2)
+            s22, s33, s23, s12, s13 = rot(s22, s33, s23, s12, s13, 1, 2)
+    ev = [s11, s22, s33]
+    for a, b in ((0, 1), (1, 2), (0, 1)):
+        if ev[a] < ev[b]:
+            ev[a], ev[b] = ev[b], ev[a]
+            for r in range(3):
+                v[r][a], v[r][b] = v[r][b], v[r][a]
+    return np.array(ev, np.float32), np.array([v[r][0] for r in range(3)]), np.array([v[r][2] for r in range(3)])
+
+
+def test_vectorised_eigen_matches_the_loop_transcription(oracle):
+    rng = np.random.default_rng(21)
+    n = 300
+    t = (rng.standard_normal((6, n)) * np.float32(1e3)).astype(np.float32)
+    t[3:, :20] = 0.0  # already diagonal
+    t[:, 20:40] = t[:, 20:21]  # repeated tensors
+    t[4, 40:60] = np.float32(1e-12)  # nearly diagonal
+    vals, vmax, vmin = oracle.eigen3x3(*t)
+    for e in range(n):
+        ev, dmax, dmin = _eigen3x3_loops(*t[:, e])
+        assert np.array_equal(vals[e], ev), e
+        assert np.array_equal(vmax[e], dmax) and np.array_equal(vmin[e], dmin), e
