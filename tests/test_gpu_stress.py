@@ -61,3 +61,20 @@ def test_stress_of_a_solved_cantilever(ctx, oracle):
     S[:, 0, 2] = S[:, 2, 0] = v[:, 5]
     w = np.sort(np.linalg.eigvalsh(S), axis=1)[:, ::-1]
     assert np.abs(out["principal"] - w).max() <= 1e-4 * np.abs(w).max()
+
+
+def test_reference_signature_mirror(ctx, rng):
+    from v119_2025_12_19_hexatop_aws_gb300.mesh import generate_mesh
+    from v119_2025_12_19_hexatop_aws_gb300.topopt import compute_stress_field
+    dims = (6, 4, 3)
+    nodes, elements, _ = generate_mesh(*dims, 1.0, 1.0, 1.0)
+    ne, nn = 72, 7 * 5 * 4
+    U = (1e-2 * rng.standard_normal(3 * nn)).astype(np.float32)
+    dens = rng.uniform(0.0, 1.0, ne).astype(np.float32)
+    pr, vm, vo, l1, dmax, dmin = compute_stress_field(nodes, elements, U, np.float32(2.0), np.float32(0.3), dens, ctx=ctx)
+    ref = stress_field(_lib.make_grid(*dims), U.astype(np.float64), dens, E=2.0, nu=0.3, ctx=ctx)
+    assert pr.shape == (3, ne) and vo.shape == (6, ne) and dmax.shape == (3, ne)
+    assert np.array_equal(pr, ref["principal"].T) and np.array_equal(vm, ref["vonmises"])
+    assert np.array_equal(l1, ref["l1"]) and np.array_equal(dmin, ref["dir_min"].T)
+    _, _, none, _, _, _ = compute_stress_field(nodes, elements, U, 2.0, 0.3, dens, return_voigt=False, ctx=ctx)
+    assert none.shape == (0, 0)

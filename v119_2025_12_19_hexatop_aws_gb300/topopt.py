@@ -190,3 +190,19 @@ def update_density(density, l1_stress_norm_field, protected_elements_mask, E, l1
         return np.float32(0), np.float32(0), np.float32(0), 0.0, 0, 0.0
     return (np.float32(st["mean_change"]), np.float32(st["R_length"]), np.float32(st["current_threshold"]),
             st["filter_time"], st["filter_iters"], st["filter_res"])
+
+
+def compute_stress_field(nodes, elements, U, E, nu, density, *, return_voigt=True, ctx=None):
+    """Drop-in for Stress.compute_stress_field (Stress.jl:286-339) on a mesh
+    that equals Mesh.generate_mesh's: returns (principal, vonmises, voigt,
+    l1, dir_max, dir_min) as the reference does, the 3 x nElem and 6 x nElem
+    matrices as (3, nElem) / (6, nElem) views of the element-major arrays
+    (the memory layout of the reference's column-major matrices); voigt is an
+    empty (0, 0) array when return_voigt is false."""
+    from .mesh import structured_dims
+    nx, ny, nz, dx, dy, dz = structured_dims(nodes, elements)
+    grid = _lib.make_grid(nx, ny, nz, dx, dy, dz)
+    out = stress_field(grid, np.asarray(U, dtype=np.float64), density, E=float(E), nu=float(nu), voigt=return_voigt,
+                       ctx=ctx)
+    voigt = out["voigt"].T if return_voigt else np.zeros((0, 0), np.float32)
+    return out["principal"].T, out["vonmises"], voigt, out["l1"], out["dir_max"].T, out["dir_min"].T
