@@ -138,3 +138,48 @@ def test_vectorised_update_matches_the_loop_transcription(oracle, it, hard):
                                               p["max_density"], p, (0.1, 0.1, 0.1))
     assert np.array_equal(new, ref)
     assert st["active_count"] == active and st["culled"] == culled and st["mean_change"] == mean
+
+
+def _radix_select_keys(keys, k, digit_bits=11):
+    """The culling selection of csrc/update.cu in Python: six passes over
+    the 64-bit keys (float bits << 32 | index), 11-bit digits from the top;
+    each pass histograms the keys that share the prefix found so far and
+    picks the digit holding the k-th smallest.  Returns the k-th smallest key."""
+    prefix, remaining = 0, k
+    top = 64
+    while top > 0:
+        width = digit_bits if top >= digit_bits else top
+        shift = top - width
+        above = shift + width
+        hist = [0] * (1 << digit_bits)
+        for key in keys:
+            if above < 64 and (key >> above) != (prefix >> above):
+                continue
+            hist[(key >> shift) & ((1 << width) - 1)] += 1
+        excl = 0
+        for digit, cnt in enumerate(hist):
+            if excl < remaining <= excl + cnt:
+                prefix |= digit << shift
+                remaining -= excl
+                break
+            excl += cnt
+        top = shift
+    return prefix
+
+
+def test_radix_select_picks_the_stable_sort_prefix():
+    rng = np.random.default_rng(3)
+    for trial in range(40):
+        n = int(rng.integers(1, 300))
+        vals = rng.uniform(0.001, 0.9, n).astype(F32)
+        if trial % 3 == 0:
+            vals[rng.uniform(size=n) < 0.5] = F32(0.25)  # heavy ties
+        if trial % 7 == 0:
+            vals[:] = F32(0.5)  # all equal
+        idx = np.sort(rng.choice(100000, n, replace=False))
+        keys = [(int(np.float32(v).view(np.uint32)) << 32) | int(e) for v, e in zip(vals, idx)]
+        order = sorted(range(n), key=lambda i: vals[i])  # stable: ties by index
+        for k in {1, n, max(1, n // 3), max(1, n - 1)}:
+            kth = _radix_select_keys(keys, k)
+            chosen = {i for i in range(n) if keys[i] <= kth}
+            assert chosen == set(order[:k]), (trial, n, k)
