@@ -22,6 +22,11 @@ def test_header_declares_the_bound_symbols():
     assert declared_functions() == sorted(_lib.SIGNATURES)
 
 
+def test_integration_guide_covers_every_entry_point():
+    doc = (HEADER.parents[1] / "INTEGRATION.md").read_text()
+    assert [n for n in declared_functions() if f"`{n}`" not in doc] == []
+
+
 def test_library_exports_every_declared_symbol(built_lib):
     lib = C.CDLL(str(built_lib))
     missing = [n for n in declared_functions() if not hasattr(lib, n)]
