@@ -740,7 +740,9 @@ int hexa_update_density(hexa_ctx* h, const hexa_grid* g, float* density, const f
     return set_err(h, HEXA_ERR_ARG, "invalid grid or null array");
   if (p->number_of_iterations < 1 || !(p->E > 0.0f) || !(p->l1_stress_allowable > 0.0f) || !std::isfinite(p->E) ||
       !std::isfinite(p->l1_stress_allowable) || !(p->filter_tolerance > 0.0f) || p->filter_max_iter < 1 ||
-      !(p->min_density <= p->max_density))
+      !(p->min_density <= p->max_density) || !std::isfinite(p->min_density) || !std::isfinite(p->max_density) ||
+      !(p->max_culling_ratio >= 0.0f) || !std::isfinite(p->max_culling_ratio) ||
+      !std::isfinite(p->final_density_threshold))
     return set_err(h, HEXA_ERR_ARG, "invalid density update parameters");
   Ctx& c = h->c;
   c.err.clear();
