@@ -183,3 +183,35 @@ def test_radix_select_picks_the_stable_sort_prefix():
             kth = _radix_select_keys(keys, k)
             chosen = {i for i in range(n) if keys[i] <= kth}
             assert chosen == set(order[:k]), (trial, n, k)
+
+
+def test_dropin_reads_the_reference_config_keys(monkeypatch, built_lib):
+    """topopt.update_density maps update_density!'s arguments and config keys
+    (TopOpt.jl:238-300, 420-462) onto hexa_density_update_params; the GPU
+    call is replaced by a recorder, so this runs anywhere."""
+    from v119_2025_12_19_hexatop_aws_gb300 import topopt
+    seen = {}
+
+    def record(grid, density, l1, protected, original, params, ctx=None):
+        seen.update(grid=(grid.nx, grid.ny, grid.nz, grid.dx), params=params)
+        return dict(status=0, mean_change=0.5, R_length=0.25, current_threshold=0.125, filter_time=0.0,
+                    filter_iters=3, filter_res=1e-6)
+
+    monkeypatch.setattr(topopt, "update_density_gpu", record)
+    config = {"optimization_parameters": {"filter_R_init_perc": 6.0, "filter_R_final_perc": 1.5,
+                                          "max_culling_ratio": 0.05, "density_update_method": "hard",
+                                          "final_density_threshold": 0.9},
+              "solver_parameters": {"filter_tolerance": 1e-4},
+              "geometry": {"nElem_x_computed": 8, "nElem_y_computed": 4, "nElem_z_computed": 2,
+                           "dx_computed": 0.5, "dy_computed": 0.5, "dz_computed": 0.5, "max_domain_dim": 4.0}}
+    out = topopt.update_density(np.zeros(64, F32), np.zeros(64, F32), None, F32(7.0), F32(2.0), 12, 40,
+                                np.ones(64, F32), F32(0.01), F32(0.9), config)
+    p = seen["params"]
+    assert seen["grid"] == (8, 4, 2, 0.5)
+    assert (p.E, p.l1_stress_allowable, p.iter, p.number_of_iterations) == (7.0, 2.0, 12, 40)
+    assert p.min_density == F32(0.01) and p.max_density == F32(0.9) and p.max_domain_dim == 4.0
+    assert p.filter_R_init_perc == 6.0 and p.filter_R_interm_perc == 0.0 and p.filter_R_final_perc == 1.5
+    assert p.filter_R_interm_iter_perc == 50.0 and p.minimum_filter_radius_as_elements == 2.5
+    assert p.filter_tolerance == F32(1e-4) and p.final_density_threshold == F32(0.9)
+    assert p.max_culling_ratio == F32(0.05) and p.hard_update == 1
+    assert out == (F32(0.5), F32(0.25), F32(0.125), 0.0, 3, 1e-6)
