@@ -115,3 +115,34 @@ def test_vectorised_remap_matches_the_loop_transcription(oracle, projection):
     nd, na, _ = oracle.remap_fields(old, new, h, L, dens, alpha, projection)
     rd, ra = _remap_loops(old, new, h, L, dens, alpha, projection)
     assert np.array_equal(nd, rd) and np.array_equal(na, ra)
+
+
+def test_refine_entry_keeps_the_mesh_when_no_growth_is_due(monkeypatch):
+    """refine_mesh_and_fields returns its inputs untouched when the reference
+    would skip (target reached, growth under 5 %, memory limit after the
+    distribution) and calls the transfer otherwise; the GPU call is recorded."""
+    from v119_2025_12_19_hexatop_aws_gb300 import _lib, refine
+    calls = []
+
+    def fake_remap(old, new, lengths, density, alpha=None, *, projection=True, ctx=None):
+        calls.append((new.nx, new.ny, new.nz, projection))
+        n = new.nx * new.ny * new.nz
+        return np.zeros(n, np.float32), None if alpha is None else np.zeros(n, np.float32)
+
+    monkeypatch.setattr(refine, "remap_fields", fake_remap)
+    g = _lib.make_grid(10, 5, 5, 1.0, 1.0, 1.0)
+    dens = np.full(250, 0.5, np.float32)
+    L = refine.domain_lengths(g)
+    out = refine.refine_mesh_and_fields(g, dens, None, 100, L)  # 250 active >= 100
+    assert out[0] is g and out[1] is dens and not out[3].refine and not calls
+    out = refine.refine_mesh_and_fields(g, dens, None, 1000, L, max_growth_rate=1.02)  # growth under 5 %
+    assert out[0] is g and not calls
+    out = refine.refine_mesh_and_fields(g, dens, None, 1000, L, max_growth_rate=2.0, memory_limit=260)
+    assert out[0] is g and not calls  # the memory limit leaves growth under 5 %
+    # 333 elements allowed, but the distribution rounds up to 11 x 6 x 6 = 396 (MeshRefiner.jl:151-155)
+    assert refine.element_distribution(*L, 333)[6] == 396
+    out = refine.refine_mesh_and_fields(g, dens, None, 1000, L, max_growth_rate=2.0, memory_limit=333)
+    assert out[0] is g and not out[3].refine and not calls
+    g2, d2, a2, plan = refine.refine_mesh_and_fields(g, dens, None, 1000, L, max_growth_rate=2.0,
+                                                     update_method="soft")
+    assert plan.refine and calls == [(g2.nx, g2.ny, g2.nz, False)] and d2.size == g2.nx * g2.ny * g2.nz

@@ -107,7 +107,8 @@ def refine_mesh_and_fields(grid, density, alpha, target_active, lengths, *, max_
     if not plan.refine:
         return grid, density, alpha, plan
     nx, ny, nz, dx, dy, dz, count = element_distribution(*lengths, plan.new_total)
-    if memory_limit is not None and count > memory_limit:  # the post-distribution check of MeshRefiner.jl:151-155
+    ram = memory_limit if memory_limit is not None else hard_element_limit
+    if count > ram:  # the post-distribution check of MeshRefiner.jl:151-155
         return grid, density, alpha, RefinePlan(False, n_old, "memory limit after distribution")
     new_grid = _lib.make_grid(nx, ny, nz, dx, dy, dz)
     nd, na = remap_fields(grid, new_grid, lengths, dens, alpha, projection=(update_method == "hard"), ctx=ctx)
