@@ -415,7 +415,7 @@ def run_ours(a):
     pipe["solve_filter_sensitivities_s"] = round(ms / 1e3 + pipe["filter_s"] + pipe["sensitivities_s"], 6)
 
     try:
-        rows = next_rows(ctx, grid, u_d, rho, dev)
+        rows = next_rows(ctx, grid, u_d, rho, dev, peak)
     except Exception as e:  # the rows either side of the solve never void the headline line
         rows = {"error": str(e)[:200]}
 
@@ -451,7 +451,7 @@ def run_ours(a):
     dist.close()
 
 
-def next_rows(ctx, grid, u_d, rho, dev, reps=3):
+def next_rows(ctx, grid, u_d, rho, dev, peak=None, reps=3):
     """The kernels either side of the solve on the solved workload, device
     arrays, each timed over `reps` calls after one warm call (the calls end
     with a stream synchronize, so the events bracket complete work):
@@ -524,6 +524,10 @@ def next_rows(ctx, grid, u_d, rho, dev, reps=3):
     t = timed(remap)
     rows["remap"] = {"ms": round(t, 4), "new_grid": [nx, ny, nz], "bytes": 12 * cnt,
                      "gbs": round(12 * cnt / (t * 1e-3) / 1e9, 1)}
+    if peak:
+        for r in rows.values():
+            if "gbs" in r:
+                r["frac_of_measured_hbm"] = round(r["gbs"] / peak, 4)
     return rows
 
 
