@@ -125,6 +125,10 @@ typedef struct hexa_filter_stats {
 } hexa_filter_stats;
 
 /* ---- context ----------------------------------------------------------- */
+/* A context replaces the reference's module-global workspaces
+ * (GPUSolver.jl:63, GPUGeometricMultigrid.jl:37) and its CUDA.functional()
+ * check (GPUSolver.jl:470-472: HEXA_ERR_NO_DEVICE); hexa_default_params gives
+ * the configs/default.yaml solver_parameters defaults. */
 int hexa_create(int32_t device, hexa_ctx** out);
 void hexa_destroy(hexa_ctx* ctx);
 const char* hexa_last_error(const hexa_ctx* ctx);
@@ -153,9 +157,11 @@ int hexa_scalar_canonical_matrices(double dx, double dy, double dz, int32_t quir
  * Entries of x at fixed DOFs are ignored (expand_kernel! semantics). */
 int hexa_apply_operator(hexa_ctx* ctx, const hexa_grid* g, const hexa_bc* bc, double nu,
                         const double* factor, const double* x, double sigma, double* y);
+/* The same operator in FP32 (the reference runs T = Float32 on its RTX profile, GPUSolver.jl:188-189). */
 int hexa_apply_operator_f32(hexa_ctx* ctx, const hexa_grid* g, const hexa_bc* bc, double nu,
                             const float* factor, const float* x, float sigma, float* y);
-/* Times `reps` back-to-back launches of the operator kernel alone on the
+/* No counterpart in the reference (a benchmark hook).
+ * Times `reps` back-to-back launches of the operator kernel alone on the
  * context's stream with CUDA events (inputs already on the device) and
  * returns the mean launch duration in ms.  precision: HEXA_PREC_FP64 or
  * HEXA_PREC_FP32 (factor/x/y then float).  mode: 0 y = Ax, 1 y = Ax with
@@ -189,14 +195,15 @@ int hexa_solve_system_gpu(hexa_ctx* ctx, const hexa_grid* g, float E, const floa
                           const float* u_guess, double* u_out, double* relres_out,
                           char* method_out, int32_t method_cap, hexa_solve_stats* stats);
 
-/* k load cases as one block PCG (each K0/factor load serves k right-hand
- * sides).  F and U are k consecutive 3*nNodes vectors. */
+/* No counterpart in the reference (it solves one load case per call,
+ * GPUSolver.jl:467-477): k load cases as one block PCG (each K0/factor load
+ * serves k right-hand sides).  F and U are k consecutive 3*nNodes vectors. */
 int hexa_solve_multi_rhs(hexa_ctx* ctx, const hexa_grid* g, const hexa_bc* bc, const double* factor,
                          int32_t k, const double* F, const hexa_solve_params* p, double* U,
                          hexa_solve_stats* stats);
 
-/* `count` independent problems on grids of uneven sizes solved together (no
- * counterpart in the reference): one launch per kernel over all instances,
+/* No counterpart in the reference: `count` independent problems on grids of
+ * uneven sizes solved together: one launch per kernel over all instances,
  * per-instance reductions and convergence, the PCG iteration and V-cycle
  * replayed from one CUDA graph.  grids[i], bcs[i] (clamp faces only:
  * fixed_dof must be NULL; bcs may be NULL for no clamps), factors[i] (nElem_i),
@@ -334,6 +341,10 @@ int hexa_update_density(hexa_ctx* ctx, const hexa_grid* g, float* density, const
                         const hexa_density_update_params* p, hexa_density_update_stats* stats);
 
 /* ---- (e) SIMP sensitivities and OC update ------------------------------ */
+/* No counterpart in the reference (its update is the stress-ratio rule of
+ * TopOpt.jl:211-482, hexa_update_density): the published SIMP/OC method
+ * (modified SIMP modulus, OC with move limit and a bisection on the
+ * Lagrange multiplier), reaching the same solve with SIMP factors. */
 /* dc_e = -penal * rho_e^(penal-1) * (E0 - Emin) * u_e^T K0 u_e and
  * compliance = sum_e (Emin + rho_e^penal (E0-Emin)) u_e^T K0 u_e. */
 int hexa_sensitivities(hexa_ctx* ctx, const hexa_grid* g, double nu, const double* rho,
