@@ -22,6 +22,21 @@ def test_header_declares_the_bound_symbols():
     assert declared_functions() == sorted(_lib.SIGNATURES)
 
 
+def test_header_cites_the_reference_for_every_entry_point():
+    """Each declaration's comment block (or its section's) names the
+    reference file it replaces, or says that the reference has no counterpart."""
+    text = HEADER.read_text()
+    missing = []
+    last_comment = ""
+    for m in re.finditer(r"(/\*.*?\*/)|\b(?:int|void|double|int64_t|const char\*)\s+(hexa_[a-z0-9_]+)\s*\(", text, re.S):
+        if m.group(1):
+            last_comment = m.group(1) if ".jl" in m.group(1) or "counterpart" in m.group(1) else last_comment
+            continue
+        if ".jl" not in last_comment and "counterpart" not in last_comment:
+            missing.append(m.group(2))
+    assert missing == []
+
+
 def test_integration_guide_covers_every_entry_point():
     doc = (HEADER.parents[1] / "INTEGRATION.md").read_text()
     assert [n for n in declared_functions() if f"`{n}`" not in doc] == []
