@@ -6,8 +6,9 @@ import struct
 import numpy as np
 
 from v119_2025_12_19_hexatop_aws_gb300 import _lib
-from v119_2025_12_19_hexatop_aws_gb300.exporters import (export_indices, read_hexa_binary, read_vti_arrays,
-                                                         signed_l1, write_hexa_binary, write_vti)
+from v119_2025_12_19_hexatop_aws_gb300.exporters import (checkpoint_density, export_indices, load_checkpoint,
+                                                         read_hexa_binary, read_vti_arrays, signed_l1,
+                                                         write_hexa_binary, write_vti)
 
 
 def test_export_indices_threshold_and_fractional_stride():
@@ -80,3 +81,33 @@ def test_vti_header_and_arrays(tmp_path):
         else:
             assert "PrincipalValues" not in arrs
         assert open(path, "rb").read().endswith(b"\n  </AppendedData>\n</VTKFile>\n")
+
+
+def test_checkpoint_reload_and_full_field(tmp_path):
+    """load_checkpoint returns what Configuration.load_checkpoint returns; the
+    full field is rebuilt from the stored centroids even from a thresholded,
+    thinned file (the reference's restart needs count == nElem)."""
+    dims, h = (10, 6, 4), (0.5, 1.0, 2.0)
+    grid = _lib.make_grid(*dims, *h)
+    ne = 240
+    rng = np.random.default_rng(8)
+    dens = rng.uniform(0, 1, ne).astype(np.float32)
+    princ = rng.standard_normal((ne, 3)).astype(np.float32)
+    l1 = np.abs(princ).sum(axis=1).astype(np.float32)
+    cfg = {"number_of_iterations": 30, "optimization_parameters": {"min_density": 0.001}}
+    path = tmp_path / "ck.bin"
+    n = write_hexa_binary(path, grid, dens, l1, princ, iteration=12, radius=0.75, threshold=0.3, config=cfg,
+                          max_export_cells=50)
+    config, d, it, r, thr = load_checkpoint(path)
+    assert n == 50 and d.size == 50 and it == 12 and r == np.float32(0.75) and thr == np.float32(0.3)
+    assert config["number_of_iterations"] == 30 and config["iteration"] == 12
+    idx = export_indices(dens, 0.3, 50)
+    assert np.array_equal(d, dens[idx])
+    full = checkpoint_density(path, *dims, *h, fill=0.001)
+    expect = np.full(ne, np.float32(0.001))
+    expect[idx] = dens[idx]
+    assert np.array_equal(full, expect)
+    # every cell stored: the original field comes back exactly
+    write_hexa_binary(path, grid, dens, l1, princ, iteration=1, radius=0.5, threshold=0.0, config=cfg)
+    assert np.array_equal(checkpoint_density(path, *dims, *h), dens)
+

@@ -11,6 +11,9 @@ Restated from the reference's writers (host code, no GPU):
   reference's fractional stride; a cell's centroid is the Float32 mean of its
   8 node coordinates (MeshUtilities.jl:16-31) and its signed L1 carries the
   sign of the principal stress of largest magnitude (first wins ties).
+* ``load_checkpoint`` (src/IO/Configuration.jl:32-78) reads the same file
+  back; ``checkpoint_density`` rebuilds the full element field from the
+  stored centroids (the reference's restart needs an unthinned file).
 * ``export_solution_vti`` (src/IO/ExportVTK.jl:16-110): ImageData with
   appended raw Float32 cell arrays Density, L1_Stress, VonMises and, when the
   config asks for principal vectors, PrincipalValues, MaxPrincipalDirection,
@@ -142,6 +145,34 @@ def read_hexa_binary(path) -> dict:
         raise ValueError("trailing bytes after the JSON metadata")
     return dict(iteration=iteration, radius=radius, threshold=threshold, count=count, spacing=(dx, dy, dz),
                 centroids=cent, density=dens, signed_l1=sl1, meta=meta)
+
+
+def load_checkpoint(path):
+    """Configuration.load_checkpoint (src/IO/Configuration.jl:32-78): returns
+    (config, density, iteration, radius, threshold), density being the
+    `count` stored values in file order."""
+    d = read_hexa_binary(path)
+    return d["meta"], np.array(d["density"], dtype=np.float32), int(d["iteration"]), np.float32(d["radius"]), \
+        np.float32(d["threshold"])
+
+
+def checkpoint_density(path, nx, ny, nz, dx, dy, dz, fill=1.0e-3) -> np.ndarray:
+    """The full element field behind a checkpoint: each stored cell goes back
+    to the element its centroid lies in (floor(c / d) per axis), every other
+    element gets `fill`.  The reference's restart needs the stored count to
+    equal the element count (Main.jl:269-271), which a file thresholded and
+    thinned by export_binary_for_web (Postprocessing.jl:383-402) does not
+    meet; this gives a full field either way."""
+    d = read_hexa_binary(path)
+    cent = np.asarray(d["centroids"], dtype=np.float64)
+    h = np.array([dx, dy, dz], dtype=np.float64)
+    ijk = np.floor(cent / h).astype(np.int64)
+    n = np.array([nx, ny, nz])
+    if ijk.size and (ijk.min() < 0 or np.any(ijk.max(axis=0) >= n)):
+        raise ValueError("checkpoint cells lie outside the given grid")
+    out = np.full(nx * ny * nz, np.float32(fill), dtype=np.float32)
+    out[ijk[:, 0] + nx * (ijk[:, 1] + ny * ijk[:, 2])] = d["density"]
+    return out
 
 
 def _jl(v) -> str:
