@@ -425,7 +425,8 @@ def run_ours(a):
         "warmup": a.warmup, "ms_per_step": round(ms, 3), "higher_is_better": False, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic (seeded cantilever, Helmholtz-smoothed density)",
         "config": {"workload": f"{a.config} cantilever {nx}x{ny}x{nz} hex8, {ndof} DOF, SIMP p=3 Emin=1e-9, "
-                               f"mixed: FP32 GMG-PCG (autotuned: {s_last['mg_levels']} levels, Chebyshev) with "
+                               f"mixed: FP32 GMG-PCG (autotuned: {s_last['mg_levels']} levels, Chebyshev V({s_last['smooth_steps']},"
+                               f"{s_last['smooth_steps']}) on [lmax/{pm.cheb_ratio}, lmax]) with "
                                f"FP64 reliable updates to true residual 1e-9; plain: FP64 GMG-PCG "
                                f"({solver_params(a.config, 'fp64').mg_levels} levels, V(2,2))",
                    "parallelism": f"replicas{dist.ws}", "l2": "inputs larger than L2 (no flush)"},
