@@ -22,7 +22,8 @@ def build(force: bool = False) -> Path:
     OUT.parent.mkdir(exist_ok=True)
     cc = os.environ.get("CC", "gcc")
     tmp = OUT.with_suffix(".so.tmp")
-    cmd = [cc, "-O2", "-fopenmp", "-fPIC", "-shared", "-std=c11", str(SRC), "-o", str(tmp), "-lm"]
+    # no FMA contraction: Julia rounds each product and sum, and x86-64 and aarch64 then agree
+    cmd = [cc, "-O2", "-ffp-contract=off", "-fopenmp", "-fPIC", "-shared", "-std=c11", str(SRC), "-o", str(tmp), "-lm"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"oracle build failed:\n{' '.join(cmd)}\n{r.stderr}")
