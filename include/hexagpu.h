@@ -115,6 +115,9 @@ typedef struct hexa_solve_stats {
   double total_ms;          /* host wall time of the call */
   double fine_applies;      /* fine-grid operator applications (FP64 + FP32) */
   double fine_applies_fp64;
+  double unshifted_relres;  /* ||f - K u|| / ||f|| recomputed in FP64 without the shift (the residual of
+                               the unshifted system; equals true_relres when sigma = 0; multi-RHS: the
+                               largest over the columns; batches: NaN when sigma > 0) */
 } hexa_solve_stats;
 
 typedef struct hexa_filter_stats {
@@ -228,16 +231,23 @@ int hexa_filter(hexa_ctx* ctx, const hexa_grid* g, const double* rho_in, double 
 
 /* The filter of hexa_filter without any device allocation (this entry point
  * has no counterpart in the reference).  For callers that cannot allocate
- * device memory where they filter -- code running while its application
- * captures a CUDA stream, or hosts whose own pool owns the device-memory
- * budget.  All scratch lives in one fixed device array inside the library
- * (about 15 MB, held by every GPU that loads the library until exit), so the
- * grid may have at most HEXA_NOALLOC_MAX_NODES nodes; larger grids return
- * HEXA_ERR_TOO_LARGE.  rho_in and rho_out must be device pointers (host
- * arrays would need a staging allocation: HEXA_ERR_ARG); FP64 arithmetic,
- * same algorithm and results as hexa_filter with HEXA_PREC_FP64.  stream may
- * be NULL (default stream); the call returns when its work is done.  Every
- * call reuses the array: calls that overlap on the GPU race and must be
+ * device memory where they filter -- code running on its own stream while
+ * another stream of its application is being captured into a CUDA graph, or
+ * hosts whose own pool owns the device-memory budget.  All scratch lives in
+ * one fixed device array inside the library (about 15 MB, held by every GPU
+ * that loads the library until exit), so the grid may have at most
+ * HEXA_NOALLOC_MAX_NODES nodes; larger grids return HEXA_ERR_TOO_LARGE.
+ * rho_in and rho_out must be device pointers on the current device (host
+ * arrays would need a staging allocation, and another GPU's arrays are not
+ * this device's: HEXA_ERR_ARG); FP64 arithmetic, same algorithm and results
+ * as hexa_filter with HEXA_PREC_FP64 (a NaN residual or a p.Ap breakdown
+ * gives a NaN field).  The call synchronizes its stream and cannot itself be
+ * captured: a stream that is capturing is refused (HEXA_ERR_ARG).  While the
+ * application captures another stream, pass a non-blocking stream
+ * (cudaStreamNonBlocking); NULL is the legacy default stream, whose work
+ * joins a capture on any blocking stream.  The call returns when its work is
+ * done, with the calling thread's capture mode as it found it.  Every call
+ * reuses the array: calls that overlap on the GPU race and must be
  * serialised by the caller.  The first call on a device resolves the array's
  * device address; make it before any stream capture begins. */
 #define HEXA_NOALLOC_MAX_NODES 262144

@@ -268,6 +268,97 @@ void ho_helm_extract(int nx, int ny, int nz, const double* psi, double* out) {
   }
 }
 
+/* GPUHelmholtz.jl:190-266 (solve_helmholtz_on_gpu) on the host in FP64:
+ * Jacobi-PCG of (R^2 Ke + Me) psi = sum_e rho_e vol/8, the recursive
+ * ||r||/||b|| tested every 10 iterations, at most max_iter iterations, then
+ * the element mean of psi (GPUHelmholtz.jl:99-110).  Ae is the 8x8 element
+ * matrix, column-major in n1..n8 order.  A zero right-hand side returns rho
+ * unchanged (GPUHelmholtz.jl:203-206).  Returns the iteration count; *relres
+ * gets the last tested residual.  Vector passes are OpenMP loops with
+ * reductions (the sum order depends on the thread count, as the reference's
+ * CUBLAS sums depend on its launch shape). */
+int ho_helm_pcg(int nx, int ny, int nz, const double* Ae, const double* rho, double scale, double tol, int max_iter,
+                double* out, double* relres) {
+  const long long nn = (long long)(nx + 1) * (ny + 1) * (nz + 1), ne = (long long)nx * ny * nz;
+  double* b = (double*)malloc(sizeof(double) * nn);
+  double* x = (double*)calloc((size_t)nn, sizeof(double));
+  double* r = (double*)malloc(sizeof(double) * nn);
+  double* z = (double*)malloc(sizeof(double) * nn);
+  double* q = (double*)malloc(sizeof(double) * nn);
+  double* pv = (double*)malloc(sizeof(double) * nn);
+  double* dinv = (double*)calloc((size_t)nn, sizeof(double));
+  int it = 0;
+  *relres = 0.0;
+  if (!b || !x || !r || !z || !q || !pv || !dinv) {
+    it = -1;
+    goto done;
+  }
+  ho_helm_rhs(nx, ny, nz, rho, scale, b);
+  for (long long e = 0; e < ne; ++e) { /* assembled diagonal: sum of Ae[a][a] over the node's elements */
+    long long n[8];
+    elem_nodes(nx, ny, e, n);
+    for (int a = 0; a < 8; ++a) dinv[n[a]] += Ae[a + 8 * a];
+  }
+  double bb = 0.0;
+#pragma omp parallel for reduction(+ : bb) schedule(static)
+  for (long long i = 0; i < nn; ++i) {
+    dinv[i] = 1.0 / dinv[i];
+    bb += b[i] * b[i];
+  }
+  const double nb = sqrt(bb);
+  if (nb == 0.0) {
+    memcpy(out, rho, sizeof(double) * ne);
+    goto done;
+  }
+  double rz = 0.0;
+#pragma omp parallel for reduction(+ : rz) schedule(static)
+  for (long long i = 0; i < nn; ++i) {
+    r[i] = b[i];
+    z[i] = r[i] * dinv[i];
+    pv[i] = z[i];
+    rz += r[i] * z[i];
+  }
+  for (it = 1; it <= max_iter; ++it) {
+    ho_helm_apply(nx, ny, nz, Ae, pv, q);
+    double pq = 0.0;
+#pragma omp parallel for reduction(+ : pq) schedule(static)
+    for (long long i = 0; i < nn; ++i) pq += pv[i] * q[i];
+    const double alpha = rz / pq;
+    double rr = 0.0;
+#pragma omp parallel for reduction(+ : rr) schedule(static)
+    for (long long i = 0; i < nn; ++i) {
+      x[i] += alpha * pv[i];
+      r[i] -= alpha * q[i];
+      rr += r[i] * r[i];
+    }
+    if (it % 10 == 0) {
+      *relres = sqrt(rr) / nb;
+      if (*relres < tol) break;
+    }
+    double rzn = 0.0;
+#pragma omp parallel for reduction(+ : rzn) schedule(static)
+    for (long long i = 0; i < nn; ++i) {
+      z[i] = r[i] * dinv[i];
+      rzn += r[i] * z[i];
+    }
+    const double beta = rzn / rz;
+#pragma omp parallel for schedule(static)
+    for (long long i = 0; i < nn; ++i) pv[i] = z[i] + beta * pv[i];
+    rz = rzn;
+  }
+  if (it > max_iter) it = max_iter;
+  ho_helm_extract(nx, ny, nz, x, out);
+done:
+  free(b);
+  free(x);
+  free(r);
+  free(z);
+  free(q);
+  free(pv);
+  free(dinv);
+  return it;
+}
+
 /* ---------------------------------------------------------------------------
  * CPUSolver.jl:56-255 -- the reference's CPU matrix_free path, in Float32 as
  * the reference runs it (T = Float32 from nodes/E, src/Main.jl:289-294):

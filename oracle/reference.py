@@ -37,6 +37,8 @@ def lib():
         L.ho_helm_apply.argtypes = [I, I, I, P, P, P]
         L.ho_helm_rhs.argtypes = [I, I, I, P, D, P]
         L.ho_helm_extract.argtypes = [I, I, I, P, P]
+        L.ho_helm_pcg.argtypes = [I, I, I, P, P, D, D, I, P, C.POINTER(D)]
+        L.ho_helm_pcg.restype = I
         L.ho_cpu_matrix_free_cg.argtypes = [I, I, I, P, C.c_float, P, P, P, C.c_float, I, C.c_float, C.c_float, I, D,
                                             P, C.POINTER(D), C.POINTER(D), C.POINTER(I)]
         L.ho_cpu_matrix_free_cg.restype = I
@@ -433,6 +435,19 @@ def helmholtz_reference(g: Grid, rho, R, tol, max_iter=200, quirk=True):
         p = z + (rho_new / rho_old) * p
         rho_old = rho_new
     return helm_extract(g, x), final_iter, final_rel
+
+
+def helmholtz_pcg_c(g: Grid, rho, R, tol, max_iter=200, quirk=True):
+    """helmholtz_reference in C with OpenMP (oracle/hexa_oracle.c ho_helm_pcg):
+    the same Jacobi-PCG loop, for grids where the numpy loop is too slow."""
+    A = np.asfortranarray(helm_matrix(g, R, quirk)).ravel(order="F").copy()
+    out = np.empty(g.nelem)
+    rel = C.c_double()
+    it = lib().ho_helm_pcg(g.nx, g.ny, g.nz, _p(A), _p(np.ascontiguousarray(rho, dtype=np.float64)),
+                           g.dx * g.dy * g.dz / 8.0, float(tol), int(max_iter), _p(out), C.byref(rel))
+    if it < 0:
+        raise MemoryError("ho_helm_pcg: allocation failed")
+    return out, it, rel.value
 
 
 _HELM_LU = {}

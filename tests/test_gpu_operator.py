@@ -95,3 +95,37 @@ def test_diagonal_matches_oracle(ctx, oracle, rng, quirk):
     d_ref[oracle.fixed_mask(g, 1)] = 0
     d = operator_diagonal(_lib.make_grid(*dims, *h), fac, clamp_faces=1, diag_quirk=quirk, ctx=ctx)
     assert np.abs(d - d_ref).max() <= 1e-14 * d_ref.max()
+
+
+@pytest.mark.parametrize("dims", [(5, 3, 7), (33, 17, 9)])
+def test_timed_chebyshev_step_reads_its_previous_iterate(ctx, oracle, rng, dims):
+    """hexa_time_operator's mode 5 is the smoother's Chebyshev step written in
+    place over its previous iterate y (one warm-up launch, then `reps`), so the
+    benchmark's roofline times the kernel the V-cycle runs, x_prev stream
+    included: y <- x + 0.5 (x - y) + 0.3 D^-1 (b - A x), D the x-diagonal form."""
+    import ctypes as C
+    torch = pytest.importorskip("torch")
+    g, fac, x, fd, fixed = _case(oracle, rng, dims)
+    x[fixed] = 0.0
+    b = rng.standard_normal(g.ndof)
+    b[fixed] = 0.0
+    y0 = rng.standard_normal(g.ndof)
+    f32 = lambda a: a.astype(np.float32)
+    fac, x, b, y0 = f32(fac), f32(x), f32(b), f32(y0)
+    K0 = oracle.canonical_stiffness(1, 1, 1, 0.3)
+    ax = oracle.apply_A(g, K0, fac.astype(np.float64), x.astype(np.float64), fixed)
+    d = oracle.diag_K(g, K0, fac.astype(np.float64), quirk=True)
+    dinv = np.where(fixed, 0.0, 1.0 / np.where(fixed, 1.0, d))
+    reps = 2
+    want = y0.astype(np.float64)
+    for _ in range(reps + 1):
+        want = np.where(fixed, 0.0, x + 0.5 * (x - want) + 0.3 * dinv * (b - ax))
+    dev = lambda a: torch.from_numpy(a).cuda()
+    fac_d, x_d, b_d, y_d = dev(fac), dev(x), dev(b), dev(y0.copy())
+    t = C.c_double()
+    bc = _lib.make_bc(1)
+    rc = ctx.lib.hexa_time_operator(ctx.h, C.byref(_lib.make_grid(*dims)), C.byref(bc), 0.3, 2, 5, fac_d.data_ptr(),
+                                    x_d.data_ptr(), b_d.data_ptr(), y_d.data_ptr(), reps, C.byref(t))
+    assert rc == _lib.HEXA_OK and t.value > 0
+    got = y_d.cpu().numpy().astype(np.float64)
+    assert np.abs(got - want).max() <= 2e-5 * np.abs(want).max()

@@ -31,19 +31,58 @@ def rel(a, b):
 
 @pytest.mark.parametrize("precond", ["jacobi", "multigrid"])
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
-def test_solution_matches_direct(ctx, oracle, rng, precond, precision):
+@pytest.mark.parametrize("shift_factor", [0.0, 1e-10])
+def test_solution_matches_direct(ctx, oracle, rng, precond, precision, shift_factor):
+    """Both systems against LU: the unshifted K_ff u = f (shift_factor 0) and
+    the reference's shifted (K_ff + sigma I) u = f, sigma = 1e-10 max diag
+    (GPUSolver.jl:343).  unshifted_relres is ||f - K u|| / ||f|| in FP64."""
     dims = (16, 8, 8)
     g, fac, f, fixed = cantilever(oracle, rng, dims)
     K0 = oracle.canonical_stiffness(1, 1, 1, 0.3)
-    sigma = shift_of(oracle, g, fac, fixed)
+    sigma = shift_of(oracle, g, fac, fixed, factor=shift_factor)
     u_ref = oracle.direct_solve(g, K0, fac, f, fixed, sigma)
-    p = _lib.default_params(precond=precond, precision=precision, tol=1e-13, max_iter=20000, mg_levels=3)
+    p = _lib.default_params(precond=precond, precision=precision, tol=1e-13, max_iter=20000, mg_levels=3,
+                            shift_factor=shift_factor)
     u, st = solve(_lib.make_grid(*dims), fac, f, clamp_faces=1, params=p, ctx=ctx)
     assert st["status"] == 0
+    assert st["shift"] == pytest.approx(sigma, rel=1e-12, abs=0.0)
     assert st["true_relres"] <= 1e-13
+    r_unshifted = np.linalg.norm(f * ~fixed - oracle.apply_A(g, K0, fac, u, fixed)) / np.linalg.norm(f)
+    assert st["unshifted_relres"] == pytest.approx(r_unshifted, rel=1e-6, abs=1e-15)
+    if shift_factor == 0.0:
+        assert st["unshifted_relres"] == st["true_relres"]
     assert rel(u, u_ref) <= 1e-10
     assert abs(f @ u - f @ u_ref) <= 1e-10 * abs(f @ u_ref)
     assert st["compliance"] == pytest.approx(f @ u_ref, rel=1e-10)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_unshifted_void_contrast_reaches_fp64_residual(ctx, oracle, rng, precision):
+    """SIMP factors down to 1e-9 (void contrast): with shift_factor 0 the solve
+    reaches ||f - K u|| / ||f|| <= 1e-9 and matches LU of the unshifted system;
+    with the reference's shift the same solve leaves the unshifted residual at
+    about sigma ||u|| / ||f||."""
+    dims = (24, 12, 12)
+    g = oracle.Grid(*dims)
+    rho = np.clip(0.3 + 0.35 * rng.standard_normal(g.nelem), 1e-3, 1.0)
+    fac = 1e-9 + rho ** 3 * (1 - 1e-9)
+    f = workloads.edge_load(*dims)
+    fixed = oracle.fixed_mask(g, 1)
+    K0 = oracle.canonical_stiffness(1, 1, 1, 0.3)
+    u_ref = oracle.direct_solve(g, K0, fac, f, fixed, 0.0)
+    grid = _lib.make_grid(*dims)
+    p = _lib.default_params(precision=precision, tol=1e-9, max_iter=60000, divergence_check=0, shift_factor=0.0)
+    u, st = solve(grid, fac, f, clamp_faces=1, params=p, ctx=ctx)
+    assert st["status"] == 0 and st["shift"] == 0.0
+    assert st["unshifted_relres"] <= 1e-9
+    r = np.linalg.norm(f * ~fixed - oracle.apply_A(g, K0, fac, u, fixed)) / np.linalg.norm(f)
+    assert r <= 1.05e-9
+    assert abs(f @ u - f @ u_ref) <= 1e-10 * abs(f @ u_ref)
+    ps = _lib.default_params(precision=precision, tol=1e-9, max_iter=60000, divergence_check=0, shift_factor=1e-10)
+    us, sts = solve(grid, fac, f, clamp_faces=1, params=ps, ctx=ctx)
+    assert sts["true_relres"] <= 1e-9
+    expect = sts["shift"] * np.linalg.norm(us) / np.linalg.norm(f)
+    assert sts["unshifted_relres"] == pytest.approx(expect, rel=0.5)
 
 
 def test_fp32_solution_close(ctx, oracle, rng):

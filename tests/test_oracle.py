@@ -144,6 +144,22 @@ def test_helmholtz_reference_vs_direct(oracle, rng):
     assert np.abs(ref - d).max() < 1e-10 and it % 10 == 0
 
 
+@pytest.mark.parametrize("quirk", [True, False])
+def test_helmholtz_c_loop_matches_numpy_loop(oracle, rng, quirk):
+    """The C restatement of the filter's Jacobi-PCG (used where the numpy loop
+    is too slow, e.g. to make the 384x192x192 densities on the host) takes the
+    same iterations and gives the same field as the numpy loop."""
+    g = oracle.Grid(13, 7, 5)
+    rho = rng.uniform(0, 1, g.nelem)
+    ref, it_ref, rel_ref = oracle.helmholtz_reference(g, rho, 1.1, 1e-10, max_iter=500, quirk=quirk)
+    out, it, rel = oracle.helmholtz_pcg_c(g, rho, 1.1, 1e-10, max_iter=500, quirk=quirk)
+    assert it == it_ref
+    assert rel == pytest.approx(rel_ref, rel=1e-6)
+    assert np.abs(out - ref).max() <= 1e-13 * np.abs(ref).max()
+    z, itz, _ = oracle.helmholtz_pcg_c(g, np.zeros(g.nelem), 1.1, 1e-10)
+    assert itz == 0 and not z.any()
+
+
 def test_oc_volume_and_bounds(oracle, rng):
     x = rng.uniform(0, 1, 1000)
     dc = -rng.uniform(0.1, 2, 1000)

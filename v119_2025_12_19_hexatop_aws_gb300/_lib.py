@@ -58,7 +58,7 @@ class SolveStats(C.Structure):
         ("true_relres", C.c_double),
         ("shift", C.c_double), ("max_diag", C.c_double), ("compliance", C.c_double), ("setup_ms", C.c_double),
         ("solve_ms", C.c_double), ("total_ms", C.c_double), ("fine_applies", C.c_double),
-        ("fine_applies_fp64", C.c_double),
+        ("fine_applies_fp64", C.c_double), ("unshifted_relres", C.c_double),
     ]
 
     def as_dict(self) -> dict:

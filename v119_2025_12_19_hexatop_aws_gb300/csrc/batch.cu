@@ -665,6 +665,7 @@ int batch_problem(Ctx& c, int count, const hexa_grid* grids, const hexa_bc* bcs,
       st.smooth_steps = mg.nu2;
       st.relres = rel[i];
       st.true_relres = rel[i];
+      st.unshifted_relres = sigma[i] == 0.0 ? rel[i] : NAN;  // not recomputed for shifted batches
       st.shift = sigma[i];
       st.max_diag = hmax[i];
       st.compliance = hcomp[i];

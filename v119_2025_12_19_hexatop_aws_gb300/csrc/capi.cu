@@ -333,6 +333,8 @@ static int time_operator_t(hexa_ctx* h, const hexa_grid* g, const hexa_bc* bc, d
   else a.K = modal_to_f32(K64);
   a.sigma = T(0);
   a.omega = T(0.6);
+  a.xin = nullptr;
+  a.c1 = a.c2 = T(0);
   if (mode == OP_CHEB2) {  // in place over the previous iterate, as in the V-cycle
     a.xin = y;
     a.c1 = T(0.5);
@@ -340,8 +342,6 @@ static int time_operator_t(hexa_ctx* h, const hexa_grid* g, const hexa_bc* bc, d
   }
   a.kchunk = op_pick_kchunk<T>(G);
   a.diag_quirk = 1;
-  a.xin = nullptr;
-  a.c1 = a.c2 = T(0);
   const long long nb = op_num_blocks<T>(G, a.kchunk);
   if (!c.ensure_partials((size_t)nb * 2 + 64)) return HEXA_ERR_NOMEM;
   a.red.partials = c.partials;

@@ -2,8 +2,9 @@
 // that cannot allocate device memory.
 //
 // Some callers must not call cudaMalloc (or any allocating routine) at the
-// point where they filter: code that runs while an enclosing application is
-// capturing a CUDA stream (allocation is not a capturable operation), or
+// point where they filter: code that runs on its own stream while another
+// stream of the application is being captured into a CUDA graph (during a
+// global-mode capture an allocation is a prohibited call on every thread), or
 // hosts that hand the whole device-memory budget to their own pool and forbid
 // other allocations mid-run.  This entry point takes device arrays for its
 // input and output and keeps all of its scratch -- the six work vectors and
@@ -11,6 +12,17 @@
 // counter and the iteration scalars -- in one file-scope device array of fixed
 // size, so it allocates nothing: no cudaMalloc, no cudaFree, no allocating
 // library call.
+//
+// The call itself cannot be captured: it reads the iteration scalars back to
+// the host between groups of iterations and synchronizes its stream.  The
+// stream it is given must therefore not be capturing (HEXA_ERR_ARG
+// otherwise).  While another stream captures, pass a non-blocking stream
+// (cudaStreamNonBlocking): work on the legacy default stream (stream NULL)
+// would join a capture on any blocking stream.  For its own duration the call
+// switches the calling thread to the relaxed capture mode
+// (cudaThreadExchangeStreamCaptureMode), so its copies and synchronizations are
+// not refused because the application is capturing elsewhere, and restores the
+// thread's mode before it returns.
 //
 // The array holds HEXA_NOALLOC_MAX_NODES grid nodes (about 15 MB); every GPU
 // that loads the library keeps it until the process exits.  Every call shares
@@ -26,6 +38,7 @@
 #include <chrono>
 #include <cmath>
 #include <cstring>
+#include <limits>
 #include <mutex>
 
 #include "../../include/hexagpu.h"
@@ -70,14 +83,34 @@ double* scratch_for_current_device(int* err) {
   return g_addr[dev];
 }
 
-bool on_device(const void* p) {
+// Device memory of the current device (or managed memory): anything else --
+// host memory, or an array on another GPU while the scratch is resolved for
+// the current one -- is rejected.
+bool on_current_device(const void* p) {
   cudaPointerAttributes a;
   if (!p || cudaPointerGetAttributes(&a, p) != cudaSuccess) {
     cudaGetLastError();
     return false;
   }
-  return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+  if (a.type == cudaMemoryTypeManaged) return true;
+  if (a.type != cudaMemoryTypeDevice) return false;
+  int dev = -1;
+  if (cudaGetDevice(&dev) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return a.device == dev;
 }
+
+// Restores the calling thread's stream-capture mode on every return path.
+struct RelaxedCaptureMode {
+  cudaStreamCaptureMode prev = cudaStreamCaptureModeRelaxed;
+  bool ok = false;
+  RelaxedCaptureMode() { ok = cudaThreadExchangeStreamCaptureMode(&prev) == cudaSuccess; }
+  ~RelaxedCaptureMode() {
+    if (ok) cudaThreadExchangeStreamCaptureMode(&prev);
+  }
+};
 
 }  // namespace
 
@@ -90,11 +123,25 @@ extern "C" int hexa_filter_noalloc(const hexa_grid* g, const double* rho_in, dou
     return HEXA_ERR_ARG;
   const Grid G = make_grid(g->nx, g->ny, g->nz);
   if (G.nnode() > kMaxNodes) return HEXA_ERR_TOO_LARGE;
-  if (!on_device(rho_in) || !on_device(rho_out)) return HEXA_ERR_ARG;  // staging would need an allocation
+  RelaxedCaptureMode relaxed;  // before any other CUDA call of this entry point
+  if (!relaxed.ok) {
+    cudaGetLastError();
+    return HEXA_ERR_CUDA;
+  }
+  // staging a host array would need an allocation
+  if (!on_current_device(rho_in) || !on_current_device(rho_out)) return HEXA_ERR_ARG;
+  cudaStream_t st = (cudaStream_t)stream;
+  if (st) {  // the call synchronizes: it cannot run on a stream that is being captured
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(st, &cs) != cudaSuccess) {
+      cudaGetLastError();
+      return HEXA_ERR_ARG;
+    }
+    if (cs != cudaStreamCaptureStatusNone) return HEXA_ERR_ARG;
+  }
   int err = 0;
   double* base = scratch_for_current_device(&err);
   if (!base) return err;
-  cudaStream_t st = (cudaStream_t)stream;
 
   double Ke[64], Me[64];
   if (scalar_matrices(g->dx, g->dy, g->dz, quirk, Ke, Me) != 0) return HEXA_ERR_ARG;
@@ -168,7 +215,13 @@ extern "C" int hexa_filter_noalloc(const hexa_grid* g, const double* rho_in, dou
       }
       if (hs.halt) break;
     }
-    launch_helm_extract<double>(G, x, rho_out, st);
+    if (hs.status == 2 || hs.status == 4) {
+      // a NaN residual or a breakdown of p.Ap gives a NaN field, as hexa_filter
+      // and the reference's loop do (its callers test for it, TopOpt.jl:360-363)
+      launch_fill<double>(rho_out, std::numeric_limits<double>::quiet_NaN(), G.nelem(), st);
+    } else {
+      launch_helm_extract<double>(G, x, rho_out, st);
+    }
     out.iterations = hs.iter;
     out.relres = hs.relres;
   }

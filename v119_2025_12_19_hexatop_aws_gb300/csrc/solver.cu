@@ -1541,16 +1541,33 @@ int solve_block(Ctx& c, const Problem& P, int k, const hexa_solve_params& prm, d
   return status;
 }
 
+// ||f - K u|| / ||f|| in FP64 without the diagonal shift: the residual of the
+// unshifted system, which the shifted solve (GPUSolver.jl:343) leaves at about
+// sigma ||u|| / ||f||.  Equal to the solve's own true residual when sigma = 0.
+double unshifted_relres(Ctx& c, const Problem& P, int quirk, const double* u) {
+  ModalK<double> K64;
+  std::string e;
+  if (!build_modal(P.dx, P.dy, P.dz, P.nu, &K64, &e)) return NAN;
+  double* r64 = c.vec<double>("rtrue", P.g.ndof());
+  if (!r64) return NAN;
+  const double fnorm = std::sqrt(std::fmax(device_dot(c, P.f64, P.f64, P.g.ndof(), 13), 0.0));
+  if (fnorm == 0.0) return 0.0;
+  return true_residual_norm(c, P, K64, quirk, 0.0, u, r64) / fnorm;
+}
+
 }  // namespace
 
 int solve_problem(Ctx& c, const Problem& P, const hexa_solve_params& prm, const double* u0, double* u,
                   hexa_solve_stats* st) {
+  int rc;
   switch (prm.precision) {
-    case HEXA_PREC_FP64: return solve_plain<double>(c, P, prm, u0, u, st);
-    case HEXA_PREC_FP32: return solve_plain<float>(c, P, prm, u0, u, st);
-    case HEXA_PREC_MIXED: return solve_mixed(c, P, prm, u0, u, st);
+    case HEXA_PREC_FP64: rc = solve_plain<double>(c, P, prm, u0, u, st); break;
+    case HEXA_PREC_FP32: rc = solve_plain<float>(c, P, prm, u0, u, st); break;
+    case HEXA_PREC_MIXED: rc = solve_mixed(c, P, prm, u0, u, st); break;
     default: c.err = "unknown precision"; return HEXA_ERR_ARG;
   }
+  if (rc >= 0) st->unshifted_relres = (st->shift == 0.0) ? st->true_relres : unshifted_relres(c, P, prm.diag_quirk, u);
+  return rc;
 }
 
 int multi_rhs_problem(Ctx& c, const Problem& P, int k, const double* F_dev, const hexa_solve_params& prm,
@@ -1585,6 +1602,13 @@ int multi_rhs_problem(Ctx& c, const Problem& P, int k, const double* F_dev, cons
     acc.smooth_steps = s1.smooth_steps;
     acc.shift = s1.shift;
     acc.max_diag = s1.max_diag;
+    for (int j = 0; j < kb; ++j) {
+      Problem Qj = P;
+      Qj.f64 = F_dev + (long long)(j0 + j) * n;
+      const double* uj = U_dev + (long long)(j0 + j) * n;
+      const double ur = (s1.shift == 0.0 && kb == 1) ? s1.true_relres : unshifted_relres(c, Qj, prm.diag_quirk, uj);
+      acc.unshifted_relres = std::fmax(acc.unshifted_relres, ur);
+    }
   }
   *st = acc;
   return worst;

@@ -86,6 +86,7 @@ class SimpRecord:
     u: np.ndarray = field(repr=False)
     dc: np.ndarray = field(repr=False)
     xphys: np.ndarray = field(repr=False)
+    unshifted_relres: float = float("nan")  # ||f - K u|| / ||f|| in FP64, without the diagonal shift
 
 
 def run_simp(S: SimpSetup, x0: np.ndarray, n_iter: int = 10, keep=True, ctx=None) -> list[SimpRecord]:
@@ -105,7 +106,7 @@ def run_simp(S: SimpSetup, x0: np.ndarray, n_iter: int = 10, keep=True, ctx=None
         dcx, _ = filter_density(S.grid, dc, S.filter_radius, tol=S.filter_tol, quirk=False, max_iter=10000, ctx=ctx)
         hist.append(SimpRecord(c, float(xphys.mean()), int(st["iterations"]), float(st["true_relres"]),
                                u.copy() if keep else None, dc.copy() if keep else None,
-                               xphys.copy() if keep else None))
+                               xphys.copy() if keep else None, float(st["unshifted_relres"])))
         x, _ = oc_update(x, dcx, dv, S.volfrac, S.move, ctx=ctx)
     return hist
 
