@@ -198,6 +198,27 @@ int hexa_solve_system_gpu(hexa_ctx* ctx, const hexa_grid* g, float E, const floa
                           const float* u_guess, double* u_out, double* relres_out,
                           char* method_out, int32_t method_cap, hexa_solve_stats* stats);
 
+/* Replaces Solver.solve_system for the gpu solver type (src/Solvers/Solver.jl:39-160),
+ * the call the SIMP loop makes (src/Main.jl:439-443), with the same argument
+ * types as hexa_solve_system_gpu plus the dispatcher's own:
+ * min_stiffness_threshold, prune_voids and config["current_outer_iter"].  When
+ * prune_voids is set, current_outer_iter >= 3 and fewer than 99 % of the
+ * elements have density > min_stiffness_threshold * 1.01f (Solver.jl:66-90),
+ * the system solved is the pruned one of MeshPruner.prune_system
+ * (src/Mesh/MeshPruner.jl:10-87): those elements removed, the nodes no kept
+ * element touches removed (their loads dropped), the shift taken from the
+ * pruned diagonal; u_out then holds zeros at removed nodes, as
+ * reconstruct_full_solution (MeshPruner.jl:89-107) writes.  On the structured
+ * grid this is the full grid with the removed elements' factors set to zero
+ * and the removed nodes' DOFs fixed.  No element kept: HEXA_ERR_ARG with the
+ * reference's message.  active_elements (nullable) receives the number of
+ * elements in the solved system.  u_prev may be NULL. */
+int hexa_solve_system(hexa_ctx* ctx, const hexa_grid* g, float E, const float* bc_indicator, const float* f,
+                      const float* density, float min_stiffness_threshold, int32_t prune_voids,
+                      int32_t current_outer_iter, const hexa_solve_params* p, const float* u_prev, double* u_out,
+                      double* relres_out, char* method_out, int32_t method_cap, hexa_solve_stats* stats,
+                      int64_t* active_elements);
+
 /* No counterpart in the reference (it solves one load case per call,
  * GPUSolver.jl:467-477): k load cases as one block PCG (each K0/factor load
  * serves k right-hand sides).  F and U are k consecutive 3*nNodes vectors. */

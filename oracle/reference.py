@@ -158,6 +158,106 @@ def direct_solve(g: Grid, K0, factor, f, fixed, sigma=0.0) -> np.ndarray:
     return u
 
 
+# ------------------------------------------------------------ void pruning
+def prune_system(nodes, elements, density, threshold, bc_indicator, F):
+    """MeshPruner.prune_system (src/Mesh/MeshPruner.jl:10-87), 0-based: keeps the
+    elements with density > threshold and the nodes they touch, renumbered in
+    increasing old order; bc rows, loads and densities follow."""
+    density = np.asarray(density, dtype=np.float32)
+    active = np.nonzero(density > np.float32(threshold))[0]
+    if active.size == 0:
+        raise ValueError(f"MeshPruner: No active elements found (Threshold: {threshold}). System is empty.")
+    n_nodes = np.asarray(nodes).shape[0]
+    on = np.zeros(n_nodes, dtype=bool)
+    on[np.asarray(elements)[active].ravel()] = True
+    new_to_old = np.nonzero(on)[0]
+    old_to_new = np.full(n_nodes, -1, dtype=np.int64)
+    old_to_new[new_to_old] = np.arange(new_to_old.size)
+    return dict(nodes=np.asarray(nodes)[new_to_old], elements=old_to_new[np.asarray(elements)[active]],
+                bc_indicator=np.asarray(bc_indicator)[new_to_old],
+                F=np.asarray(F, dtype=np.float32).reshape(-1, 3)[new_to_old].ravel(),
+                density=density[active], new_to_old_node_map=new_to_old, active_element_indices=active)
+
+
+def reconstruct_full_solution(u_reduced, new_to_old, n_full_nodes):
+    """MeshPruner.reconstruct_full_solution (MeshPruner.jl:89-107): zeros at removed nodes."""
+    u = np.zeros((n_full_nodes, 3), dtype=np.asarray(u_reduced).dtype)
+    u[new_to_old] = np.asarray(u_reduced).reshape(-1, 3)
+    return u.ravel()
+
+
+def solve_mesh(elements, K0, factor, F, fixed, shift_factor, tol=1e-14, max_iter=100000):
+    """(K_ff + sigma I) u = f_free on an arbitrary hex8 connectivity (elements:
+    (nElem, 8) 0-based node indices in the K0 node order), sigma = shift_factor
+    * max over free DOFs of the x-diagonal form (GPUSolver.jl:130-144, 343),
+    by Jacobi-PCG on the assembled sparse matrix to a tight residual."""
+    elements = np.asarray(elements)
+    ndof = 3 * (int(elements.max()) + 1)
+    ndof = max(ndof, np.asarray(F).size)
+    dofs = (3 * elements[:, :, None] + np.arange(3)[None, None, :]).reshape(-1, 24)
+    rows = np.repeat(dofs, 24, axis=1).ravel()
+    cols = np.tile(dofs, (1, 24)).ravel()
+    vals = (np.asarray(factor, dtype=np.float64)[:, None] * np.asarray(K0).ravel(order="C")[None, :]).ravel()
+    K = sp.csr_matrix((vals, (rows, cols)), shape=(ndof, ndof))
+    dq = np.zeros(ndof)
+    np.add.at(dq, dofs.ravel(), np.tile(np.repeat(np.diag(K0)[0::3], 3), elements.shape[0]) *
+              np.repeat(np.asarray(factor, dtype=np.float64), 24))
+    free = np.nonzero(~np.asarray(fixed, dtype=bool))[0]
+    sigma = shift_factor * dq[free].max() if free.size else 0.0
+    A = (K[free][:, free] + sigma * sp.identity(free.size)).tocsr()
+    b = np.asarray(F, dtype=np.float64)[free]
+    d = A.diagonal()
+    x = np.zeros_like(b)
+    r = b.copy()
+    nb = np.linalg.norm(b)
+    u = np.zeros(ndof)
+    if nb == 0.0:
+        return u, sigma
+    z = r / d
+    p = z.copy()
+    rz = r @ z
+    for _ in range(max_iter):
+        q = A @ p
+        a = rz / (p @ q)
+        x += a * p
+        r -= a * q
+        if np.linalg.norm(r) / nb < tol:
+            break
+        z = r / d
+        rzn = r @ z
+        p = z + (rzn / rz) * p
+        rz = rzn
+    u[free] = x
+    return u, sigma
+
+
+def solve_system_pruned(g: Grid, E, density, bc_indicator, F, *, min_stiffness_threshold, prune_voids,
+                        current_outer_iter, shift_factor, nu=0.3, tol=1e-14):
+    """Solver.solve_system's gpu path (src/Solvers/Solver.jl:39-160) with its
+    pruning rule: from outer iteration 3, when fewer than 99 % of the elements
+    have density > min_stiffness_threshold * 1.01f0, the MeshPruner system is
+    solved and mapped back; else the full system.  factor = Float32(E .*
+    density) (GPUSolver.jl:254).  Returns (U_full, active element count)."""
+    nodes = np.zeros((g.nnode, 3), dtype=np.float32)
+    elements = element_nodes(g)
+    K0 = canonical_stiffness(g.dx, g.dy, g.dz, nu)
+    density = np.asarray(density, dtype=np.float32)
+    thr = np.float32(min_stiffness_threshold) * np.float32(1.01)
+    prune = bool(prune_voids) and current_outer_iter >= 3
+    if prune:
+        prune = np.count_nonzero(density > thr) < g.nelem * 0.99
+    if not prune:
+        fixed = np.asarray(bc_indicator).reshape(-1) > 0
+        fac = (np.float32(E) * density).astype(np.float64)
+        u, _ = solve_mesh(elements, K0, fac, F, fixed, shift_factor, tol)
+        return u, g.nelem
+    P = prune_system(nodes, elements, density, thr, bc_indicator, F)
+    fixed = np.asarray(P["bc_indicator"]).reshape(-1) > 0
+    fac = (np.float32(E) * P["density"]).astype(np.float64)
+    u_red, _ = solve_mesh(P["elements"], K0, fac, P["F"], fixed, shift_factor, tol)
+    return reconstruct_full_solution(u_red, P["new_to_old_node_map"], g.nnode), int(P["active_element_indices"].size)
+
+
 # ----------------------------------------------------- reference PCG control
 @dataclass
 class PcgInfo:

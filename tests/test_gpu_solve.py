@@ -258,3 +258,56 @@ def test_mixed_matches_fp64_on_a_grid_with_interior_tiles(ctx, oracle, rng):
     assert sm["true_relres"] <= 1e-11
     assert np.linalg.norm(um - u64) <= 1e-7 * np.linalg.norm(u64)
     assert abs(sm["compliance"] - s64["compliance"]) <= 1e-10 * abs(s64["compliance"])
+
+
+def _voided_density(oracle, g, seed, void_frac=0.15, thr=1e-3):
+    rng = np.random.default_rng(seed)
+    s = oracle.helmholtz_direct(g, rng.standard_normal(g.nelem), 0.8, quirk=False)
+    rho = np.clip(0.3 + 0.4 * (s - s.mean()) / s.std(), 0.05, 1.0)
+    rho[s <= np.quantile(s, void_frac)] = thr
+    return rho.astype(np.float32)
+
+
+@pytest.mark.parametrize("shift_factor", [1e-10, 0.0])
+def test_solve_system_prunes_voids_like_the_reference(ctx, oracle, shift_factor):
+    """Main.jl:439-443 calls Solver.solve_system with prune_voids=true.  From
+    outer iteration 3, with 15 % of the elements at the minimum density, the
+    reference solves MeshPruner's compacted system and maps it back
+    (Solver.jl:85-156); the oracle restates exactly that (renumbered mesh,
+    assembled, Jacobi-PCG to 1e-14).  The library's solve_system on the full
+    structured mesh gives the same U_full within 1e-10, zeros at the removed
+    nodes, and the unpruned solve before iteration 3."""
+    dims = workloads.SIZES["c1"]
+    g = oracle.Grid(*dims)
+    nodes, elements, bc, F = _reference_inputs(dims)
+    dens = _voided_density(oracle, g, seed=11)
+    cfg = {"solver_parameters": {"solver_type": "gpu", "preconditioner": "multigrid", "tolerance": 1e-13,
+                                 "max_iterations": 60000, "diagonal_shift_factor": shift_factor},
+           "force_float64": True, "geometry": {}, "current_outer_iter": 3}
+    st = {}
+    u, relres, name = solve_system(nodes, elements, 1.0, 0.3, bc, F, density=dens, config=cfg,
+                                   min_stiffness_threshold=np.float32(1e-3), prune_voids=True, stats=st)
+    assert name == "GMG_GPU" and st["status"] == 0
+    u_ref, nact = oracle.solve_system_pruned(g, 1.0, dens, bc, F, min_stiffness_threshold=np.float32(1e-3),
+                                             prune_voids=True, current_outer_iter=3, shift_factor=float(np.float32(shift_factor)))
+    assert st["active_elements"] == nact < 0.99 * g.nelem
+    assert rel(u, u_ref) <= 1e-10
+    assert abs(F @ u - F @ u_ref) <= 1e-10 * abs(F @ u_ref)
+    on = np.zeros(g.nnode, dtype=bool)
+    on[oracle.element_nodes(g)[dens > np.float32(1e-3) * np.float32(1.01)].ravel()] = True
+    assert (~on).any() and not u.reshape(-1, 3)[~on].any()  # reconstruct_full_solution's zeros
+    cfg2 = dict(cfg, current_outer_iter=2)
+    st2 = {}
+    solve_system(nodes, elements, 1.0, 0.3, bc, F, density=dens, config=cfg2, min_stiffness_threshold=np.float32(1e-3),
+                 prune_voids=True, stats=st2)
+    assert st2["active_elements"] == g.nelem
+
+
+def test_solve_system_with_every_element_pruned_is_an_error(ctx):
+    dims = (8, 4, 4)
+    nodes, elements, bc, F = _reference_inputs(dims)
+    cfg = {"solver_parameters": {"solver_type": "gpu", "tolerance": 1e-9, "diagonal_shift_factor": 1e-10},
+           "force_float64": True, "geometry": {}, "current_outer_iter": 5}
+    with pytest.raises(_lib.HexaError, match="No active elements"):
+        solve_system(nodes, elements, 1.0, 0.3, bc, F, density=np.full(128, 1e-3, np.float32), config=cfg,
+                     min_stiffness_threshold=np.float32(1e-3), prune_voids=True)

@@ -114,6 +114,8 @@ SIGNATURES = {
                          C.POINTER(SolveStats)]),
     "hexa_solve_system_gpu": (I32, [P, C.POINTER(Grid), C.c_float, P, P, P, C.POINTER(SolveParams), P, P,
                                     C.POINTER(D), C.c_char_p, I32, C.POINTER(SolveStats)]),
+    "hexa_solve_system": (I32, [P, C.POINTER(Grid), C.c_float, P, P, P, C.c_float, I32, I32, C.POINTER(SolveParams),
+                                P, P, C.POINTER(D), C.c_char_p, I32, C.POINTER(SolveStats), C.POINTER(I64)]),
     "hexa_solve_multi_rhs": (I32, [P, C.POINTER(Grid), C.POINTER(BC), P, I32, P, C.POINTER(SolveParams), P,
                                    C.POINTER(SolveStats)]),
     "hexa_solve_batch": (I32, [P, I32, C.POINTER(Grid), C.POINTER(BC), D, C.POINTER(P), C.POINTER(P),

@@ -8,6 +8,7 @@
 #include <algorithm>
 #include <chrono>
 #include <cmath>
+#include <cstdio>
 #include <cstring>
 #include <limits>
 #include <new>
@@ -439,13 +440,26 @@ int hexa_solve(hexa_ctx* h, const hexa_grid* g, const hexa_bc* bc, const double*
   return rc;
 }
 
-int hexa_solve_system_gpu(hexa_ctx* h, const hexa_grid* g, float E, const float* bc_indicator, const float* f,
-                          const float* density, const hexa_solve_params* p, const float* u_guess, double* u_out,
-                          double* relres_out, char* method_out, int32_t method_cap, hexa_solve_stats* stats) {
+}  // extern "C"
+
+// Body of the two reference-signature entries: the reference's Float32
+// arguments converted on the host, optionally with the void pruning of
+// Solver.solve_system (MeshPruner.prune_system, src/Mesh/MeshPruner.jl:10-87)
+// restated on the structured grid.  Pruning removes the elements with density
+// <= prune_thr and the nodes no kept element touches, then renumbers; on the
+// structured grid the same system is the full grid with those elements'
+// factors set to zero and the removed nodes' DOFs fixed: K_ff, f_free, the
+// diagonal and its maximum (hence sigma) are then exactly the pruned
+// system's, and the solver's zeros at fixed DOFs are what
+// reconstruct_full_solution (MeshPruner.jl:89-107) writes at removed nodes.
+static int solve_reference_args(hexa_ctx* h, const hexa_grid* g, float E, const float* bc_indicator, const float* f,
+                                const float* density, bool prune, float prune_thr, const hexa_solve_params* p,
+                                const float* u_guess, double* u_out, double* relres_out, char* method_out,
+                                int32_t method_cap, hexa_solve_stats* stats, int64_t* active_out) {
   if (!h) return HEXA_ERR_ARG;
   if (!valid_grid(g) || !f || !density || !u_out || !bc_indicator) return set_err(h, HEXA_ERR_ARG, "invalid grid or null array");
-  Ctx& c = h->c;
-  const long long nn = (long long)(g->nx + 1) * (g->ny + 1) * (g->nz + 1);
+  const long long NX = g->nx + 1, NY = g->ny + 1;
+  const long long nn = NX * NY * (g->nz + 1);
   const long long ne = (long long)g->nx * g->ny * g->nz;
   // host conversion of the reference's Float32 arguments
   std::vector<float> hd(ne), hf(3 * nn), hb(3 * nn);
@@ -456,12 +470,36 @@ int hexa_solve_system_gpu(hexa_ctx* h, const hexa_grid* g, float E, const float*
   fetch(density, hd.data(), ne);
   fetch(f, hf.data(), 3 * nn);
   fetch(bc_indicator, hb.data(), 3 * nn);
+  std::vector<uint8_t> elem_on, node_on;
+  long long nactive = ne;
+  if (prune) {
+    elem_on.assign(ne, 0);
+    node_on.assign(nn, 0);
+    nactive = 0;
+    for (long long e = 0; e < ne; ++e) {
+      if (!(hd[e] > prune_thr)) continue;  // active_mask = density .> threshold (MeshPruner.jl:20)
+      elem_on[e] = 1;
+      ++nactive;
+      const long long i = e % g->nx, j = (e / g->nx) % g->ny, k = e / ((long long)g->nx * g->ny);
+      for (int c = 0; c < 8; ++c)
+        node_on[(i + (c & 1)) + NX * ((j + ((c >> 1) & 1)) + NY * (k + (c >> 2)))] = 1;
+    }
+    if (nactive == 0) {
+      char msg[160];
+      std::snprintf(msg, sizeof(msg), "MeshPruner: No active elements found (Threshold: %g). System is empty.",
+                    (double)prune_thr);
+      return set_err(h, HEXA_ERR_ARG, msg);
+    }
+  }
+  if (active_out) *active_out = nactive;
   std::vector<double> fac(ne), fd(3 * nn), ug;
-  for (long long e = 0; e < ne; ++e) fac[e] = (double)(float)(E * hd[e]);  // Vector{T}(E .* density)
+  for (long long e = 0; e < ne; ++e)  // Vector{T}(E .* density), GPUSolver.jl:254; pruned elements removed
+    fac[e] = (prune && !elem_on[e]) ? 0.0 : (double)(float)(E * hd[e]);
   for (long long i = 0; i < 3 * nn; ++i) fd[i] = (double)hf[i];
   std::vector<uint8_t> fixed(3 * nn);
   for (long long n = 0; n < nn; ++n)
-    for (int d = 0; d < 3; ++d) fixed[3 * n + d] = hb[n + nn * d] > 0.0f ? 1 : 0;  // column-major Matrix(nNodes,3)
+    for (int d = 0; d < 3; ++d)  // column-major Matrix(nNodes,3); removed nodes are not in the system
+      fixed[3 * n + d] = (hb[n + nn * d] > 0.0f || (prune && !node_on[n])) ? 1 : 0;
   if (u_guess) {
     std::vector<float> hu(3 * nn);
     fetch(u_guess, hu.data(), 3 * nn);
@@ -481,8 +519,40 @@ int hexa_solve_system_gpu(hexa_ctx* h, const hexa_grid* g, float E, const float*
     method_out[method_cap - 1] = 0;
   }
   if (stats) *stats = st;
-  (void)c;
   return rc;
+}
+
+extern "C" {
+
+int hexa_solve_system_gpu(hexa_ctx* h, const hexa_grid* g, float E, const float* bc_indicator, const float* f,
+                          const float* density, const hexa_solve_params* p, const float* u_guess, double* u_out,
+                          double* relres_out, char* method_out, int32_t method_cap, hexa_solve_stats* stats) {
+  return solve_reference_args(h, g, E, bc_indicator, f, density, false, 0.0f, p, u_guess, u_out, relres_out,
+                              method_out, method_cap, stats, nullptr);
+}
+
+int hexa_solve_system(hexa_ctx* h, const hexa_grid* g, float E, const float* bc_indicator, const float* f,
+                      const float* density, float min_stiffness_threshold, int32_t prune_voids,
+                      int32_t current_outer_iter, const hexa_solve_params* p, const float* u_prev, double* u_out,
+                      double* relres_out, char* method_out, int32_t method_cap, hexa_solve_stats* stats,
+                      int64_t* active_elements) {
+  if (!h) return HEXA_ERR_ARG;
+  if (!valid_grid(g) || !density) return set_err(h, HEXA_ERR_ARG, "invalid grid or null array");
+  // Solver.jl:66-72: the GPU solver type prunes from outer iteration 3 on
+  bool prune = prune_voids != 0 && current_outer_iter >= 3;
+  // Solver.jl:85-90: threshold min_stiffness_threshold * 1.01f0, pruned only below 99 % active
+  const float thr = min_stiffness_threshold * 1.01f;
+  if (prune) {
+    const long long ne = (long long)g->nx * g->ny * g->nz;
+    std::vector<float> hd(ne);
+    if (is_device_ptr(density)) cudaMemcpy(hd.data(), density, ne * sizeof(float), cudaMemcpyDeviceToHost);
+    else std::memcpy(hd.data(), density, ne * sizeof(float));
+    long long nact = 0;
+    for (long long e = 0; e < ne; ++e) nact += hd[e] > thr ? 1 : 0;
+    prune = (double)nact < (double)ne * 0.99;
+  }
+  return solve_reference_args(h, g, E, bc_indicator, f, density, prune, thr, p, u_prev, u_out, relres_out,
+                              method_out, method_cap, stats, active_elements);
 }
 
 int hexa_solve_multi_rhs(hexa_ctx* h, const hexa_grid* g, const hexa_bc* bc, const double* factor, int32_t k,

@@ -18,7 +18,6 @@ preconditioner, stagnation_tolerance, max_shift_attempts, shift_multiplier}``,
 from __future__ import annotations
 
 import ctypes as C
-import warnings
 
 import numpy as np
 
@@ -177,13 +176,18 @@ def solve_system_gpu(nodes, elements, E, nu, bc, f, density, *, max_iter=40000, 
 
 
 def solve_system(nodes, elements, E, nu, bc_indicator, F, *, density, config, min_stiffness_threshold=1.0e-3,
-                 prune_voids=True, u_prev=None):
-    """Solver.solve_system for solver_type "gpu" (Solver.jl:39-160).
+                 prune_voids=True, u_prev=None, stats=None):
+    """Solver.solve_system for solver_type "gpu" (Solver.jl:39-160): returns
+    (U_full, relres, name).
 
-    The tolerance is cast to Float32 as the reference does (Solver.jl:57).
-    Void pruning (MeshPruner) produces unstructured meshes the structured
-    kernels cannot take, so it is not performed; the reference itself skips it
-    while current_outer_iter < 3 (Solver.jl:67-72)."""
+    The tolerance and shift factor are cast to Float32 as the reference does
+    (Solver.jl:57-59).  Void pruning keeps the reference's rule (from
+    config["current_outer_iter"] 3 on, when fewer than 99 % of the elements
+    have density > 1.01 min_stiffness_threshold, MeshPruner.jl:10-87): the
+    library solves the pruned system on the structured grid (removed elements'
+    factors zero, removed nodes' DOFs fixed) and U_full is zero at removed
+    nodes, as reconstruct_full_solution writes.  `stats`, when a dict, receives
+    the solve statistics and the number of elements in the solved system."""
     sp = config["solver_parameters"]
     stype = str(sp.get("solver_type", "direct")).lower()
     if stype != "gpu":
@@ -191,11 +195,36 @@ def solve_system(nodes, elements, E, nu, bc_indicator, F, *, density, config, mi
     tol = float(np.float32(sp.get("tolerance", 1.0e-6)))
     max_iter = int(sp.get("max_iterations", 1000))
     shift = float(np.float32(sp.get("diagonal_shift_factor", 1.0e-6)))
-    if prune_voids and int(config.get("current_outer_iter", 1)) >= 3:
-        warnings.warn("prune_voids ignored: the structured GPU path solves the full grid", stacklevel=2)
-    return solve_system_gpu(nodes, elements, np.float32(E), np.float32(nu), bc_indicator, F, density,
-                            max_iter=max_iter, tol=tol, shift_factor=shift,
-                            min_stiffness_threshold=min_stiffness_threshold, u_guess=u_prev, config=config)
+    nx, ny, nz, dx, dy, dz = structured_dims(nodes, elements)
+    geom = config.get("geometry", {}) or {}
+    grid = _lib.make_grid(nx, ny, nz, float(geom.get("dx_computed", dx)), float(geom.get("dy_computed", dy)),
+                          float(geom.get("dz_computed", dz)))
+    params = params_from_config(config, nu=nu, tol=tol, max_iter=max_iter, shift_factor=shift)
+    has_density = density is not None and len(density) > 0
+    dens = np.ascontiguousarray(density if has_density else np.ones(nx * ny * nz), dtype=np.float32)
+    bc_cm = np.ascontiguousarray(np.asarray(bc_indicator, dtype=np.float32).ravel(order="F"))  # Matrix(nNodes,3)
+    f32 = np.ascontiguousarray(np.asarray(F, dtype=np.float32))
+    guess = None
+    if u_prev is not None and len(u_prev) == len(f32):
+        guess = np.ascontiguousarray(np.asarray(u_prev, dtype=np.float32))
+    u = np.empty(f32.shape[0], dtype=np.float64)
+    relres = C.c_double()
+    name = C.create_string_buffer(32)
+    active = C.c_int64()
+    st = _lib.SolveStats()
+    ctx = context()
+    rc = ctx.lib.hexa_solve_system(ctx.h, C.byref(grid), float(np.float32(E)), _lib.ptr(bc_cm), _lib.ptr(f32),
+                                   _lib.ptr(dens), float(np.float32(min_stiffness_threshold)),
+                                   int(bool(prune_voids) and has_density), int(config.get("current_outer_iter", 1)),
+                                   C.byref(params), _lib.ptr(guess), _lib.ptr(u), C.byref(relres), name, 32,
+                                   C.byref(st), C.byref(active))
+    if rc == _lib.HEXA_ERR_CORRUPT_INPUT:
+        return np.zeros(u.shape[0], dtype=np.float64), float("nan"), "Failed_Corrupt_Input"
+    ctx.check(rc)
+    if isinstance(stats, dict):
+        stats.update(st.as_dict())
+        stats["active_elements"] = int(active.value)
+    return u, float(relres.value), name.value.decode()
 
 
 def apply_operator(grid, factor, x, *, nu=0.3, sigma=0.0, clamp_faces=0, fixed_dof=None, ctx=None, fp32=False):
