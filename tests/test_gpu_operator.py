@@ -129,3 +129,46 @@ def test_timed_chebyshev_step_reads_its_previous_iterate(ctx, oracle, rng, dims)
     assert rc == _lib.HEXA_OK and t.value > 0
     got = y_d.cpu().numpy().astype(np.float64)
     assert np.abs(got - want).max() <= 2e-5 * np.abs(want).max()
+
+
+def test_staged_operator_wait_that_runs_out_is_reported():
+    """Every wait of the TMA-staged FP32 operator is bounded.  With
+    HEXA_OP_TEST_STALL=q, CTA 0 leaves out its layer load q, so its threads'
+    wait for that layer runs out (about half a second of clock cycles): the
+    kernel sets its error word, drains its other copies and returns, and the
+    call reports HEXA_ERR_CUDA with the reason.  The context stays usable: an
+    FP64 apply (no staging) afterwards is correct.  Runs in a child process
+    because the variable is read once per process."""
+    import os
+    import subprocess
+    import sys
+    from pathlib import Path
+    root = str(Path(__file__).resolve().parents[1])
+    script = f"""
+import sys
+sys.path.insert(0, {root!r})
+import numpy as np
+from oracle import reference as ref
+from v119_2025_12_19_hexatop_aws_gb300 import _lib
+from v119_2025_12_19_hexatop_aws_gb300.solver import apply_operator
+ctx = _lib.Context(0)
+g = _lib.make_grid(40, 20, 20)
+rng = np.random.default_rng(0)
+fac = rng.uniform(0.1, 1, 40 * 20 * 20)
+x = rng.standard_normal(3 * 41 * 21 * 21)
+try:
+    apply_operator(g, fac.astype(np.float32), x.astype(np.float32), clamp_faces=1, ctx=ctx, fp32=True)
+    print("NO_ERROR")
+except _lib.HexaError as e:
+    print("ERR", e.code, str(e))
+y = apply_operator(g, fac, x, clamp_faces=1, ctx=ctx)
+gg = ref.Grid(40, 20, 20)
+y_ref = ref.apply_A(gg, ref.canonical_stiffness(1, 1, 1, 0.3), fac, x, ref.fixed_mask(gg, 1))
+print("FP64_ERR", float(np.abs(y - y_ref).max() / np.abs(y_ref).max()))
+"""
+    env = dict(os.environ, HEXA_OP_TEST_STALL="5")
+    r = subprocess.run([sys.executable, "-c", script], env=env, capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr[-2000:]
+    assert "ERR -2" in r.stdout and "bounded wait ran out" in r.stdout, r.stdout
+    err = float(r.stdout.split("FP64_ERR")[1].split()[0])
+    assert err < 1e-13

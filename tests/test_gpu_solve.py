@@ -48,7 +48,8 @@ def test_solution_matches_direct(ctx, oracle, rng, precond, precision, shift_fac
     assert st["shift"] == pytest.approx(sigma, rel=1e-12, abs=0.0)
     assert st["true_relres"] <= 1e-13
     r_unshifted = np.linalg.norm(f * ~fixed - oracle.apply_A(g, K0, fac, u, fixed)) / np.linalg.norm(f)
-    assert st["unshifted_relres"] == pytest.approx(r_unshifted, rel=1e-6, abs=1e-15)
+    # at a 1e-13 residual the FP64 recomputations (GPU and oracle) differ in their own rounding
+    assert abs(st["unshifted_relres"] - r_unshifted) <= 0.1 * r_unshifted + 1e-14
     if shift_factor == 0.0:
         assert st["unshifted_relres"] == st["true_relres"]
     assert rel(u, u_ref) <= 1e-10

@@ -24,6 +24,7 @@ namespace hexa {
 namespace {
 
 constexpr int kThreads = 256;
+constexpr int kGramFold = 8;  // tiles summed in T before one fold into the FP64 accumulators
 
 template <typename T>
 constexpr int gram_td() { return sizeof(T) == 8 ? 64 : 128; }
@@ -42,8 +43,11 @@ __device__ __forceinline__ bool halt_set(const int* h) { return h && *((volatile
 
 // out[i * NBC + j] = sum_d a_i[d] * b_j[d] for i < KC, j < NBC, where
 // b_j = b1_j for j < KC and b2_{j-KC} otherwise; columns >= k read as zero.
-// Tiles of TD DOFs are staged in shared memory; each thread accumulates an
-// RI x RJ block of pairs over one DOF slice in T, folded to FP64 per tile.
+// Tiles of TD DOFs are staged in shared memory (a warp loads one column's TD
+// consecutive values: coalesced, shift-and-mask indexing); each thread
+// accumulates an RI x RJ block of pairs over one DOF slice in T across
+// kGramFold tiles before folding into FP64 -- GB300's FP64 rate is a small
+// fraction of its FP32 rate, and folding every tile made the pass FP64-bound.
 // Per-block partials are summed in block order by the last block (ticket):
 // the result is bitwise reproducible.
 template <typename T, int KC, int NB>
@@ -66,26 +70,32 @@ __global__ void __launch_bounds__(kThreads) gram_kernel(const T* __restrict__ a,
   for (int i = 0; i < S::RI; ++i)
 #pragma unroll
     for (int j = 0; j < S::RJ; ++j) acc[i][j] = 0.0;
+  static_assert((TD & (TD - 1)) == 0, "TD is a power of two");
+  constexpr int TDLOG = TD == 128 ? 7 : 6;
   const long long ntiles = (n + TD - 1) / TD;
+  T part[S::RI][S::RJ];
+#pragma unroll
+  for (int i = 0; i < S::RI; ++i)
+#pragma unroll
+    for (int j = 0; j < S::RJ; ++j) part[i][j] = T(0);
+  int folded = 0;
   for (long long t = blockIdx.x; t < ntiles; t += gridDim.x) {
     const long long d0 = t * TD;
+    const bool full = d0 + TD <= n;
+#pragma unroll 4
     for (int e = tid; e < (KC + S::NBC) * TD; e += kThreads) {
-      const int col = e / TD, d = e - col * TD;
+      const int col = e >> TDLOG, d = e & (TD - 1);
       const long long gd = d0 + d;
+      const bool in = full || gd < n;
       if (col < KC) {
-        sA[col][d] = (col < k && gd < n) ? a[(long long)col * n + gd] : T(0);
+        sA[col][d] = (col < k && in) ? a[(long long)col * n + gd] : T(0);
       } else {
-        const int cb = col - KC, j = cb % KC;
+        const int cb = col - KC, j = cb < KC ? cb : cb - KC;
         const T* src = cb < KC ? b1 : b2;
-        sB[cb][d] = (j < k && gd < n) ? src[(long long)j * n + gd] : T(0);
+        sB[cb][d] = (j < k && in) ? src[(long long)j * n + gd] : T(0);
       }
     }
     __syncthreads();
-    T part[S::RI][S::RJ];
-#pragma unroll
-    for (int i = 0; i < S::RI; ++i)
-#pragma unroll
-      for (int j = 0; j < S::RJ; ++j) part[i][j] = T(0);
     for (int d = slice; d < TD; d += S::SLICES) {
       T av[S::RI], bv[S::RJ];
 #pragma unroll
@@ -97,16 +107,20 @@ __global__ void __launch_bounds__(kThreads) gram_kernel(const T* __restrict__ a,
 #pragma unroll
         for (int j = 0; j < S::RJ; ++j) part[i][j] = fma(av[i], bv[j], part[i][j]);
     }
+    if (++folded == kGramFold) {
+      folded = 0;
 #pragma unroll
-    for (int i = 0; i < S::RI; ++i)
+      for (int i = 0; i < S::RI; ++i)
 #pragma unroll
-      for (int j = 0; j < S::RJ; ++j) acc[i][j] += (double)part[i][j];
+        for (int j = 0; j < S::RJ; ++j) acc[i][j] += (double)part[i][j], part[i][j] = T(0);
+    }
     __syncthreads();
   }
 #pragma unroll
   for (int i = 0; i < S::RI; ++i)
 #pragma unroll
-    for (int j = 0; j < S::RJ; ++j) sred[slice][(gi * S::RI + i) * S::NBC + gj * S::RJ + j] = acc[i][j];
+    for (int j = 0; j < S::RJ; ++j)
+      sred[slice][(gi * S::RI + i) * S::NBC + gj * S::RJ + j] = acc[i][j] + (double)part[i][j];
   __syncthreads();
   for (int p = tid; p < S::NPAIR; p += kThreads) {
     double s = 0.0;

@@ -114,6 +114,14 @@ bool prepare_problem(hexa_ctx* h, const hexa_grid* g, const hexa_bc* bc, double 
   return true;
 }
 
+// A staged operator launch that gave up a bounded wait (op.cu) leaves its
+// output incomplete: the call reports it as a CUDA-level failure.
+bool staging_ok(hexa_ctx* h, const char* where) {
+  if (!op_take_wait_error(h->c.st)) return true;
+  h->c.err = std::string(where) + ": an operator launch gave up waiting for its staged input (bounded wait ran out)";
+  return false;
+}
+
 double wall_ms(std::chrono::steady_clock::time_point t0) {
   return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
 }
@@ -288,6 +296,7 @@ static int apply_operator_t(hexa_ctx* h, const hexa_grid* g, const hexa_bc* bc, 
   c.launches += 2;
   stage_out<T>(c, y, yd, G.ndof());
   if (cudaStreamSynchronize(c.st) != cudaSuccess || !c.cuda_ok("apply")) return set_err(h, HEXA_ERR_CUDA, c.err);
+  if (!staging_ok(h, "apply")) return HEXA_ERR_CUDA;
   float ms = 0;
   cudaEventElapsedTime(&ms, c.ev[0], c.ev[1]);
   c.last_ms = ms;
@@ -358,6 +367,7 @@ static int time_operator_t(hexa_ctx* h, const hexa_grid* g, const hexa_bc* bc, d
   cudaEventRecord(c.ev[1], c.st);
   c.launches += reps + 1;
   if (cudaEventSynchronize(c.ev[1]) != cudaSuccess || !c.cuda_ok("time_operator")) return set_err(h, HEXA_ERR_CUDA, c.err);
+  if (!staging_ok(h, "time_operator")) return HEXA_ERR_CUDA;
   float ms = 0;
   cudaEventElapsedTime(&ms, c.ev[0], c.ev[1]);
   *avg_ms = ms / reps;
@@ -433,6 +443,7 @@ int hexa_solve(hexa_ctx* h, const hexa_grid* g, const hexa_bc* bc, const double*
     c.cuda_ok("solve");
     rc = HEXA_ERR_CUDA;
   }
+  if (!staging_ok(h, "solve")) rc = HEXA_ERR_CUDA;
   st.status = rc;
   st.total_ms = wall_ms(t0);
   c.last_ms = st.setup_ms + st.solve_ms;
@@ -584,6 +595,7 @@ int hexa_solve_multi_rhs(hexa_ctx* h, const hexa_grid* g, const hexa_bc* bc, con
     c.cuda_ok("multi-rhs solve");
     rc = HEXA_ERR_CUDA;
   }
+  if (!staging_ok(h, "multi-rhs solve")) rc = HEXA_ERR_CUDA;
   st.status = rc;
   st.total_ms = wall_ms(t0);
   c.last_ms = st.setup_ms + st.solve_ms;
@@ -919,8 +931,9 @@ int hexa_solve_batch(hexa_ctx* h, int32_t count, const hexa_grid* grids, const h
   Ctx& c = h->c;
   c.err.clear();
   cudaSetDevice(c.device);
-  const int rc = batch_problem(c, count, grids, bcs, nu, factors, forces, *p, u_out, stats);
+  int rc = batch_problem(c, count, grids, bcs, nu, factors, forces, *p, u_out, stats);
   if (rc < 0 && c.err.empty()) c.err = "batch solve failed";
+  if (!staging_ok(h, "batch solve")) rc = HEXA_ERR_CUDA;
   return rc;
 }
 

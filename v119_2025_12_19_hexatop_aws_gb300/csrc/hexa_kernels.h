@@ -39,10 +39,14 @@ struct OpArgs {
   const int* halt;  // nullable: PcgScalars::halt
   int ncol = 1;     // columns (x, b, y advance by ndof per column): OP_APPLY and
                     // OP_RESID only
+  int test_stall = -1;  // FP32 staged form: layer load that CTA 0 leaves out (tests of the bounded waits)
 };
 
 template <typename T>
 void launch_op(int mode, const OpArgs<T>& a, cudaStream_t st);
+// Whether a staged FP32 operator launch gave up a bounded wait since the last
+// call (reads and clears the device word; synchronizes st).
+bool op_take_wait_error(cudaStream_t st);
 template <typename T>
 long long op_num_blocks(const Grid& g, int kchunk);
 // node layers per work item so that every resident CTA gets ~8 items

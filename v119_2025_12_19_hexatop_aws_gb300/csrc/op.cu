@@ -16,6 +16,7 @@
 // Chebyshev step.
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <vector>
 
 #include "hexa_common.cuh"
@@ -535,6 +536,364 @@ __global__ void __launch_bounds__(32 * TYW, op_min_ctas<T>()) op_kernel(const Op
   }
 }
 
+// ------------------------------------------------- TMA-staged FP32 operator
+// The same node-centric product with the new node layer of x staged in shared
+// memory by the TMA engine instead of twelve predicated global loads per
+// thread and layer: for each layer a CTA needs, one lane per node row of the
+// tile issues one bulk copy (cp.async.bulk) of that row's 33 nodes into a
+// ring of NS layer slots, completed on the slot's mbarrier (transaction
+// bytes).  Threads read their four corners with plain shared-memory loads at
+// fixed offsets: no address arithmetic and no bounds tests per corner.
+// Rows and layers outside the grid are not copied; the only elements that
+// read them have factor zero (element column, row or layer outside the grid),
+// so stale slot contents never reach a result (the ring is zeroed at start so
+// that they are finite).  Rows start at any 4-byte offset while bulk copies
+// move whole 16-byte granules: each copy is widened to the granules around
+// the row (never past a granule that holds some of the row, so it stays inside
+// x's allocation) and lands so that the row's first node sits aoff floats into
+// its slot; the producer lane records aoff beside the data.  The ring keeps
+// NS layers in flight across the CTA's whole sequence of work items, so
+// items do not drain the pipeline.  Every wait is bounded (about half a
+// second of clock cycles): a wait that runs out sets the device error word
+// g_op_wait_err, every thread of the CTA leaves at the next barrier, the
+// copies still in flight are waited for (bounded again) and the kernel
+// returns; the host reads the word after the call (op_wait_error).
+namespace tma {
+constexpr int NS = 4;        // layer slots in flight
+constexpr int PITCH = 112;   // floats per staged node row: 33 nodes x 3 + granule slack
+constexpr long long kWaitCycles = 1000000000LL;
+}  // namespace tma
+
+__device__ int g_op_wait_err = 0;
+
+template <int TYW>
+struct OpRing {
+  float v[tma::NS][TYW + 1][tma::PITCH];
+  int aoff[tma::NS][TYW + 1];
+  unsigned long long bar[tma::NS];
+};
+
+__device__ __forceinline__ uint32_t smem_addr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ void mbar_init(unsigned long long* b, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(b)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(unsigned long long* b, uint32_t bytes) {
+  asm volatile("mbarrier.expect_tx.relaxed.cta.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(b)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(unsigned long long* b) {
+  asm volatile("{ .reg .b64 st; mbarrier.arrive.shared::cta.b64 st, [%0]; }" ::"r"(smem_addr(b)) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(unsigned long long* b, uint32_t parity) {
+  uint32_t ok;
+  asm volatile("{ .reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2; selp.u32 %0, 1, 0, p; }"
+               : "=r"(ok)
+               : "r"(smem_addr(b)), "r"(parity)
+               : "memory");
+  return ok != 0;
+}
+// bounded: false when the slot did not fill within tma::kWaitCycles
+__device__ __forceinline__ bool ring_wait(unsigned long long* b, uint32_t parity) {
+  if (mbar_try_wait(b, parity)) return true;
+  const long long t0 = clock64();
+  do {
+    if (mbar_try_wait(b, parity)) return true;
+  } while (clock64() - t0 < tma::kWaitCycles);
+  return false;
+}
+
+// The CTA's sequence of layer loads: item by item (static stride), node
+// layers k0-1 .. k1 of each item's z-chunk.
+struct LoadCursor {
+  int item, kk, k1, tx, ty;
+};
+template <typename A>
+__device__ __forceinline__ void cursor_start(const A& a, int item, LoadCursor& c) {
+  const int nxy = a.tiles_x * a.tiles_y;
+  const int chunk = item / nxy, t = item - chunk * nxy;
+  c.item = item;
+  c.ty = t / a.tiles_x;
+  c.tx = t - c.ty * a.tiles_x;
+  const int k0 = chunk * a.kchunk;
+  c.kk = k0 - 1;
+  c.k1 = min(k0 + a.kchunk, a.g.NZ);
+}
+
+// Lane `lane` of the producer warp copies node row `lane` of layer c.kk into
+// slot q % NS; lane 0 then arrives on the slot's mbarrier.  test_stall: the
+// copy and the arrival of this load are left out (a wait that runs out).
+template <int TYW>
+__device__ __forceinline__ void issue_layer(OpRing<TYW>& R, long long q, const Grid& g, const float* x,
+                                            const LoadCursor& c, int lane, bool test_stall) {
+  const int slot = (int)(q % tma::NS);
+  unsigned long long* bar = &R.bar[slot];
+  if (lane <= TYW && !test_stall) {
+    const int j = c.ty * (TYW - 1) - 1 + lane;
+    const int i0m = c.tx * 31 - 1;
+    const int ifirst = max(i0m, 0), ilast = min(i0m + 32, g.NX - 1);
+    int aoff = 0;
+    if (j >= 0 && j < g.NY && c.kk >= 0 && c.kk < g.NZ) {
+      const long long s = 3LL * ((long long)ifirst + (long long)g.NX * ((long long)j + (long long)g.NY * c.kk));
+      const unsigned long long sb = (unsigned long long)(x + s);
+      const unsigned long long b0 = sb & ~15ull;
+      const unsigned long long b1 = (sb + 12ull * (unsigned long long)(ilast - ifirst + 1) + 15ull) & ~15ull;
+      const int slack = (int)((sb & 15ull) >> 2), delta = ifirst - i0m;
+      aoff = (slack - 3 * delta) & 3;
+      float* dst = &R.v[slot][lane][aoff + 3 * delta - slack];  // 0 or 4 floats in: 16-byte aligned
+      const uint32_t bytes = (uint32_t)(b1 - b0);
+      mbar_expect_tx(bar, bytes);
+      asm volatile(
+          "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+              smem_addr(dst)),
+          "l"(b0), "r"(bytes), "r"(smem_addr(bar))
+          : "memory");
+    }
+    R.aoff[slot][lane] = aoff;
+  }
+  __syncwarp();
+  if (lane == 0 && !test_stall) mbar_arrive(bar);
+}
+
+template <int MODE, int TYW, typename IX>
+__device__ __forceinline__ bool op_item_tma(const OpArgs<float>& a, const LoadCursor& it, OpRing<TYW>& R,
+                                            long long& cq, long long& pq, LoadCursor& pc, int& p_items_left,
+                                            float (&xch)[2][TYW][32][4], double& acc0) {
+  using T = float;
+  constexpr int BM = MODE == OP_JACOBI_DOT ? OP_JACOBI : (MODE == OP_CHEB2_DOT ? OP_CHEB2 : MODE);
+  constexpr bool DOTB = MODE == OP_JACOBI_DOT || MODE == OP_CHEB2_DOT;
+  constexpr int NX_OWN = 31, NY_OWN = TYW - 1;
+  constexpr bool NEED_F = (BM == OP_JACOBI || BM == OP_CHEB2);
+  const Grid& g = a.g;
+  const int lane = threadIdx.x, wy = threadIdx.y;
+  const int i0 = it.tx * NX_OWN, j0 = it.ty * NY_OWN;
+  const int k0 = it.kk + 1, k1 = it.k1;
+  const int ie = i0 - 1 + lane, je = j0 - 1 + wy;
+  const bool colv = (ie >= 0) && (ie < g.nx) && (je >= 0) && (je < g.ny);
+  const IX ecol = colv ? ((IX)ie + (IX)g.nx * je) : (IX)0;
+  const IX eplane = (IX)g.nx * g.ny;
+  const int in = i0 + lane, jn = j0 + wy;
+  const bool own = (lane < NX_OWN) && (wy < NY_OWN) && (in < g.NX) && (jn < g.NY);
+  const T* __restrict__ bv = a.b;
+  T* yv = a.y;  // not restrict: CHEB2 runs in place (xin == y)
+  const T* xinv = a.xin;
+  const T* __restrict__ fac = a.fac;
+  const uint32_t F = a.m.faces;
+  const unsigned colfix =
+      (((F & 1u) && in == 0) || ((F & 2u) && in == g.NX - 1) || ((F & 4u) && jn == 0) || ((F & 8u) && jn == g.NY - 1))
+          ? 7u : 0u;
+  const IX nplane = (IX)g.NX * g.NY;
+  const IX ncol = (IX)in + (IX)g.NX * jn;
+  const bool stall = a.test_stall >= 0 && blockIdx.x == 0;
+  bool bad = false;
+
+  auto facload = [&](int k) -> T { return (colv && k >= 0 && k < g.nz) ? __ldg(fac + ecol + eplane * k) : T(0); };
+  // the four corners of this thread's element column at the next staged layer
+  auto take = [&](T (&v)[4][3]) {
+    const int slot = (int)(cq % tma::NS);
+    if (!ring_wait(&R.bar[slot], (uint32_t)((cq / tma::NS) & 1))) bad = true;
+    const float* r0 = &R.v[slot][wy][R.aoff[slot][wy] + 3 * lane];
+    const float* r1 = &R.v[slot][wy + 1][R.aoff[slot][wy + 1] + 3 * lane];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      v[0][c] = r0[c];
+      v[1][c] = r0[3 + c];
+      v[2][c] = r1[c];
+      v[3][c] = r1[3 + c];
+    }
+    ++cq;
+  };
+  // after a barrier every consumer has read the slots of loads < cq: refill
+  auto produce = [&]() {
+    if (wy != 0) return;
+    while (p_items_left > 0 && pq < cq + tma::NS) {
+      issue_layer<TYW>(R, pq, g, a.x, pc, lane, stall && pq == a.test_stall);
+      ++pq;
+      if (++pc.kk > pc.k1) {
+        if (--p_items_left > 0) cursor_start(a, pc.item + gridDim.x, pc);
+      }
+    }
+  };
+
+  T Lm[4][3], carry[4][3], xown[3];
+  T fprev;
+  {
+    T raw[4][3], Lprev[4][3], lo[4][3];
+    take(raw);
+    xy_forward<T>(raw, Lprev);
+    take(raw);
+#pragma unroll
+    for (int c = 0; c < 3; ++c) xown[c] = raw[3][c];
+    xy_forward<T>(raw, Lm);
+    fprev = facload(k0 - 1);
+    element_modal<T>(a.K, Lprev, Lm, fprev, lo, carry);
+  }
+  constexpr bool NEED_B = BM == OP_RESID || BM == OP_RESID_NORM || BM == OP_JACOBI || BM == OP_CHEB2;
+  constexpr bool NEED_P = BM == OP_CHEB2;
+  T bnext[3] = {T(0), T(0), T(0)}, pnext[3] = {T(0), T(0), T(0)};
+  auto load_bp = [&](int kk) {
+    if (own) {
+      const IX n3 = (IX)3 * (ncol + nplane * (IX)kk);
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        if (NEED_B) bnext[c] = __ldg(bv + n3 + c);
+        if (NEED_P) pnext[c] = xinv ? xinv[n3 + c] : T(0);  // plain load: y may alias xin
+      }
+    }
+  };
+  if (NEED_B || NEED_P) load_bp(k0);
+  T accT = T(0);
+  T fnext = facload(k0);
+  bool aborted = false;
+
+#pragma unroll 2
+  for (int k = k0; k < k1; ++k) {
+    T raw[4][3];
+    take(raw);
+    const T f = fnext;
+    T bk[3], pk3[3];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) bk[c] = bnext[c], pk3[c] = pnext[c];
+    if (k + 1 < k1) {
+      fnext = facload(k + 1);
+      if (NEED_B || NEED_P) load_bp(k + 1);
+    }
+    T Um[4][3];
+    xy_forward<T>(raw, Um);
+    T lo[4][3], hi[4][3];
+    element_modal<T>(a.K, Lm, Um, f, lo, hi);
+    add_carry<T>(lo, carry);
+#pragma unroll
+    for (int m = 0; m < 4; ++m)
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        carry[m][c] = hi[m][c];
+        Lm[m][c] = Um[m][c];
+      }
+    T cv[4][3];
+    xy_inverse<T>(lo, cv);
+    T T1[3], T0[3];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      T1[c] = cv[3][c] + __shfl_down_sync(0xffffffffu, cv[2][c], 1);
+      T0[c] = cv[1][c] + __shfl_down_sync(0xffffffffu, cv[0][c], 1);
+    }
+    T F1 = T(0);
+    if (NEED_F) {
+      const T fcol = fprev + f;
+      F1 = fcol + __shfl_down_sync(0xffffffffu, fcol, 1);
+    }
+    fprev = f;
+    const int buf = k & 1;
+    store4(&xch[buf][wy][lane][0], T0[0], T0[1], T0[2], F1);
+    if (__syncthreads_or(bad ? 1 : 0)) {  // a staging wait ran out somewhere in the CTA
+      aborted = true;
+      break;
+    }
+    produce();
+    if (own) {
+      const IX n = ncol + nplane * (IX)k;
+      unsigned fx = colfix;
+      if (((F & 16u) && k == 0) || ((F & 32u) && k == g.NZ - 1)) fx = 7u;
+      if (a.m.node) fx |= (unsigned)__ldg(a.m.node + n);
+      T nb[4];
+      load4(&xch[buf][wy + 1][lane][0], nb);
+      T Kx[3];
+#pragma unroll
+      for (int c = 0; c < 3; ++c) Kx[c] = T1[c] + nb[c];
+      T dinv[3] = {T(0), T(0), T(0)};
+      if (NEED_F) {
+        const T fsum = F1 + nb[3];
+        if (a.diag_quirk) {
+          const T r = recip(fma(a.K.dd[0], fsum, a.sigma));
+          dinv[0] = dinv[1] = dinv[2] = r;
+        } else {
+#pragma unroll
+          for (int c = 0; c < 3; ++c) dinv[c] = recip(fma(a.K.dd[c], fsum, a.sigma));
+        }
+      }
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        const bool fixd = (fx >> c) & 1u;
+        const T Ax = fma(a.sigma, xown[c], Kx[c]);
+        T out;
+        if (BM == OP_APPLY) {
+          out = fixd ? T(0) : Ax;
+        } else if (BM == OP_APPLY_DOT) {
+          out = fixd ? T(0) : Ax;
+          accT = fma(xown[c], out, accT);
+        } else if (BM == OP_RESID || BM == OP_RESID_NORM) {
+          out = fixd ? T(0) : (bk[c] - Ax);
+          if (BM == OP_RESID_NORM) accT = fma(out, out, accT);
+        } else if (BM == OP_JACOBI) {
+          out = fixd ? T(0) : fma(a.omega * dinv[c], bk[c] - Ax, xown[c]);
+        } else {
+          const T t = fma(a.c1, xown[c] - pk3[c], xown[c]);
+          out = fixd ? T(0) : fma(a.c2 * dinv[c], bk[c] - Ax, t);
+        }
+        if (DOTB) accT = fma(bk[c], out, accT);
+        yv[3 * n + c] = out;
+      }
+    }
+#pragma unroll
+    for (int c = 0; c < 3; ++c) xown[c] = raw[3][c];
+  }
+  acc0 += (double)accT;
+  if (aborted) return false;
+  __syncthreads();  // the next item reuses xch
+  return true;
+}
+
+template <int MODE, int TYW, typename IX>
+__global__ void __launch_bounds__(32 * TYW, 1) op_tma_kernel(const OpArgs<float> a) {
+  if (a.halt && *((volatile const int*)a.halt)) return;
+  __shared__ __align__(16) float xch[2][TYW][32][4];
+  __shared__ __align__(128) OpRing<TYW> R;
+  const int tid = threadIdx.x + 32 * threadIdx.y;
+  {  // finite stale contents, then the barriers
+    float* z = &R.v[0][0][0];
+    for (int e = tid; e < tma::NS * (TYW + 1) * tma::PITCH; e += 32 * TYW) z[e] = 0.f;
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    if (tid == 0) {
+      for (int q = 0; q < tma::NS; ++q) mbar_init(&R.bar[q], 1);
+      asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+  }
+  __syncthreads();
+  const int nxy = a.tiles_x * a.tiles_y;
+  const int items = nxy * a.nchunks;
+  int p_items_left = items > (int)blockIdx.x ? (items - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
+  long long cq = 0, pq = 0;
+  LoadCursor pc;
+  if (p_items_left > 0) cursor_start(a, blockIdx.x, pc);
+  if (threadIdx.y == 0) {  // prime the ring
+    const bool stall = a.test_stall >= 0 && blockIdx.x == 0;
+    while (p_items_left > 0 && pq < tma::NS) {
+      issue_layer<TYW>(R, pq, a.g, a.x, pc, threadIdx.x, stall && pq == a.test_stall);
+      ++pq;
+      if (++pc.kk > pc.k1) {
+        if (--p_items_left > 0) cursor_start(a, pc.item + gridDim.x, pc);
+      }
+    }
+  }
+  double acc0 = 0.0;
+  bool ok = true;
+  for (int item = blockIdx.x; item < items && ok; item += gridDim.x) {
+    LoadCursor it;
+    cursor_start(a, item, it);
+    ok = op_item_tma<MODE, TYW, IX>(a, it, R, cq, pq, pc, p_items_left, xch, acc0);
+  }
+  if (!ok) {  // bounded drain of the copies still in flight, then report
+    if (tid == 0) {
+      for (long long q = cq > 0 ? cq - 1 : 0; q < pq; ++q) ring_wait(&R.bar[q % tma::NS], (uint32_t)((q / tma::NS) & 1));
+      atomicExch(&g_op_wait_err, 1);
+    }
+    __syncthreads();
+  }
+  if (MODE == OP_APPLY_DOT || MODE == OP_RESID_NORM || MODE == OP_JACOBI_DOT || MODE == OP_CHEB2_DOT) {
+    double v[1] = {acc0};
+    block_reduce_finalize<1>(a.red, v);
+  }
+}
+
 template <typename T>
 static ModalK<T> cast_modal(const ModalK<double>& K) {
   ModalK<T> o;
@@ -599,6 +958,73 @@ int op_pick_kchunk(const Grid& g) {
   return (int)((g.NZ + chunks - 1) / chunks);
 }
 
+static int env_int(const char* name, int dflt) {
+  const char* v = std::getenv(name);
+  return (v && *v) ? std::atoi(v) : dflt;
+}
+
+// FP32 single-column launches use the TMA-staged kernel; HEXA_OP_TMA=0 selects
+// the kernel with per-thread global loads (A/B timing), HEXA_OP_TEST_STALL=q
+// makes CTA 0 leave out its layer load q (tests of the bounded waits).
+static bool op_use_tma() {
+  static const bool on = env_int("HEXA_OP_TMA", 1) != 0;
+  return on;
+}
+
+static int tma_resident_ctas() {
+  static int cached = 0;
+  if (!cached) {
+    int dev = 0, sms = 0, occ = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, op_tma_kernel<OP_CHEB2, HEXA_OP_TYW32, int>, 32 * HEXA_OP_TYW32,
+                                                  0);
+    cached = std::max(1, sms) * std::max(1, occ);
+  }
+  return cached;
+}
+
+bool op_take_wait_error(cudaStream_t st) {
+  int h = 0;
+  if (cudaMemcpyFromSymbolAsync(&h, g_op_wait_err, sizeof(int), 0, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+      cudaStreamSynchronize(st) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  if (h) {
+    static const int zero = 0;
+    cudaMemcpyToSymbolAsync(g_op_wait_err, &zero, sizeof(int), 0, cudaMemcpyHostToDevice, st);
+    cudaStreamSynchronize(st);
+  }
+  return h != 0;
+}
+
+static void launch_op_tma(int mode, OpArgs<float>& a, bool i32, cudaStream_t st) {
+  constexpr int TYW = HEXA_OP_TYW32;
+  static const int stall = env_int("HEXA_OP_TEST_STALL", -1);
+  a.test_stall = stall;
+  const long long items = (long long)a.tiles_x * a.tiles_y * a.nchunks;
+  const int grid = (int)std::min<long long>(items, tma_resident_ctas());
+  const dim3 block(32, TYW);
+#define HEXA_OPT_CASE(M)                                                          \
+  case M:                                                                        \
+    if (i32) op_tma_kernel<M, TYW, int><<<grid, block, 0, st>>>(a);              \
+    else op_tma_kernel<M, TYW, long long><<<grid, block, 0, st>>>(a);            \
+    break;
+  switch (mode) {
+    HEXA_OPT_CASE(OP_APPLY)
+    HEXA_OPT_CASE(OP_APPLY_DOT)
+    HEXA_OPT_CASE(OP_RESID)
+    HEXA_OPT_CASE(OP_RESID_NORM)
+    HEXA_OPT_CASE(OP_JACOBI)
+    HEXA_OPT_CASE(OP_CHEB2)
+    HEXA_OPT_CASE(OP_JACOBI_DOT)
+    HEXA_OPT_CASE(OP_CHEB2_DOT)
+    default: break;
+  }
+#undef HEXA_OPT_CASE
+}
+
 template <typename T>
 void launch_op(int mode, const OpArgs<T>& a0, cudaStream_t st) {
   constexpr int TYW = op_tyw<T>();
@@ -608,6 +1034,12 @@ void launch_op(int mode, const OpArgs<T>& a0, cudaStream_t st) {
   const int grid = (int)std::min<long long>(items, resident_ctas<T>(mode));
   const dim3 block(32, TYW);
   const bool i32 = a.g.ndof() < (1LL << 30) && a.g.nelem() < (1LL << 30);
+  if constexpr (sizeof(T) == 4) {
+    if (a.ncol <= 1 && op_use_tma()) {
+      launch_op_tma(mode, a, i32, st);
+      return;
+    }
+  }
   if (a.ncol > 1) {  // multi-column forms: the plain apply and the residual
     if (mode == OP_APPLY) {
       if (i32) op_kernel<T, OP_APPLY, TYW, int, true><<<grid, block, 0, st>>>(a);

@@ -269,10 +269,12 @@ bool build_mg(Ctx& c, MG<T>& mg, const Grid& g0, const Mask& m0, const T* fac0, 
   return Lc.dinv && Lc.p && Lc.q && Lc.z && Lc.xa;
 }
 
-// Coarsest grids of at most this many DOFs are solved exactly by one dense
-// matvec with the inverse of (K + sigma I) on their free DOFs (Cholesky and
-// inverse in FP64 on the host at setup, about n^3 flops, well under 0.1 s at
-// the limit); larger ones by the coarse PCG.
+// Coarsest grids of at most this many free DOFs are solved exactly by one
+// dense matvec with the inverse of (K + sigma I) on their free DOFs (Cholesky
+// and inverse in FP64 on the host at setup, about n^3 flops, well under 0.1 s
+// at the limit); larger ones by the coarse PCG.  The count is of free DOFs:
+// the 8x4x4 coarsest grid of a 256x128x128 hierarchy has 675 DOFs, 600 of
+// them free once its x = 0 face is clamped.
 constexpr long long kDenseCoarse = 640;
 
 template <typename T>
@@ -280,7 +282,7 @@ void coarse_dense_setup(Ctx& c, MG<T>& mg, double sigma_c) {
   Lev<T>& V = mg.L.back();
   V.ainv = nullptr;
   const long long n = V.g.ndof();
-  if (n > kDenseCoarse || mg.ke.size() != 576) return;
+  if (n > 4 * kDenseCoarse || mg.ke.size() != 576) return;
   const Grid& g = V.g;
   std::vector<T> fac(g.nelem());
   std::vector<uint8_t> mask;
@@ -308,7 +310,7 @@ void coarse_dense_setup(Ctx& c, MG<T>& mg, double sigma_c) {
         for (int cc = 0; cc < 3; ++cc)
           if (!((fx >> cc) & 1u)) fidx[3 * nd + cc] = nf++;
       }
-  if (nf == 0) return;
+  if (nf == 0 || nf > kDenseCoarse) return;
   std::vector<double> A((size_t)nf * nf, 0.0);
   for (int q = 0; q < nf; ++q) A[(size_t)q * nf + q] = sigma_c;
   static const int ref_to_corner[8] = {0, 1, 3, 2, 4, 5, 7, 6};  // K0 node order (Mesh.jl:45-53) -> dx + 2dy + 4dz
