@@ -9,8 +9,6 @@
 // atomics), prolongation is fused with the correction add, coarse operators
 // are rediscretised (K0 at 2h = 2 K0(h), factor = mean of the 8 children),
 // and the first damped-Jacobi sweep from a zero guess is a pointwise pass.
-#include <cstdlib>
-
 #include "hexa_common.cuh"
 #include "hexa_kernels.h"
 
@@ -24,36 +22,27 @@ static inline int mg_blocks(long long n, int threads = 256) {
 }
 
 template <typename T>
-__global__ void coarsen_factors_kernel(Grid gf, const T* __restrict__ ff, Grid gc, T* __restrict__ fc, int rule) {
+__global__ void coarsen_factors_kernel(Grid gf, const T* __restrict__ ff, Grid gc, T* __restrict__ fc) {
   const long long ne = gc.nelem();
   for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < ne;
        e += (long long)gridDim.x * blockDim.x) {
     const int I = (int)(e % gc.nx);
     const long long t = e / gc.nx;
     const int J = (int)(t % gc.ny), K = (int)(t / gc.ny);
-    double s = 0.0;
+    T s = T(0);
 #pragma unroll
     for (int c = 0; c < 2; ++c)
 #pragma unroll
       for (int b = 0; b < 2; ++b)
 #pragma unroll
-        for (int a = 0; a < 2; ++a) {
-          const double f =
-              (double)ff[(long long)(2 * I + a) + (long long)gf.nx * ((long long)(2 * J + b) + (long long)gf.ny * (2 * K + c))];
-          s += rule == 1 ? log(f) : (rule == 2 ? cbrt(f) : (rule == 3 ? 1.0 / f : f));
-        }
-    s *= 0.125;
-    const double m = rule == 1 ? exp(s) : (rule == 2 ? s * s * s : (rule == 3 ? 1.0 / s : s));
-    fc[e] = (T)(2.0 * m);  // K0(2h) = 2 K0(h)
+        for (int a = 0; a < 2; ++a)
+          s += ff[(long long)(2 * I + a) + (long long)gf.nx * ((long long)(2 * J + b) + (long long)gf.ny * (2 * K + c))];
+    fc[e] = T(0.25) * s;  // 2 * (sum / 8)
   }
 }
 template <typename T>
 void launch_coarsen_factors(const Grid& gf, const T* ff, const Grid& gc, T* fc, cudaStream_t st) {
-  static const int rule = [] {
-    const char* v = std::getenv("HEXA_MG_COARSEN");
-    return v ? std::atoi(v) : 0;
-  }();
-  coarsen_factors_kernel<T><<<mg_blocks(gc.nelem()), 256, 0, st>>>(gf, ff, gc, fc, rule);
+  coarsen_factors_kernel<T><<<mg_blocks(gc.nelem()), 256, 0, st>>>(gf, ff, gc, fc);
 }
 
 __global__ void coarsen_mask_kernel(Grid gf, const uint8_t* __restrict__ mf, Grid gc, uint8_t* __restrict__ mc) {

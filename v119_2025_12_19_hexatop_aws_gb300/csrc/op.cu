@@ -539,10 +539,12 @@ __global__ void __launch_bounds__(32 * TYW, op_min_ctas<T>()) op_kernel(const Op
 // ------------------------------------------------- TMA-staged FP32 operator
 // The same node-centric product with the new node layer of x staged in shared
 // memory by the TMA engine instead of twelve predicated global loads per
-// thread and layer: for each layer a CTA needs, one lane per node row of the
-// tile issues one bulk copy (cp.async.bulk) of that row's 33 nodes into a
-// ring of NS layer slots, completed on the slot's mbarrier (transaction
-// bytes).  Threads read their four corners with plain shared-memory loads at
+// thread and layer: for each layer a CTA needs, one thread per node row of
+// the tile (lane 0 of warp r for row r, lane 1 of warp 0 for the last row, so
+// that no warp carries the issue work of the others into the per-layer
+// barrier) issues one bulk copy (cp.async.bulk) of that row's 33 nodes into a
+// ring of NS layer slots and arrives on the slot's mbarrier with the copy's
+// transaction bytes.  Threads read their four corners with plain shared-memory loads at
 // fixed offsets: no address arithmetic and no bounds tests per corner.
 // Rows and layers outside the grid are not copied; the only elements that
 // read them have factor zero (element column, row or layer outside the grid),
@@ -579,6 +581,11 @@ __device__ __forceinline__ void mbar_init(unsigned long long* b, uint32_t count)
 }
 __device__ __forceinline__ void mbar_expect_tx(unsigned long long* b, uint32_t bytes) {
   asm volatile("mbarrier.expect_tx.relaxed.cta.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(b)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive_expect_tx(unsigned long long* b, uint32_t bytes) {
+  asm volatile("{ .reg .b64 st; mbarrier.arrive.expect_tx.shared::cta.b64 st, [%0], %1; }" ::"r"(smem_addr(b)),
+               "r"(bytes)
+               : "memory");
 }
 __device__ __forceinline__ void mbar_arrive(unsigned long long* b) {
   asm volatile("{ .reg .b64 st; mbarrier.arrive.shared::cta.b64 st, [%0]; }" ::"r"(smem_addr(b)) : "memory");
@@ -618,45 +625,67 @@ __device__ __forceinline__ void cursor_start(const A& a, int item, LoadCursor& c
   c.k1 = min(k0 + a.kchunk, a.g.NZ);
 }
 
-// Lane `lane` of the producer warp copies node row `lane` of layer c.kk into
-// slot q % NS; lane 0 then arrives on the slot's mbarrier.  test_stall: the
-// copy and the arrival of this load are left out (a wait that runs out).
+// Node row `row` of layer c.kk into slot q % NS, by the row's issuing thread:
+// it arrives on the slot's mbarrier with the copy's bytes (a row outside the
+// grid: a plain arrival).  test_stall: the load is left out, no arrival (a
+// wait that runs out).
 template <int TYW>
-__device__ __forceinline__ void issue_layer(OpRing<TYW>& R, long long q, const Grid& g, const float* x,
-                                            const LoadCursor& c, int lane, bool test_stall) {
-  const int slot = (int)(q % tma::NS);
+__device__ __forceinline__ void issue_row(OpRing<TYW>& R, int q, const Grid& g, const float* x, const LoadCursor& c,
+                                          int row, bool test_stall) {
+  if (test_stall) return;
+  const int slot = q % tma::NS;
   unsigned long long* bar = &R.bar[slot];
-  if (lane <= TYW && !test_stall) {
-    const int j = c.ty * (TYW - 1) - 1 + lane;
-    const int i0m = c.tx * 31 - 1;
-    const int ifirst = max(i0m, 0), ilast = min(i0m + 32, g.NX - 1);
-    int aoff = 0;
-    if (j >= 0 && j < g.NY && c.kk >= 0 && c.kk < g.NZ) {
-      const long long s = 3LL * ((long long)ifirst + (long long)g.NX * ((long long)j + (long long)g.NY * c.kk));
-      const unsigned long long sb = (unsigned long long)(x + s);
-      const unsigned long long b0 = sb & ~15ull;
-      const unsigned long long b1 = (sb + 12ull * (unsigned long long)(ilast - ifirst + 1) + 15ull) & ~15ull;
-      const int slack = (int)((sb & 15ull) >> 2), delta = ifirst - i0m;
-      aoff = (slack - 3 * delta) & 3;
-      float* dst = &R.v[slot][lane][aoff + 3 * delta - slack];  // 0 or 4 floats in: 16-byte aligned
-      const uint32_t bytes = (uint32_t)(b1 - b0);
-      mbar_expect_tx(bar, bytes);
-      asm volatile(
-          "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-              smem_addr(dst)),
-          "l"(b0), "r"(bytes), "r"(smem_addr(bar))
-          : "memory");
-    }
-    R.aoff[slot][lane] = aoff;
+  const int j = c.ty * (TYW - 1) - 1 + row;
+  const int i0m = c.tx * 31 - 1;
+  const int ifirst = max(i0m, 0), ilast = min(i0m + 32, g.NX - 1);
+  if (j >= 0 && j < g.NY && c.kk >= 0 && c.kk < g.NZ) {
+    const long long s = 3LL * ((long long)ifirst + (long long)g.NX * ((long long)j + (long long)g.NY * c.kk));
+    const unsigned long long sb = (unsigned long long)(x + s);
+    const unsigned long long b0 = sb & ~15ull;
+    const unsigned long long b1 = (sb + 12ull * (unsigned long long)(ilast - ifirst + 1) + 15ull) & ~15ull;
+    const int slack = (int)((sb & 15ull) >> 2), delta = ifirst - i0m;
+    const int aoff = (slack - 3 * delta) & 3;
+    float* dst = &R.v[slot][row][aoff + 3 * delta - slack];  // 0 or 4 floats in: 16-byte aligned
+    const uint32_t bytes = (uint32_t)(b1 - b0);
+    R.aoff[slot][row] = aoff;
+    mbar_arrive_expect_tx(bar, bytes);
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(smem_addr(dst)),
+        "l"(b0), "r"(bytes), "r"(smem_addr(bar))
+        : "memory");
+  } else {
+    R.aoff[slot][row] = 0;
+    mbar_arrive(bar);
   }
-  __syncwarp();
-  if (lane == 0 && !test_stall) mbar_arrive(bar);
+}
+
+// The issuing thread of each row: lane 0 of warp r for rows 0..TYW-1, lane 1
+// of warp 0 for row TYW; -1 for every other thread.
+template <int TYW>
+__device__ __forceinline__ int my_row() {
+  return threadIdx.x == 0 ? (int)threadIdx.y : ((threadIdx.x == 1 && threadIdx.y == 0) ? TYW : -1);
+}
+
+// Issue loads while fewer than NS are outstanding; every thread walks the
+// cursor (uniform integer work), the row owners issue.
+template <int TYW, typename A>
+__device__ __forceinline__ void produce_loads(const A& a, OpRing<TYW>& R, int cq, int& pq, LoadCursor& pc,
+                                              int& p_items_left) {
+  const int row = my_row<TYW>();
+  const bool stall_cta = a.test_stall >= 0 && blockIdx.x == 0;
+  while (p_items_left > 0 && pq < cq + tma::NS) {
+    if (row >= 0) issue_row<TYW>(R, pq, a.g, a.x, pc, row, stall_cta && pq == a.test_stall);
+    ++pq;
+    if (++pc.kk > pc.k1) {
+      if (--p_items_left > 0) cursor_start(a, pc.item + gridDim.x, pc);
+    }
+  }
 }
 
 template <int MODE, int TYW, typename IX>
-__device__ __forceinline__ bool op_item_tma(const OpArgs<float>& a, const LoadCursor& it, OpRing<TYW>& R,
-                                            long long& cq, long long& pq, LoadCursor& pc, int& p_items_left,
-                                            float (&xch)[2][TYW][32][4], double& acc0) {
+__device__ __forceinline__ bool op_item_tma(const OpArgs<float>& a, const LoadCursor& it, OpRing<TYW>& R, int& cq,
+                                            int& pq, LoadCursor& pc, int& p_items_left, float (&xch)[2][TYW][32][4],
+                                            double& acc0) {
   using T = float;
   constexpr int BM = MODE == OP_JACOBI_DOT ? OP_JACOBI : (MODE == OP_CHEB2_DOT ? OP_CHEB2 : MODE);
   constexpr bool DOTB = MODE == OP_JACOBI_DOT || MODE == OP_CHEB2_DOT;
@@ -682,13 +711,12 @@ __device__ __forceinline__ bool op_item_tma(const OpArgs<float>& a, const LoadCu
           ? 7u : 0u;
   const IX nplane = (IX)g.NX * g.NY;
   const IX ncol = (IX)in + (IX)g.NX * jn;
-  const bool stall = a.test_stall >= 0 && blockIdx.x == 0;
   bool bad = false;
 
   auto facload = [&](int k) -> T { return (colv && k >= 0 && k < g.nz) ? __ldg(fac + ecol + eplane * k) : T(0); };
   // the four corners of this thread's element column at the next staged layer
   auto take = [&](T (&v)[4][3]) {
-    const int slot = (int)(cq % tma::NS);
+    const int slot = cq % tma::NS;
     if (!ring_wait(&R.bar[slot], (uint32_t)((cq / tma::NS) & 1))) bad = true;
     const float* r0 = &R.v[slot][wy][R.aoff[slot][wy] + 3 * lane];
     const float* r1 = &R.v[slot][wy + 1][R.aoff[slot][wy + 1] + 3 * lane];
@@ -700,17 +728,6 @@ __device__ __forceinline__ bool op_item_tma(const OpArgs<float>& a, const LoadCu
       v[3][c] = r1[3 + c];
     }
     ++cq;
-  };
-  // after a barrier every consumer has read the slots of loads < cq: refill
-  auto produce = [&]() {
-    if (wy != 0) return;
-    while (p_items_left > 0 && pq < cq + tma::NS) {
-      issue_layer<TYW>(R, pq, g, a.x, pc, lane, stall && pq == a.test_stall);
-      ++pq;
-      if (++pc.kk > pc.k1) {
-        if (--p_items_left > 0) cursor_start(a, pc.item + gridDim.x, pc);
-      }
-    }
   };
 
   T Lm[4][3], carry[4][3], xown[3];
@@ -788,7 +805,7 @@ __device__ __forceinline__ bool op_item_tma(const OpArgs<float>& a, const LoadCu
       aborted = true;
       break;
     }
-    produce();
+    produce_loads<TYW>(a, R, cq, pq, pc, p_items_left);  // every consumer has read the loads < cq
     if (own) {
       const IX n = ncol + nplane * (IX)k;
       unsigned fx = colfix;
@@ -853,7 +870,7 @@ __global__ void __launch_bounds__(32 * TYW, 1) op_tma_kernel(const OpArgs<float>
     for (int e = tid; e < tma::NS * (TYW + 1) * tma::PITCH; e += 32 * TYW) z[e] = 0.f;
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     if (tid == 0) {
-      for (int q = 0; q < tma::NS; ++q) mbar_init(&R.bar[q], 1);
+      for (int q = 0; q < tma::NS; ++q) mbar_init(&R.bar[q], TYW + 1);  // one arrival per node row
       asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
   }
@@ -861,19 +878,10 @@ __global__ void __launch_bounds__(32 * TYW, 1) op_tma_kernel(const OpArgs<float>
   const int nxy = a.tiles_x * a.tiles_y;
   const int items = nxy * a.nchunks;
   int p_items_left = items > (int)blockIdx.x ? (items - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
-  long long cq = 0, pq = 0;
+  int cq = 0, pq = 0;
   LoadCursor pc;
   if (p_items_left > 0) cursor_start(a, blockIdx.x, pc);
-  if (threadIdx.y == 0) {  // prime the ring
-    const bool stall = a.test_stall >= 0 && blockIdx.x == 0;
-    while (p_items_left > 0 && pq < tma::NS) {
-      issue_layer<TYW>(R, pq, a.g, a.x, pc, threadIdx.x, stall && pq == a.test_stall);
-      ++pq;
-      if (++pc.kk > pc.k1) {
-        if (--p_items_left > 0) cursor_start(a, pc.item + gridDim.x, pc);
-      }
-    }
-  }
+  produce_loads<TYW>(a, R, cq, pq, pc, p_items_left);  // prime the ring
   double acc0 = 0.0;
   bool ok = true;
   for (int item = blockIdx.x; item < items && ok; item += gridDim.x) {
@@ -883,7 +891,7 @@ __global__ void __launch_bounds__(32 * TYW, 1) op_tma_kernel(const OpArgs<float>
   }
   if (!ok) {  // bounded drain of the copies still in flight, then report
     if (tid == 0) {
-      for (long long q = cq > 0 ? cq - 1 : 0; q < pq; ++q) ring_wait(&R.bar[q % tma::NS], (uint32_t)((q / tma::NS) & 1));
+      for (int q = cq > 0 ? cq - 1 : 0; q < pq; ++q) ring_wait(&R.bar[q % tma::NS], (uint32_t)((q / tma::NS) & 1));
       atomicExch(&g_op_wait_err, 1);
     }
     __syncthreads();
