@@ -813,7 +813,11 @@ def run_c4(a):
                       "separate_mixed_solves_s": round(tc, 4), "separate_iterations": [q["iterations"] for q in sc],
                       "compliance_sum_block": sb["compliance"],
                       "compliance_sum_separate": sum(q["compliance"] for q in sc),
-                      "block_over_separate": round(tb / tc, 4)}))
+                      "block_over_separate": round(tb / tc, 4),
+                      "ms_per_block_iteration": round(1e3 * tb / max(1, sb["iterations"]), 4),
+                      "ms_per_single_rhs_iteration": round(1e3 * tc / max(1, sum(q["iterations"] for q in sc)), 4),
+                      "block_iteration_over_single": round((tb / max(1, sb["iterations"])) /
+                                                           (tc / max(1, sum(q["iterations"] for q in sc))), 3)}))
     ctx.close()
 
 

@@ -132,8 +132,8 @@ def test_timed_chebyshev_step_reads_its_previous_iterate(ctx, oracle, rng, dims)
 
 
 def test_staged_operator_wait_that_runs_out_is_reported():
-    """Every wait of the TMA-staged FP32 operator is bounded.  With
-    HEXA_OP_TEST_STALL=q, CTA 0 leaves out its layer load q, so its threads'
+    """Every wait of the TMA-staged FP32 operator (HEXA_OP_FORM=1) is bounded.
+    With HEXA_OP_TEST_STALL=q, CTA 0 leaves out its layer load q, so its threads'
     wait for that layer runs out (about half a second of clock cycles): the
     kernel sets its error word, drains its other copies and returns, and the
     call reports HEXA_ERR_CUDA with the reason.  The context stays usable: an
@@ -166,7 +166,7 @@ gg = ref.Grid(40, 20, 20)
 y_ref = ref.apply_A(gg, ref.canonical_stiffness(1, 1, 1, 0.3), fac, x, ref.fixed_mask(gg, 1))
 print("FP64_ERR", float(np.abs(y - y_ref).max() / np.abs(y_ref).max()))
 """
-    env = dict(os.environ, HEXA_OP_TEST_STALL="5")
+    env = dict(os.environ, HEXA_OP_TEST_STALL="5", HEXA_OP_FORM="1")  # the TMA-staged form
     r = subprocess.run([sys.executable, "-c", script], env=env, capture_output=True, text=True, timeout=300)
     assert r.returncode == 0, r.stderr[-2000:]
     assert "ERR -2" in r.stdout and "bounded wait ran out" in r.stdout, r.stdout
