@@ -172,3 +172,52 @@ print("FP64_ERR", float(np.abs(y - y_ref).max() / np.abs(y_ref).max()))
     assert "ERR -2" in r.stdout and "bounded wait ran out" in r.stdout, r.stdout
     err = float(r.stdout.split("FP64_ERR")[1].split()[0])
     assert err < 1e-13
+
+
+def test_staged_operator_form_matches_oracle():
+    """The TMA-staged FP32 form (HEXA_OP_FORM=1, an alternative to the default
+    one-row form) against the oracle on grids with boundary and interior
+    tiles, every operator mode it serves through the solver included (a
+    multigrid solve).  Child process: the form is read once per process."""
+    import os
+    import subprocess
+    import sys
+    from pathlib import Path
+    root = str(Path(__file__).resolve().parents[1])
+    script = f"""
+import sys
+sys.path.insert(0, {root!r})
+import numpy as np
+from oracle import reference as ref
+from v119_2025_12_19_hexatop_aws_gb300 import _lib, workloads
+from v119_2025_12_19_hexatop_aws_gb300.solver import apply_operator, solve
+ctx = _lib.Context(0)
+rng = np.random.default_rng(3)
+worst = 0.0
+for dims in [(5, 3, 7), (33, 17, 9), (62, 15, 20), (64, 32, 12)]:
+    g = ref.Grid(*dims)
+    fac = rng.uniform(1e-3, 1.0, g.nelem).astype(np.float32)
+    x = rng.standard_normal(g.ndof).astype(np.float32)
+    fixed = ref.fixed_mask(g, 1)
+    y_ref = ref.apply_A(g, ref.canonical_stiffness(1, 1, 1, 0.3), fac.astype(np.float64), x.astype(np.float64), fixed)
+    y = apply_operator(_lib.make_grid(*dims), fac, x, clamp_faces=1, ctx=ctx, fp32=True)
+    worst = max(worst, float(np.abs(y - y_ref).max() / np.abs(y_ref).max()))
+print("OP_ERR", worst)
+dims = (16, 8, 8)
+g = ref.Grid(*dims)
+fac = rng.uniform(0.1, 1.0, g.nelem)
+f = workloads.edge_load(*dims)
+fixed = ref.fixed_mask(g, 1)
+K0 = ref.canonical_stiffness(1, 1, 1, 0.3)
+u_ref = ref.direct_solve(g, K0, fac, f, fixed, 0.0)
+u, st = solve(_lib.make_grid(*dims), fac, f, clamp_faces=1, ctx=ctx,
+              params=_lib.default_params(precision="mixed", tol=1e-12, max_iter=20000, mg_levels=3, shift_factor=0.0))
+print("SOLVE_ERR", float(np.linalg.norm(u - u_ref) / np.linalg.norm(u_ref)), st["status"])
+"""
+    env = dict(os.environ, HEXA_OP_FORM="1")
+    r = subprocess.run([sys.executable, "-c", script], env=env, capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr[-2000:]
+    op_err = float(r.stdout.split("OP_ERR")[1].split()[0])
+    solve_err, status = r.stdout.split("SOLVE_ERR")[1].split()[:2]
+    assert op_err <= 2e-6
+    assert float(solve_err) <= 1e-9 and int(status) == 0

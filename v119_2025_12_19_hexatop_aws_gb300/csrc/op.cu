@@ -40,12 +40,16 @@ __device__ __forceinline__ T ldx(const T* p) { return __ldg(p); }
 
 // Addressing of one element column's four corner nodes (cc = dx + 2*dy):
 // x/y validity is fixed per thread, each node layer adds one plane offset.
+// A corner outside the grid is read at the nearest grid node (clamped index):
+// every element that has such a corner lies outside the grid and has factor
+// zero, so the (finite) value read never reaches a result, and the loads need
+// no per-corner bounds test.
 template <typename IX>
 struct ColumnAddr {
   IX base;   // 3 * node index of corner 0 at layer 0
   IX row3;   // 3 * NX: corner 2 is one node row up
   IX plane3; // 3 * NX * NY
-  bool ok[4];
+  IX off[4]; // 3 * (clamped) node index of each corner within a layer
 };
 
 template <typename IX>
@@ -56,15 +60,15 @@ __device__ __forceinline__ ColumnAddr<IX> column_addr(const Grid& g, int ie, int
   a.plane3 = (IX)3 * g.NX * g.NY;
 #pragma unroll
   for (int cc = 0; cc < 4; ++cc) {
-    const int i = ie + (cc & 1), j = je + (cc >> 1);
-    a.ok[cc] = (i >= 0) && (i < g.NX) && (j >= 0) && (j < g.NY);
+    const int i = min(max(ie + (cc & 1), 0), g.NX - 1), j = min(max(je + (cc >> 1), 0), g.NY - 1);
+    a.off[cc] = (IX)3 * ((IX)i + (IX)g.NX * j);
   }
   return a;
 }
 
-// Corner values of the column at node layer kk; zeros outside the grid.
-// INTERIOR: every corner of every column of the tile lies inside the grid in
-// x and y, so only the (CTA-uniform) layer test remains.
+// Corner values of the column at node layer kk, read at clamped positions
+// (see ColumnAddr).  INTERIOR: every corner of every column of the tile lies
+// inside the grid in x and y; layers outside the grid read as zeros.
 template <typename T, typename IX, bool INTERIOR = false>
 __device__ __forceinline__ void load_corners(const Grid& g, const ColumnAddr<IX>& ca, const T* __restrict__ x, int kk,
                                              T (&v)[4][3]) {
@@ -89,12 +93,12 @@ __device__ __forceinline__ void load_corners(const Grid& g, const ColumnAddr<IX>
     }
     return;
   }
+  const IX L = ca.plane3 * (IX)min(max(kk, 0), g.NZ - 1);
 #pragma unroll
   for (int cc = 0; cc < 4; ++cc) {
-    const bool ok = kok && ca.ok[cc];
-    const IX o = lb + ((cc & 1) ? 3 : 0) + ((cc >> 1) ? ca.row3 : (IX)0);
+    const T* __restrict__ p = x + (L + ca.off[cc]);
 #pragma unroll
-    for (int c = 0; c < 3; ++c) v[cc][c] = ok ? ldx(x + o + c) : T(0);
+    for (int c = 0; c < 3; ++c) v[cc][c] = ldx(p + c);
   }
 }
 
@@ -902,310 +906,6 @@ __global__ void __launch_bounds__(32 * TYW, 1) op_tma_kernel(const OpArgs<float>
   }
 }
 
-// ------------------------------------------------ two-row packed FP32 operator
-// The same node-centric product with each thread computing two element rows
-// of its element column (rows je and je+1), every arithmetic step of the two
-// elements issued as one packed FP32x2 instruction (FADD2/FFMA2/FMUL2: the
-// element pair in the two halves, the modal coefficient of K0 in both halves
-// of a constant-bank pair).  Per element this halves the arithmetic
-// instructions of the one-row form (there the (x, y) components are packed
-// and z is scalar), and the two elements share their middle node row: 18
-// corner values per thread and layer instead of 24.  A CTA is 8 warps (256
-// threads, up to 255 registers each) owning the same 31 x 15 node columns as
-// the one-row form.  Corner and factor loads use clamped indices, so they
-// need no per-load predicates: an element outside the grid reads some grid
-// node's (finite) values and has factor zero, which makes its contribution
-// exactly zero.
-namespace op2 {
-constexpr int TW = 8;  // warps per CTA
-}
-
-struct Op2Args {
-  OpArgs<float> a;
-  float2 B2[8][3][3];  // ModalK<float>::B with each coefficient in both halves
-};
-
-__device__ __forceinline__ float2 f2add(float2 a, float2 b) { return __fadd2_rn(a, b); }
-__device__ __forceinline__ float2 f2sub(float2 a, float2 b) { return __ffma2_rn(b, make_float2(-1.f, -1.f), a); }
-__device__ __forceinline__ float2 f2mul(float2 a, float2 b) { return __fmul2_rn(a, b); }
-__device__ __forceinline__ float2 f2fma(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
-__device__ __forceinline__ float2 f2shfl_down(float2 v) {
-  return make_float2(__shfl_down_sync(0xffffffffu, v.x, 1), __shfl_down_sync(0xffffffffu, v.y, 1));
-}
-
-// rows (r0, r1, r2) x nodes (0, 1) x components -> xy modes of the element
-// pair (A: rows r0-r1, B: rows r1-r2), modes indexed dx + 2 dy as xy_forward
-__device__ __forceinline__ void xy_forward2(const float (&v)[3][2][3], float2 (&m)[4][3]) {
-#pragma unroll
-  for (int c = 0; c < 3; ++c) {
-    const float2 lo0 = make_float2(v[0][0][c], v[1][0][c]), lo1 = make_float2(v[0][1][c], v[1][1][c]);
-    const float2 hi0 = make_float2(v[1][0][c], v[2][0][c]), hi1 = make_float2(v[1][1][c], v[2][1][c]);
-    const float2 a0 = f2add(lo0, lo1), a1 = f2sub(lo1, lo0), b0 = f2add(hi0, hi1), b1 = f2sub(hi1, hi0);
-    m[0][c] = f2add(a0, b0);
-    m[1][c] = f2add(a1, b1);
-    m[2][c] = f2sub(b0, a0);
-    m[3][c] = f2sub(b1, a1);
-  }
-}
-
-__device__ __forceinline__ void xy_inverse2(const float2 (&m)[4][3], float2 (&v)[4][3]) {
-#pragma unroll
-  for (int c = 0; c < 3; ++c) {
-    const float2 A0 = f2sub(m[0][c], m[2][c]), B0 = f2add(m[0][c], m[2][c]);
-    const float2 A1 = f2sub(m[1][c], m[3][c]), B1 = f2add(m[1][c], m[3][c]);
-    v[0][c] = f2sub(A0, A1);
-    v[1][c] = f2add(A0, A1);
-    v[2][c] = f2sub(B0, B1);
-    v[3][c] = f2add(B0, B1);
-  }
-}
-
-__device__ __forceinline__ void element_modal2(const float2 (&B2)[8][3][3], const float2 (&L)[4][3],
-                                               const float2 (&U)[4][3], float2 f, float2 (&lo)[4][3],
-                                               float2 (&hi)[4][3]) {
-  const float2 nf = make_float2(-f.x, -f.y);
-  float2 uh[8][3];
-#pragma unroll
-  for (int mxy = 0; mxy < 4; ++mxy)
-#pragma unroll
-    for (int c = 0; c < 3; ++c) {
-      const float2 fu = f2mul(f, U[mxy][c]);
-      uh[mxy][c] = f2fma(f, L[mxy][c], fu);
-      uh[mxy + 4][c] = f2fma(nf, L[mxy][c], fu);
-    }
-  float2 wh[8][3];
-#pragma unroll
-  for (int m = 0; m < 8; ++m)
-#pragma unroll
-    for (int c = 0; c < 3; ++c) {
-      const int q = m ^ (1 << c);
-      float2 s = make_float2(0.f, 0.f);
-#pragma unroll
-      for (int c2 = 0; c2 < 3; ++c2)
-        if (modal_nz(q, c, c2)) s = f2fma(B2[q][c][c2], uh[q ^ (1 << c2)][c2], s);
-      wh[m][c] = s;
-    }
-#pragma unroll
-  for (int mxy = 0; mxy < 4; ++mxy)
-#pragma unroll
-    for (int c = 0; c < 3; ++c) {
-      lo[mxy][c] = f2sub(wh[mxy][c], wh[mxy + 4][c]);
-      hi[mxy][c] = f2add(wh[mxy][c], wh[mxy + 4][c]);
-    }
-}
-
-template <int MODE, typename IX>
-__global__ void __launch_bounds__(32 * op2::TW, 1) op2_kernel(const __grid_constant__ Op2Args P) {
-  using T = float;
-  constexpr int TW = op2::TW;
-  const OpArgs<float>& a = P.a;
-  if (a.halt && *((volatile const int*)a.halt)) return;
-  constexpr int BM = MODE == OP_JACOBI_DOT ? OP_JACOBI : (MODE == OP_CHEB2_DOT ? OP_CHEB2 : MODE);
-  constexpr bool DOTB = MODE == OP_JACOBI_DOT || MODE == OP_CHEB2_DOT;
-  constexpr bool NEED_F = (BM == OP_JACOBI || BM == OP_CHEB2);
-  constexpr bool NEED_B = BM == OP_RESID || BM == OP_RESID_NORM || BM == OP_JACOBI || BM == OP_CHEB2;
-  constexpr bool NEED_P = BM == OP_CHEB2;
-  constexpr int NX_OWN = 31, NY_OWN = 2 * TW - 1;
-  __shared__ __align__(16) T xch[2][TW][32][4];
-  const Grid& g = a.g;
-  const int lane = threadIdx.x, wy = threadIdx.y;
-  const int nxy = a.tiles_x * a.tiles_y;
-  const int items = nxy * a.nchunks;
-  const IX plane3 = (IX)3 * g.NX * g.NY;
-  const IX eplane = (IX)g.nx * g.ny;
-  const uint32_t F = a.m.faces;
-  const T* __restrict__ x = a.x;
-  const T* __restrict__ bv = a.b;
-  T* yv = a.y;  // not restrict: CHEB2 runs in place (xin == y)
-  const T* xinv = a.xin;
-  const T* __restrict__ fac = a.fac;
-  double acc0 = 0.0;
-  for (int item = blockIdx.x; item < items; item += gridDim.x) {
-    const int chunk = item / nxy, t = item - chunk * nxy;
-    const int ty = t / a.tiles_x, tx = t - ty * a.tiles_x;
-    const int i0 = tx * NX_OWN, j0 = ty * NY_OWN;
-    const int k0 = chunk * a.kchunk;
-    const int k1 = min(k0 + a.kchunk, g.NZ);
-    const int ie = i0 - 1 + lane, jeA = j0 - 1 + 2 * wy;
-    // clamped corner addresses: node columns ie, ie+1 and node rows jeA .. jeA+2
-    const int xc0 = min(max(ie, 0), g.NX - 1), xc1 = min(ie + 1, g.NX - 1);
-    IX roff[3];
-#pragma unroll
-    for (int r = 0; r < 3; ++r) roff[r] = (IX)3 * ((IX)xc0 + (IX)g.NX * min(max(jeA + r, 0), g.NY - 1));
-    const IX dxo = (IX)3 * (xc1 - xc0);
-    const bool colx = (ie >= 0) && (ie < g.nx);
-    const bool vA = colx && jeA >= 0 && jeA < g.ny, vB = colx && jeA + 1 >= 0 && jeA + 1 < g.ny;
-    const int xe = min(max(ie, 0), g.nx - 1);  // clamped element column
-    const IX eA = (IX)xe + (IX)g.nx * min(max(jeA, 0), g.ny - 1), eB = (IX)xe + (IX)g.nx * min(max(jeA + 1, 0), g.ny - 1);
-    const int in = i0 + lane, nA = j0 + 2 * wy, nB = nA + 1;
-    const bool ownA = (lane < NX_OWN) && (in < g.NX) && (nA < g.NY);
-    const bool ownB = (lane < NX_OWN) && (wy < TW - 1) && (in < g.NX) && (nB < g.NY);
-    const bool fxx = ((F & 1u) && in == 0) || ((F & 2u) && in == g.NX - 1);
-    const unsigned fixA = (fxx || ((F & 4u) && nA == 0) || ((F & 8u) && nA == g.NY - 1)) ? 7u : 0u;
-    const unsigned fixB = (fxx || ((F & 4u) && nB == 0) || ((F & 8u) && nB == g.NY - 1)) ? 7u : 0u;
-    const IX ncolA = (IX)min(in, g.NX - 1) + (IX)g.NX * min(nA, g.NY - 1);
-    const IX ncolB = (IX)min(in, g.NX - 1) + (IX)g.NX * min(nB, g.NY - 1);
-    auto load_layer = [&](int kk, T (&v)[3][2][3]) {
-      const IX L = plane3 * (IX)min(max(kk, 0), g.NZ - 1);
-#pragma unroll
-      for (int r = 0; r < 3; ++r) {
-        const T* p0 = x + L + roff[r];
-#pragma unroll
-        for (int c = 0; c < 3; ++c) {
-          v[r][0][c] = __ldg(p0 + c);
-          v[r][1][c] = __ldg(p0 + dxo + c);
-        }
-      }
-    };
-    auto load_f = [&](int k) -> float2 {
-      if (k < 0 || k >= g.nz) return make_float2(0.f, 0.f);
-      const IX o = eplane * (IX)k;
-      const T fa = __ldg(fac + eA + o), fb = __ldg(fac + eB + o);
-      return make_float2(vA ? fa : 0.f, vB ? fb : 0.f);
-    };
-    float2 Lm[4][3], carry[4][3], xown[3];
-    float2 fprev;
-    {
-      T raw[3][2][3];
-      float2 Lp[4][3], lo[4][3];
-      load_layer(k0 - 1, raw);
-      xy_forward2(raw, Lp);
-      load_layer(k0, raw);
-#pragma unroll
-      for (int c = 0; c < 3; ++c) xown[c] = make_float2(raw[1][1][c], raw[2][1][c]);
-      xy_forward2(raw, Lm);
-      fprev = load_f(k0 - 1);
-      element_modal2(P.B2, Lp, Lm, fprev, lo, carry);
-    }
-    float2 bnext[3], pnext[3];
-#pragma unroll
-    for (int c = 0; c < 3; ++c) bnext[c] = pnext[c] = make_float2(0.f, 0.f);
-    auto load_bp = [&](int kk) {
-      const IX L = plane3 * (IX)kk;
-#pragma unroll
-      for (int c = 0; c < 3; ++c) {
-        if (NEED_B) bnext[c] = make_float2(ownA ? __ldg(bv + L + 3 * ncolA + c) : 0.f, ownB ? __ldg(bv + L + 3 * ncolB + c) : 0.f);
-        if (NEED_P)  // plain loads: y may alias xin
-          pnext[c] = make_float2((ownA && xinv) ? xinv[L + 3 * ncolA + c] : 0.f, (ownB && xinv) ? xinv[L + 3 * ncolB + c] : 0.f);
-      }
-    };
-    if (NEED_B || NEED_P) load_bp(k0);
-    T nraw[3][2][3];
-    load_layer(k0 + 1, nraw);
-    float2 fnext = load_f(k0);
-    float2 acc2 = make_float2(0.f, 0.f);
-#pragma unroll 1
-    for (int k = k0; k < k1; ++k) {
-      T raw[3][2][3];
-#pragma unroll
-      for (int r = 0; r < 3; ++r)
-#pragma unroll
-        for (int n = 0; n < 2; ++n)
-#pragma unroll
-          for (int c = 0; c < 3; ++c) raw[r][n][c] = nraw[r][n][c];
-      const float2 f = fnext;
-      float2 bk[3], pk3[3];
-#pragma unroll
-      for (int c = 0; c < 3; ++c) bk[c] = bnext[c], pk3[c] = pnext[c];
-      if (k + 1 < k1) {  // prefetch the next layer
-        load_layer(k + 2, nraw);
-        fnext = load_f(k + 1);
-        if (NEED_B || NEED_P) load_bp(k + 1);
-      }
-      float2 Um[4][3], lo[4][3], hi[4][3];
-      xy_forward2(raw, Um);
-      element_modal2(P.B2, Lm, Um, f, lo, hi);
-#pragma unroll
-      for (int m = 0; m < 4; ++m)
-#pragma unroll
-        for (int c = 0; c < 3; ++c) {
-          lo[m][c] = f2add(lo[m][c], carry[m][c]);
-          carry[m][c] = hi[m][c];
-          Lm[m][c] = Um[m][c];
-        }
-      float2 cv[4][3];
-      xy_inverse2(lo, cv);
-      // X: upper corner rows (A: node row nA, B: nB); Y: lower rows (A: nA-1, B: nA)
-      float2 X[3], Y[3];
-#pragma unroll
-      for (int c = 0; c < 3; ++c) {
-        X[c] = f2add(cv[3][c], f2shfl_down(cv[2][c]));
-        Y[c] = f2add(cv[1][c], f2shfl_down(cv[0][c]));
-      }
-      float2 F2 = make_float2(0.f, 0.f);
-      if (NEED_F) {
-        const float2 fcol = f2add(fprev, f);
-        F2 = f2add(fcol, f2shfl_down(fcol));
-      }
-      fprev = f;
-      const int buf = k & 1;
-      store4(&xch[buf][wy][lane][0], Y[0].x, Y[1].x, Y[2].x, F2.x);  // row nA-1 goes to the warp below
-      __syncthreads();
-      if (ownA || ownB) {
-        T nb[4] = {T(0), T(0), T(0), T(0)};
-        if (wy < TW - 1) load4(&xch[buf][wy + 1][lane][0], nb);
-        const IX Lk = plane3 * (IX)k;
-        unsigned fzA = fixA, fzB = fixB;
-        if (((F & 16u) && k == 0) || ((F & 32u) && k == g.NZ - 1)) fzA = fzB = 7u;
-        if (a.m.node) {
-          const IX np = (IX)g.NX * g.NY * (IX)k;
-          if (ownA) fzA |= (unsigned)__ldg(a.m.node + ncolA + np);
-          if (ownB) fzB |= (unsigned)__ldg(a.m.node + ncolB + np);
-        }
-        float2 dinv2[3];
-#pragma unroll
-        for (int c = 0; c < 3; ++c) dinv2[c] = make_float2(0.f, 0.f);
-        if (NEED_F) {
-          const float fsA = F2.x + F2.y, fsB = F2.y + nb[3];
-          if (a.diag_quirk) {
-            const float rA = recip(fmaf(a.K.dd[0], fsA, a.sigma)), rB = recip(fmaf(a.K.dd[0], fsB, a.sigma));
-#pragma unroll
-            for (int c = 0; c < 3; ++c) dinv2[c] = make_float2(rA, rB);
-          } else {
-#pragma unroll
-            for (int c = 0; c < 3; ++c)
-              dinv2[c] = make_float2(recip(fmaf(a.K.dd[c], fsA, a.sigma)), recip(fmaf(a.K.dd[c], fsB, a.sigma)));
-          }
-        }
-        const float2 sig2 = make_float2(a.sigma, a.sigma);
-#pragma unroll
-        for (int c = 0; c < 3; ++c) {
-          const float2 Kx = make_float2(X[c].x + Y[c].y, X[c].y + nb[c]);
-          const float2 Ax = f2fma(sig2, xown[c], Kx);
-          float2 out;
-          if (BM == OP_APPLY || BM == OP_APPLY_DOT) {
-            out = Ax;
-          } else if (BM == OP_RESID || BM == OP_RESID_NORM) {
-            out = f2sub(bk[c], Ax);
-          } else if (BM == OP_JACOBI) {
-            const float2 om = make_float2(a.omega, a.omega);
-            out = f2fma(f2mul(om, dinv2[c]), f2sub(bk[c], Ax), xown[c]);
-          } else {
-            const float2 c1 = make_float2(a.c1, a.c1), c2 = make_float2(a.c2, a.c2);
-            const float2 tt = f2fma(c1, f2sub(xown[c], pk3[c]), xown[c]);
-            out = f2fma(f2mul(c2, dinv2[c]), f2sub(bk[c], Ax), tt);
-          }
-          out.x = (((fzA >> c) & 1u) || !ownA) ? T(0) : out.x;
-          out.y = (((fzB >> c) & 1u) || !ownB) ? T(0) : out.y;
-          if (BM == OP_APPLY_DOT) acc2 = f2fma(xown[c], out, acc2);
-          if (BM == OP_RESID_NORM) acc2 = f2fma(out, out, acc2);
-          if (DOTB) acc2 = f2fma(bk[c], out, acc2);
-          if (ownA) yv[Lk + 3 * ncolA + c] = out.x;
-          if (ownB) yv[Lk + 3 * ncolB + c] = out.y;
-        }
-      }
-#pragma unroll
-      for (int c = 0; c < 3; ++c) xown[c] = make_float2(raw[1][1][c], raw[2][1][c]);
-    }
-    acc0 += (double)acc2.x + (double)acc2.y;
-    __syncthreads();  // the next item reuses xch
-  }
-  if (MODE == OP_APPLY_DOT || MODE == OP_RESID_NORM || MODE == OP_JACOBI_DOT || MODE == OP_CHEB2_DOT) {
-    double v[1] = {acc0};
-    block_reduce_finalize<1>(a.red, v);
-  }
-}
-
 template <typename T>
 static ModalK<T> cast_modal(const ModalK<double>& K) {
   ModalK<T> o;
@@ -1275,53 +975,14 @@ static int env_int(const char* name, int dflt) {
   return (v && *v) ? std::atoi(v) : dflt;
 }
 
-// Form of FP32 single-column launches: 2 (default) the two-row packed kernel,
-// 1 the TMA-staged kernel, 0 the one-row kernel with per-thread global loads
-// (HEXA_OP_FORM, for A/B timing); HEXA_OP_TEST_STALL=q makes CTA 0 of the
-// TMA-staged kernel leave out its layer load q (tests of the bounded waits).
+// Form of FP32 single-column launches (HEXA_OP_FORM, read once): 0 (default)
+// the one-row kernel with per-thread global loads, 1 the TMA-staged kernel
+// (measured slower on GB300: more instructions in an issue-bound kernel);
+// HEXA_OP_TEST_STALL=q makes CTA 0 of the TMA-staged kernel leave out its
+// layer load q (tests of the bounded waits).
 static int op_form() {
-  static const int form = env_int("HEXA_OP_FORM", 2);
+  static const int form = env_int("HEXA_OP_FORM", 0);
   return form;
-}
-
-static int op2_resident_ctas() {
-  static int cached = 0;
-  if (!cached) {
-    int dev = 0, sms = 0, occ = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, op2_kernel<OP_CHEB2, int>, 32 * op2::TW, 0);
-    cached = std::max(1, sms) * std::max(1, occ);
-  }
-  return cached;
-}
-
-static void launch_op2(int mode, const OpArgs<float>& a, bool i32, cudaStream_t st) {
-  Op2Args P;
-  P.a = a;
-  for (int q = 0; q < 8; ++q)
-    for (int c = 0; c < 3; ++c)
-      for (int c2 = 0; c2 < 3; ++c2) P.B2[q][c][c2] = make_float2(a.K.B[q][c][c2], a.K.B[q][c][c2]);
-  const long long items = (long long)a.tiles_x * a.tiles_y * a.nchunks;
-  const int grid = (int)std::min<long long>(items, op2_resident_ctas());
-  const dim3 block(32, op2::TW);
-#define HEXA_OP2_CASE(M)                                                  \
-  case M:                                                                \
-    if (i32) op2_kernel<M, int><<<grid, block, 0, st>>>(P);              \
-    else op2_kernel<M, long long><<<grid, block, 0, st>>>(P);            \
-    break;
-  switch (mode) {
-    HEXA_OP2_CASE(OP_APPLY)
-    HEXA_OP2_CASE(OP_APPLY_DOT)
-    HEXA_OP2_CASE(OP_RESID)
-    HEXA_OP2_CASE(OP_RESID_NORM)
-    HEXA_OP2_CASE(OP_JACOBI)
-    HEXA_OP2_CASE(OP_CHEB2)
-    HEXA_OP2_CASE(OP_JACOBI_DOT)
-    HEXA_OP2_CASE(OP_CHEB2_DOT)
-    default: break;
-  }
-#undef HEXA_OP2_CASE
 }
 
 static int tma_resident_ctas() {
@@ -1388,10 +1049,6 @@ void launch_op(int mode, const OpArgs<T>& a0, cudaStream_t st) {
   const dim3 block(32, TYW);
   const bool i32 = a.g.ndof() < (1LL << 30) && a.g.nelem() < (1LL << 30);
   if constexpr (sizeof(T) == 4) {
-    if (a.ncol <= 1 && op_form() == 2) {
-      launch_op2(mode, a, i32, st);
-      return;
-    }
     if (a.ncol <= 1 && op_form() == 1) {
       launch_op_tma(mode, a, i32, st);
       return;
