@@ -141,6 +141,79 @@ __global__ void __launch_bounds__(kThreads) gram_kernel(const T* __restrict__ a,
   if (tid == 0) *ticket = 0u;
 }
 
+// The same sums for FP32 columns as a streaming pass: each thread walks its
+// grid-stride DOFs with coalesced loads (consecutive lanes, consecutive DOFs
+// of one column) and keeps its KC x NJ column-pair sums in registers, NJ =
+// NBC / H columns of the right operand per thread (H = 2 threads per DOF when
+// NBC = 16, so that the sums fit in registers).  No shared-memory staging and
+// no per-tile FP64 work: GB300's FP64 rate is a small fraction of its FP32
+// rate.  Each thread's FP32 sums (a few hundred products at the sizes this
+// path serves) are folded into FP64 once, at the end, reduced over the warp by
+// shuffles and over the block in shared memory, and the per-block partials
+// are summed in block order by the last block (ticket): bitwise reproducible.
+template <int KC, int NB>
+__global__ void __launch_bounds__(kThreads, 2) gram_stream_kernel(const float* __restrict__ a, const float* __restrict__ b1,
+                                                                   const float* __restrict__ b2, int k, long long n,
+                                                                   double* partials, unsigned* ticket, double* out,
+                                                                   const int* halt) {
+  if (halt_set(halt)) return;
+  constexpr int NBC = NB * KC, H = NBC > 8 ? 2 : 1, NJ = NBC / H, NPAIR = KC * NBC, NW = kThreads / 32;
+  __shared__ double sw[NW][NPAIR];
+  __shared__ bool am_last;
+  const int tid = threadIdx.x, h = tid % H, lane = tid & 31, warp = tid >> 5;
+  float acc[KC][NJ];
+#pragma unroll
+  for (int i = 0; i < KC; ++i)
+#pragma unroll
+    for (int j = 0; j < NJ; ++j) acc[i][j] = 0.f;
+  const long long stride = (long long)gridDim.x * (kThreads / H);
+#pragma unroll 2
+  for (long long d = ((long long)blockIdx.x * kThreads + tid) / H; d < n; d += stride) {
+    float av[KC], bv[NJ];
+#pragma unroll
+    for (int i = 0; i < KC; ++i) av[i] = i < k ? __ldg(a + (long long)i * n + d) : 0.f;
+#pragma unroll
+    for (int j = 0; j < NJ; ++j) {
+      const int col = h * NJ + j, jj = col < KC ? col : col - KC;
+      const float* src = col < KC ? b1 : b2;
+      bv[j] = jj < k ? __ldg(src + (long long)jj * n + d) : 0.f;
+    }
+#pragma unroll
+    for (int i = 0; i < KC; ++i)
+#pragma unroll
+      for (int j = 0; j < NJ; ++j) acc[i][j] = fmaf(av[i], bv[j], acc[i][j]);
+  }
+  // warp: lanes of the same h (offsets that are multiples of H)
+#pragma unroll
+  for (int i = 0; i < KC; ++i)
+#pragma unroll
+    for (int j = 0; j < NJ; ++j) {
+      double v = (double)acc[i][j];
+#pragma unroll
+      for (int off = 16; off >= H; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
+      if (lane < H) sw[warp][i * NBC + lane * NJ + j] = v;
+    }
+  __syncthreads();
+  for (int q = tid; q < NPAIR; q += kThreads) {
+    double v = 0.0;
+#pragma unroll
+    for (int w = 0; w < NW; ++w) v += sw[w][q];
+    partials[(long long)blockIdx.x * NPAIR + q] = v;
+  }
+  __threadfence();
+  __syncthreads();
+  if (tid == 0) am_last = (atomicAdd(ticket, 1u) == gridDim.x - 1);
+  __syncthreads();
+  if (!am_last) return;
+  __threadfence();
+  for (int q = tid; q < NPAIR; q += kThreads) {
+    double v = 0.0;
+    for (unsigned b = 0; b < gridDim.x; ++b) v += ((volatile double*)partials)[(long long)b * NPAIR + q];
+    out[q] = v;
+  }
+  if (tid == 0) *ticket = 0u;
+}
+
 // out (k x k, row = direction, column = right-hand side) = sign * G^+ rhs with
 // G_ij = (g[i*ldg+j] + g[j*ldg+i]) / 2 and rhs_ij = r[i*ldr + roff + j].
 __global__ void block_solve_kernel(const double* g, int ldg, const double* r, int ldr, int roff, int k, double sign,
@@ -311,10 +384,16 @@ void launch_gram(const T* a, const T* b1, const T* b2, int k, long long n, doubl
   constexpr int TD = gram_td<T>();
   const int g = (int)std::max<long long>(1, std::min<long long>((n + TD - 1) / TD, kBlockRedBlocks));
   const int kc = block_kc(k);
-#define HEXA_GRAM(KCV)                                                                                   \
-  case KCV:                                                                                             \
-    if (b2) gram_kernel<T, KCV, 2><<<g, kThreads, 0, st>>>(a, b1, b2, k, n, partials, ticket, out, halt); \
-    else gram_kernel<T, KCV, 1><<<g, kThreads, 0, st>>>(a, b1, b2, k, n, partials, ticket, out, halt);    \
+#define HEXA_GRAM(KCV)                                                                                        \
+  case KCV:                                                                                                  \
+    if constexpr (sizeof(T) == 4 && (KCV == 4 || KCV == 8)) {                                                              \
+      if (b2) gram_stream_kernel<KCV, 2><<<kBlockRedBlocks, kThreads, 0, st>>>(a, b1, b2, k, n, partials, ticket, out, halt); \
+      else gram_stream_kernel<KCV, 1><<<kBlockRedBlocks, kThreads, 0, st>>>(a, b1, b2, k, n, partials, ticket, out, halt);   \
+    } else if (b2) {                                                                                         \
+      gram_kernel<T, KCV, 2><<<g, kThreads, 0, st>>>(a, b1, b2, k, n, partials, ticket, out, halt);          \
+    } else {                                                                                                 \
+      gram_kernel<T, KCV, 1><<<g, kThreads, 0, st>>>(a, b1, b2, k, n, partials, ticket, out, halt);          \
+    }                                                                                                        \
     break;
   switch (kc) {
     HEXA_GRAM(1)
