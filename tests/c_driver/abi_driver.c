@@ -98,6 +98,36 @@ static int gpu_checks(hexa_ctx* ctx) {
   CHECK(hexa_update_density(ctx, &g, dens, l1, NULL, orig, &up, &us) == HEXA_OK, 30);
   CHECK(us.status == 0 && us.filter_used == 0 && us.culled == 0 && us.active_count == ne, 31);
   for (long e = 0; e < ne; ++e) CHECK(dens[e] == 0.6f, 32);
+  /* Solver.solve_system with the reference's argument types: a void block of
+   * 2x2x2 elements (density at the minimum) is pruned from outer iteration 3 on;
+   * its interior node gets u = 0 (reconstruct_full_solution) */
+  float* dens32 = malloc(sizeof(float) * ne);
+  float* f32 = calloc(ndof, sizeof(float));
+  float* bcind = calloc(ndof, sizeof(float)); /* Matrix{Float32}(nNodes, 3), column-major */
+  CHECK(dens32 && f32 && bcind, 35);
+  for (long e = 0; e < ne; ++e) {
+    const long i = e % 16, j = (e / 16) % 8, k = e / 128;
+    dens32[e] = (i >= 6 && i < 8 && j >= 2 && j < 4 && k >= 2 && k < 4) ? 1e-3f : 0.5f;
+  }
+  for (long nd = 0; nd < nn; ++nd)
+    if (nd % 17 == 0)
+      for (int c = 0; c < 3; ++c) bcind[nd + nn * c] = 1.0f;
+  for (long j = 0; j <= 8; ++j) f32[3 * (16 + 17 * j) + 2] = -1.0f / 9.0f;
+  hexa_solve_params ps;
+  hexa_default_params(&ps);
+  ps.tol = 1e-10;
+  double relres = 1.0;
+  char name[32];
+  int64_t active = 0;
+  hexa_solve_stats ss;
+  CHECK(hexa_solve_system(ctx, &g, 1.0f, bcind, f32, dens32, 1e-3f, 1, 3, &ps, NULL, u64, &relres, name, 32, &ss,
+                          &active) == HEXA_OK, 36);
+  CHECK(active == ne - 8 && relres < 1e-10 && strcmp(name, "GMG_GPU") == 0, 37);
+  const long mid = 7 + 17 * (3 + 9 * 3); /* the node inside the void block */
+  CHECK(u64[3 * mid] == 0.0 && u64[3 * mid + 1] == 0.0 && u64[3 * mid + 2] == 0.0, 38);
+  CHECK(hexa_solve_system(ctx, &g, 1.0f, bcind, f32, dens32, 1e-3f, 1, 2, &ps, NULL, u64, &relres, name, 32, &ss,
+                          &active) == HEXA_OK && active == ne, 39);
+  free(dens32), free(f32), free(bcind);
   CHECK(hexa_solve(ctx, NULL, &bc, fac, f, &p, NULL, u64, &s64) == HEXA_ERR_ARG, 33);
   CHECK(strlen(hexa_last_error(ctx)) > 0, 34);
   free(fac), free(f), free(u32), free(u64), free(rho), free(out), free(dens), free(l1), free(orig);
