@@ -37,8 +37,8 @@ struct OpArgs {
   int diag_quirk;
   RedArgs red;
   const int* halt;  // nullable: PcgScalars::halt
-  int ncol = 1;     // columns (x, b, y advance by ndof per column): OP_APPLY and
-                    // OP_RESID only
+  int ncol = 1;     // columns (x, b, xin, y advance by ndof per column): OP_APPLY,
+                    // OP_RESID, OP_JACOBI and OP_CHEB2 only
   int test_stall = -1;  // FP32 staged form: layer load that CTA 0 leaves out (tests of the bounded waits)
 };
 

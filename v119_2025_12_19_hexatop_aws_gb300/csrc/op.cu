@@ -1054,13 +1054,19 @@ void launch_op(int mode, const OpArgs<T>& a0, cudaStream_t st) {
       return;
     }
   }
-  if (a.ncol > 1) {  // multi-column forms: the plain apply and the residual
+  if (a.ncol > 1) {  // multi-column forms (no reductions): apply, residual and the two smoothing steps
     if (mode == OP_APPLY) {
       if (i32) op_kernel<T, OP_APPLY, TYW, int, true><<<grid, block, 0, st>>>(a);
       else op_kernel<T, OP_APPLY, TYW, long long, true><<<grid, block, 0, st>>>(a);
     } else if (mode == OP_RESID) {
       if (i32) op_kernel<T, OP_RESID, TYW, int, true><<<grid, block, 0, st>>>(a);
       else op_kernel<T, OP_RESID, TYW, long long, true><<<grid, block, 0, st>>>(a);
+    } else if (mode == OP_JACOBI) {
+      if (i32) op_kernel<T, OP_JACOBI, TYW, int, true><<<grid, block, 0, st>>>(a);
+      else op_kernel<T, OP_JACOBI, TYW, long long, true><<<grid, block, 0, st>>>(a);
+    } else if (mode == OP_CHEB2) {
+      if (i32) op_kernel<T, OP_CHEB2, TYW, int, true><<<grid, block, 0, st>>>(a);
+      else op_kernel<T, OP_CHEB2, TYW, long long, true><<<grid, block, 0, st>>>(a);
     }
     return;
   }

@@ -521,6 +521,76 @@ struct Graph {
   }
 };
 
+// k columns through one V-cycle together (the block PCG's preconditioner):
+// the smoothing and residual launches of a level run over all k columns (each
+// work item applies the columns in turn while its element factors sit in
+// L1, one launch instead of k); the first sweep, the transfers and the
+// coarsest-level solve run per column.  Column j of every buffer starts at
+// j * (the level's DOF count).  The same arithmetic as k calls of vcycle
+// without a fused reduction.
+template <typename T>
+struct ColBufs {
+  std::vector<T*> xa, xb, b, r;  // per level, k columns each
+};
+
+template <typename T>
+void vcycle_cols(Ctx& c, MG<T>& mg, ColBufs<T>& cb, int l, const T* b, T* xout, int k, const int* halt) {
+  Lev<T>& V = mg.L[l];
+  const long long n = V.g.ndof();
+  if (l == (int)mg.L.size() - 1) {
+    for (int j = 0; j < k; ++j) coarse_solve<T>(c, mg, b + j * n, xout + j * n, halt);
+    return;
+  }
+  const int nw = mg.nu1 + mg.nu2;
+  T* xbk = cb.xb[l];
+  auto bufw = [&](int w) -> T* { return ((nw - 1 - w) % 2 == 0) ? xout : xbk; };
+  int w = 0;
+  T* cur = bufw(w++);
+  const RedArgs none = red(c, FIN_NONE, 1, nullptr);
+  const bool cheb = mg.smoother == HEXA_SMOOTH_CHEBYSHEV;
+  const T* prev = nullptr;
+  auto opk = [&](int mode, const T* x, T* y, const T* xin, T c1, T c2, T omega) {
+    OpArgs<T> a = opargs<T>(V, mg.K, mg.quirk, x, b, y, omega, halt, none);
+    a.xin = xin;
+    a.c1 = c1;
+    a.c2 = c2;
+    a.ncol = k;
+    op<T>(c, mode, a);
+  };
+  for (int j = 0; j < k; ++j)
+    launch_jacobi0<T>(V.g, V.m, V.fac, mg.K, mg.quirk, V.sigma, cheb ? mg.inv_theta : mg.omega, b + j * n,
+                      cur + j * n, halt, c.st);
+  c.launches += k;
+  for (int s = 1; s < mg.nu1; ++s) {
+    T* nx = bufw(w++);
+    if (cheb) {
+      opk(OP_CHEB2, cur, nx, prev, mg.c1[s], mg.c2[s], T(0));
+      prev = cur;
+    } else {
+      opk(OP_JACOBI, cur, nx, nullptr, T(0), T(0), mg.omega);
+    }
+    cur = nx;
+  }
+  opk(OP_RESID, cur, cb.r[l], nullptr, T(0), T(0), mg.omega);
+  Lev<T>& C = mg.L[l + 1];
+  const long long nc = C.g.ndof();
+  for (int j = 0; j < k; ++j) launch_restrict<T>(V.g, cb.r[l] + j * n, C.g, C.m, cb.b[l + 1] + j * nc, halt, c.st);
+  c.launches += k;
+  vcycle_cols<T>(c, mg, cb, l + 1, cb.b[l + 1], cb.xa[l + 1], k, halt);
+  for (int j = 0; j < k; ++j) launch_prolong_add<T>(C.g, cb.xa[l + 1] + j * nc, V.g, V.m, cur + j * n, halt, c.st);
+  c.launches += k;
+  for (int s = 0; s < mg.nu2; ++s) {
+    T* nx = bufw(w++);
+    if (cheb && s > 0) {
+      opk(OP_CHEB2, cur, nx, prev, mg.c1[s], mg.c2[s], T(0));
+    } else {  // damped Jacobi, or the first Chebyshev step (omega = 1/theta)
+      opk(OP_JACOBI, cur, nx, nullptr, T(0), T(0), cheb ? mg.inv_theta : mg.omega);
+    }
+    prev = cur;
+    cur = nx;
+  }
+}
+
 template <class F>
 bool capture(Ctx& c, Graph& G, F&& body) {
   G.reset();
@@ -1408,8 +1478,32 @@ int solve_block(Ctx& c, const Problem& P, int k, const hexa_solve_params& prm, d
   }
   const int* halt = &c.s->halt;
   const double eps = Is64<T>::v ? 1e-12 : 1e-6;
+  // k-column buffers of the block V-cycle (levels 1.. also need right-hand
+  // sides and solutions); the W-cycle runs column by column
+  ColBufs<T> cb;
+  const bool cols = use_mg && mg.gamma == 1 && k > 1;
+  if (cols) {
+    const int nl = (int)mg.L.size();
+    cb.xa.assign(nl, nullptr), cb.xb.assign(nl, nullptr), cb.b.assign(nl, nullptr), cb.r.assign(nl, nullptr);
+    for (int l = 0; l < nl; ++l) {
+      const long long nl_dof = mg.L[l].g.ndof() * (long long)k;
+      const std::string s = "blkmg_" + std::to_string(l) + "_";
+      if (l + 1 < nl) {
+        cb.xb[l] = c.vec<T>(s + "xb", nl_dof);
+        cb.r[l] = c.vec<T>(s + "r", nl_dof);
+        if (!cb.xb[l] || !cb.r[l]) return HEXA_ERR_NOMEM;
+      }
+      if (l > 0) {
+        cb.b[l] = c.vec<T>(s + "b", nl_dof);
+        cb.xa[l] = c.vec<T>(s + "xa", nl_dof);
+        if (!cb.b[l] || !cb.xa[l]) return HEXA_ERR_NOMEM;
+      }
+    }
+  }
   auto iteration = [&]() {
-    if (use_mg) {
+    if (cols) {
+      vcycle_cols<T>(c, mg, cb, 0, R, Z, k, halt);
+    } else if (use_mg) {
       for (int j = 0; j < k; ++j) vcycle<T>(c, mg, 0, R + (long long)j * n, Z + (long long)j * n, halt);
     } else {
       launch_cols_jacobi<T>(Z, R, dinv, n, k, halt, c.st);
