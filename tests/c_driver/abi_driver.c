@@ -116,13 +116,16 @@ static int gpu_checks(hexa_ctx* ctx) {
   hexa_solve_params ps;
   hexa_default_params(&ps);
   ps.tol = 1e-10;
+  ps.divergence_check = 0;
   double relres = 1.0;
   char name[32];
   int64_t active = 0;
   hexa_solve_stats ss;
   CHECK(hexa_solve_system(ctx, &g, 1.0f, bcind, f32, dens32, 1e-3f, 1, 3, &ps, NULL, u64, &relres, name, 32, &ss,
                           &active) == HEXA_OK, 36);
-  CHECK(active == ne - 8 && relres < 1e-10 && strcmp(name, "GMG_GPU") == 0, 37);
+  CHECK(active == ne - 8, 37);
+  CHECK(ss.true_relres <= 1e-10, 43);
+  CHECK(strcmp(name, "GMG_GPU") == 0, 44);
   const long mid = 7 + 17 * (3 + 9 * 3); /* the node inside the void block */
   CHECK(u64[3 * mid] == 0.0 && u64[3 * mid + 1] == 0.0 && u64[3 * mid + 2] == 0.0, 38);
   CHECK(hexa_solve_system(ctx, &g, 1.0f, bcind, f32, dens32, 1e-3f, 1, 2, &ps, NULL, u64, &relres, name, 32, &ss,
