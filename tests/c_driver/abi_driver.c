@@ -99,15 +99,15 @@ static int gpu_checks(hexa_ctx* ctx) {
   CHECK(us.status == 0 && us.filter_used == 0 && us.culled == 0 && us.active_count == ne, 31);
   for (long e = 0; e < ne; ++e) CHECK(dens[e] == 0.6f, 32);
   /* Solver.solve_system with the reference's argument types: a void block of
-   * 2x2x2 elements (density at the minimum) is pruned from outer iteration 3 on;
-   * its interior node gets u = 0 (reconstruct_full_solution) */
+   * 4x4x2 elements (density at the minimum, 3 % of the 1024) is pruned from
+   * outer iteration 3 on; its interior nodes get u = 0 (reconstruct_full_solution) */
   float* dens32 = malloc(sizeof(float) * ne);
   float* f32 = calloc(ndof, sizeof(float));
   float* bcind = calloc(ndof, sizeof(float)); /* Matrix{Float32}(nNodes, 3), column-major */
   CHECK(dens32 && f32 && bcind, 35);
   for (long e = 0; e < ne; ++e) {
     const long i = e % 16, j = (e / 16) % 8, k = e / 128;
-    dens32[e] = (i >= 6 && i < 8 && j >= 2 && j < 4 && k >= 2 && k < 4) ? 1e-3f : 0.5f;
+    dens32[e] = (i >= 6 && i < 10 && j >= 2 && j < 6 && k >= 2 && k < 4) ? 1e-3f : 0.5f;
   }
   for (long nd = 0; nd < nn; ++nd)
     if (nd % 17 == 0)
@@ -123,11 +123,12 @@ static int gpu_checks(hexa_ctx* ctx) {
   hexa_solve_stats ss;
   CHECK(hexa_solve_system(ctx, &g, 1.0f, bcind, f32, dens32, 1e-3f, 1, 3, &ps, NULL, u64, &relres, name, 32, &ss,
                           &active) == HEXA_OK, 36);
-  CHECK(active == ne - 8, 37);
+  CHECK(active == ne - 32, 37);
   CHECK(ss.true_relres <= 1e-10, 43);
   CHECK(strcmp(name, "GMG_GPU") == 0, 44);
-  const long mid = 7 + 17 * (3 + 9 * 3); /* the node inside the void block */
+  const long mid = 8 + 17 * (4 + 9 * 3); /* a node inside the void block */
   CHECK(u64[3 * mid] == 0.0 && u64[3 * mid + 1] == 0.0 && u64[3 * mid + 2] == 0.0, 38);
+  CHECK(u64[3 * (mid + 5) + 2] != 0.0, 45); /* a node outside it moves */
   CHECK(hexa_solve_system(ctx, &g, 1.0f, bcind, f32, dens32, 1e-3f, 1, 2, &ps, NULL, u64, &relres, name, 32, &ss,
                           &active) == HEXA_OK && active == ne, 39);
   free(dens32), free(f32), free(bcind);
