@@ -847,9 +847,6 @@ def run_c5(a):
     u_d = [torch.empty_like(f) for f in f_d]
     R = W.helmholtz_R(1.5)
     pm = solver_params("c5", "mixed")
-    # 8 Jacobi-PCG iterations of the coarsest-level solve (one CTA per instance): measured on these 64 grids,
-    # 30 / 15 / 8 / 4 iterations gave 4.43 / 3.09 / 2.49 / 2.20 s (unfiltered fields), 1165 -> 1344 outer iterations
-    pm.coarse_iters = 8
 
     # the in-batch filter runs the reference's loop (Jacobi-PCG, tolerance 1e-5, at most 200 iterations,
     # GPUHelmholtz.jl:190-266) in FP64: in FP32 the batched and the single-grid reductions, summed in
