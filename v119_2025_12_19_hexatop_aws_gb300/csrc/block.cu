@@ -269,6 +269,14 @@ __global__ void __launch_bounds__(kThreads) block_update_kernel(T* __restrict__ 
     sa[i][j] = (i < k && j < k) ? (T)alpha[i * k + j] : T(0);
   }
   __syncthreads();
+  // up to 8 columns the k x k coefficients live in registers (a shared-memory
+  // read per use made the pass instruction-bound)
+  constexpr int KR = KC <= 8 ? KC : 1;
+  T ar[KR][KR];
+#pragma unroll
+  for (int i = 0; i < KR; ++i)
+#pragma unroll
+    for (int j = 0; j < KR; ++j) ar[i][j] = sa[i][j];
   double acc[KC];
   T part[KC];
 #pragma unroll
@@ -288,8 +296,9 @@ __global__ void __launch_bounds__(kThreads) block_update_kernel(T* __restrict__ 
         T x = X[(long long)j * n + d], r = R[(long long)j * n + d];
 #pragma unroll
         for (int i = 0; i < KC; ++i) {
-          x = fma(pv[i], sa[i][j], x);
-          r = fma(-qv[i], sa[i][j], r);
+          const T aij = KC <= 8 ? ar[i % KR][j % KR] : sa[i][j];
+          x = fma(pv[i], aij, x);
+          r = fma(-qv[i], aij, r);
         }
         X[(long long)j * n + d] = x;
         R[(long long)j * n + d] = r;
@@ -319,6 +328,12 @@ __global__ void __launch_bounds__(kThreads) block_p_update_kernel(T* __restrict_
     sb[i][j] = (i < k && j < k) ? (T)beta[i * k + j] : T(0);
   }
   __syncthreads();
+  constexpr int KR = KC <= 8 ? KC : 1;
+  T br[KR][KR];
+#pragma unroll
+  for (int i = 0; i < KR; ++i)
+#pragma unroll
+    for (int j = 0; j < KR; ++j) br[i][j] = sb[i][j];
   const long long stride = (long long)gridDim.x * blockDim.x;
   for (long long d = (long long)blockIdx.x * blockDim.x + threadIdx.x; d < n; d += stride) {
     T pv[KC];
@@ -329,7 +344,7 @@ __global__ void __launch_bounds__(kThreads) block_p_update_kernel(T* __restrict_
       if (j < k) {
         T v = Z[(long long)j * n + d];
 #pragma unroll
-        for (int i = 0; i < KC; ++i) v = fma(pv[i], sb[i][j], v);
+        for (int i = 0; i < KC; ++i) v = fma(pv[i], KC <= 8 ? br[i % KR][j % KR] : sb[i][j], v);
         P[(long long)j * n + d] = v;
       }
     }
