@@ -117,8 +117,10 @@ void bvcycle(BatchCtx& B, BatchMG<T>& mg, int l, const T* b, T* xout) {
   Ctx& c = B.c;
   BLevel<T>& V = mg.L[l];
   if (V.coarse.n()) {
+    long long mnd = 0, mne = 0;
+    for (const BatchInst& ci : V.coarse.h) mnd = std::max(mnd, ci.g.ndof()), mne = std::max(mne, ci.g.nelem());
     launch_batch_coarse_pcg<T>(V.coarse.d, V.coarse.n(), V.fac, mg.K, V.dinv, b, xout, V.r, V.z, V.p, V.q, V.w,
-                               mg.citers, B.s, c.st);
+                               mg.citers, B.s, c.st, mnd, mne);
     c.launches++;
   }
   if (!V.smooth.n()) return;

@@ -302,10 +302,12 @@ void launch_batch_jacobi0(const BatchInst* in, int ninst, int nblocks, const T* 
 template <typename T>
 void launch_dense_coarse(long long n, const T* A, const T* b, T* x, const int* halt, cudaStream_t st);
 // one CTA per instance: iters Jacobi-PCG iterations on its coarsest grid
+// (vectors in shared memory when the largest grid, max_ndof / max_nelem,
+// fits; r, z, p, q, w are then unused)
 template <typename T>
 void launch_batch_coarse_pcg(const BatchInst* in, int ninst, const T* fac, const ModalK<T>& K, const T* dinv,
                              const T* b, T* x, T* r, T* z, T* p, T* q, T* w, int iters, const PcgScalars* s,
-                             cudaStream_t st);
+                             cudaStream_t st, long long max_ndof, long long max_nelem);
 // Helmholtz matvec + p.Ap per instance over node vectors
 template <typename T>
 void launch_batch_helm_apply_dot(const BatchInst* in, int ninst, int nblocks, const HelmK& K, const T* x, T* y,

@@ -249,6 +249,52 @@ __device__ __forceinline__ bool modal_nz_mg(int q, int c, int c2) {
   return true;
 }
 
+// One element's f K0 u_e in the Hadamard basis: corner values h (corner order
+// dx + 2dy + 4dz) in, corner contributions wh out.
+template <typename T>
+__device__ __forceinline__ void coarse_element_product(const ModalK<T>& K, T f, T (&h)[8][3], T (&wh)[8][3]) {
+#pragma unroll
+  for (int c = 0; c < 3; ++c)
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      const int sft = 1 << d;
+      T tmp[8];
+#pragma unroll
+      for (int cc = 0; cc < 8; ++cc) {
+        const int lo = cc & ~sft;
+        tmp[cc] = (cc & sft) ? (h[lo | sft][c] - h[lo][c]) : (h[lo][c] + h[lo | sft][c]);
+      }
+#pragma unroll
+      for (int cc = 0; cc < 8; ++cc) h[cc][c] = tmp[cc];
+    }
+#pragma unroll
+  for (int mm = 0; mm < 8; ++mm)
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      const int qq = mm ^ (1 << c);
+      T s = T(0);
+#pragma unroll
+      for (int c2 = 0; c2 < 3; ++c2)
+        if (modal_nz_mg(qq, c, c2)) s = fma(K.B[qq][c][c2], h[qq ^ (1 << c2)][c2], s);
+      wh[mm][c] = s * f;
+    }
+  // inverse transform (the forward butterflies transposed)
+#pragma unroll
+  for (int c = 0; c < 3; ++c)
+#pragma unroll
+    for (int d = 2; d >= 0; --d) {
+      const int sft = 1 << d;
+      T tmp[8];
+#pragma unroll
+      for (int cc = 0; cc < 8; ++cc) {
+        const int lo = cc & ~sft;
+        tmp[cc] = (cc & sft) ? (wh[lo][c] + wh[lo | sft][c]) : (wh[lo][c] - wh[lo | sft][c]);
+      }
+#pragma unroll
+      for (int cc = 0; cc < 8; ++cc) wh[cc][c] = tmp[cc];
+    }
+}
+
 template <typename T>
 __device__ __forceinline__ void coarse_pcg_body(const Grid& g, const Mask& m, const T* __restrict__ fac,
                                                 const ModalK<T>& K, T sigma, const T* __restrict__ dinv,
@@ -280,48 +326,8 @@ __device__ __forceinline__ void coarse_pcg_body(const Grid& g, const Mask& m, co
 #pragma unroll
         for (int c = 0; c < 3; ++c) h[cc][c] = p[3 * nd + c];
       }
-#pragma unroll
-      for (int c = 0; c < 3; ++c)
-#pragma unroll
-        for (int d = 0; d < 3; ++d) {
-          const int sft = 1 << d;
-          T tmp[8];
-#pragma unroll
-          for (int cc = 0; cc < 8; ++cc) {
-            const int lo = cc & ~sft;
-            tmp[cc] = (cc & sft) ? (h[lo | sft][c] - h[lo][c]) : (h[lo][c] + h[lo | sft][c]);
-          }
-#pragma unroll
-          for (int cc = 0; cc < 8; ++cc) h[cc][c] = tmp[cc];
-        }
-      const T f = fac[e];
       T wh[8][3];
-#pragma unroll
-      for (int mm = 0; mm < 8; ++mm)
-#pragma unroll
-        for (int c = 0; c < 3; ++c) {
-          const int qq = mm ^ (1 << c);
-          T s = T(0);
-#pragma unroll
-          for (int c2 = 0; c2 < 3; ++c2)
-            if (modal_nz_mg(qq, c, c2)) s = fma(K.B[qq][c][c2], h[qq ^ (1 << c2)][c2], s);
-          wh[mm][c] = s * f;
-        }
-      // inverse transform (the forward butterflies transposed)
-#pragma unroll
-      for (int c = 0; c < 3; ++c)
-#pragma unroll
-        for (int d = 2; d >= 0; --d) {
-          const int sft = 1 << d;
-          T tmp[8];
-#pragma unroll
-          for (int cc = 0; cc < 8; ++cc) {
-            const int lo = cc & ~sft;
-            tmp[cc] = (cc & sft) ? (wh[lo][c] + wh[lo | sft][c]) : (wh[lo][c] - wh[lo | sft][c]);
-          }
-#pragma unroll
-          for (int cc = 0; cc < 8; ++cc) wh[cc][c] = tmp[cc];
-        }
+      coarse_element_product<T>(K, fac[e], h, wh);
 #pragma unroll
       for (int cc = 0; cc < 8; ++cc)
 #pragma unroll
@@ -461,10 +467,130 @@ __global__ void __launch_bounds__(1024) batch_coarse_pcg_kernel(const BatchInst*
   coarse_pcg_body<T>(I.g, I.m, fac + I.eoff, K, (T)I.sigma, dinv + o, b + o, x + o, r + o, z + o, p + o, q + o,
                      w + 24 * I.eoff, iters);
 }
+// The same Jacobi-PCG of one instance's coarsest grid with its five vectors
+// (x, r, z, p, q) and element factors held in shared memory: every pass of an
+// iteration reads and writes shared memory instead of global memory, and the
+// element products are added into q in 8 colour passes (elements of one
+// parity in x, y and z share no node), so no element scratch is needed and
+// the sums are in a fixed order.  Grids up to about 10,000 DOFs fit in FP32
+// (5 n + nElem words).  One CTA per instance, x written to xout at the end.
+template <typename T>
+__global__ void __launch_bounds__(1024) batch_coarse_pcg_smem_kernel(const BatchInst* in, const T* __restrict__ fac,
+                                                                     ModalK<T> K, const T* __restrict__ dinv,
+                                                                     const T* __restrict__ b, T* xout, int iters,
+                                                                     const PcgScalars* s) {
+  extern __shared__ __align__(16) unsigned char coarse_smem[];
+  __shared__ double red[32];
+  const BatchInst& I = in[blockIdx.x];
+  if (batch_halted(s, I.id)) return;
+  const Grid g = I.g;
+  const Mask m = I.m;
+  const int tid = threadIdx.x, nthr = blockDim.x;
+  const int n3 = (int)g.ndof(), ne = (int)g.nelem(), nn = (int)g.nnode();
+  T* sx = (T*)coarse_smem;
+  T* sr = sx + n3;
+  T* sz = sr + n3;
+  T* sp = sz + n3;
+  T* sq = sp + n3;
+  T* sf = sq + n3;
+  const T* gb = b + I.off;
+  const T* gd = dinv + I.off;
+  const T* gf = fac + I.eoff;
+  double part = 0.0;
+  for (int e = tid; e < ne; e += nthr) sf[e] = gf[e];
+  for (int i = tid; i < n3; i += nthr) {
+    const T ri = gb[i], zi = gd[i] * ri;
+    sx[i] = T(0);
+    sr[i] = ri;
+    sz[i] = zi;
+    sp[i] = zi;
+    part += (double)ri * (double)zi;
+  }
+  double rz = cta_sum<T>(part, red);
+  const T sigma = (T)I.sigma;
+  for (int it = 0; it < iters; ++it) {
+    for (int i = tid; i < n3; i += nthr) sq[i] = T(0);
+    __syncthreads();
+    for (int color = 0; color < 8; ++color) {
+      const int cx = color & 1, cy = (color >> 1) & 1, cz = color >> 2;
+      const int mx = (g.nx - cx + 1) >> 1, my = (g.ny - cy + 1) >> 1, mz = (g.nz - cz + 1) >> 1;
+      const int mc = mx * my * mz;
+      for (int t = tid; t < mc; t += nthr) {
+        const int i = 2 * (t % mx) + cx, j = 2 * ((t / mx) % my) + cy, k = 2 * (t / (mx * my)) + cz;
+        T h[8][3];
+#pragma unroll
+        for (int cc = 0; cc < 8; ++cc) {
+          const int nd = (i + (cc & 1)) + g.NX * ((j + ((cc >> 1) & 1)) + g.NY * (k + (cc >> 2)));
+#pragma unroll
+          for (int c = 0; c < 3; ++c) h[cc][c] = sp[3 * nd + c];
+        }
+        T wh[8][3];
+        coarse_element_product<T>(K, sf[i + g.nx * (j + g.ny * k)], h, wh);
+#pragma unroll
+        for (int cc = 0; cc < 8; ++cc) {
+          const int nd = (i + (cc & 1)) + g.NX * ((j + ((cc >> 1) & 1)) + g.NY * (k + (cc >> 2)));
+#pragma unroll
+          for (int c = 0; c < 3; ++c) sq[3 * nd + c] += wh[cc][c];
+        }
+      }
+      __syncthreads();
+    }
+    part = 0.0;
+    for (int nd = tid; nd < nn; nd += nthr) {
+      const int i = nd % g.NX, t = nd / g.NX, j = t % g.NY, k = t / g.NY;
+      const unsigned fx = fixed_bits(g, m, i, j, k, nd);
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        const T pv = sp[3 * nd + c];
+        const T qv = ((fx >> c) & 1u) ? T(0) : fma(sigma, pv, sq[3 * nd + c]);
+        sq[3 * nd + c] = qv;
+        part += (double)pv * (double)qv;
+      }
+    }
+    const double pAp = cta_sum<T>(part, red);
+    if (!(pAp > 0.0)) break;  // converged to rounding or no curvature left
+    const T alpha = (T)(rz / pAp);
+    part = 0.0;
+    for (int i = tid; i < n3; i += nthr) {
+      sx[i] = fma(alpha, sp[i], sx[i]);
+      const T ri = fma(-alpha, sq[i], sr[i]);
+      sr[i] = ri;
+      const T zi = gd[i] * ri;
+      sz[i] = zi;
+      part += (double)ri * (double)zi;
+    }
+    const double rz_new = cta_sum<T>(part, red);
+    const T beta = (T)(rz != 0.0 ? rz_new / rz : 0.0);
+    rz = rz_new;
+    for (int i = tid; i < n3; i += nthr) sp[i] = fma(beta, sp[i], sz[i]);
+    __syncthreads();
+  }
+  T* gx = xout + I.off;
+  for (int i = tid; i < n3; i += nthr) gx[i] = sx[i];
+}
+
+// Shared memory the smem form needs for the largest coarsest grid of a launch
+// (0: too large, use the global-memory form).
+template <typename T>
+size_t batch_coarse_smem_bytes(long long max_ndof, long long max_nelem) {
+  const size_t bytes = (size_t)(5 * max_ndof + max_nelem) * sizeof(T);
+  return bytes <= 220u * 1024u ? bytes : 0;
+}
+
 template <typename T>
 void launch_batch_coarse_pcg(const BatchInst* in, int ninst, const T* fac, const ModalK<T>& K, const T* dinv,
                              const T* b, T* x, T* r, T* z, T* p, T* q, T* w, int iters, const PcgScalars* s,
-                             cudaStream_t st) {
+                             cudaStream_t st, long long max_ndof, long long max_nelem) {
+  const size_t smem = batch_coarse_smem_bytes<T>(max_ndof, max_nelem);
+  if (smem > 0) {
+    static bool attr = false;
+    if (!attr) {
+      cudaFuncSetAttribute(batch_coarse_pcg_smem_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
+      attr = true;
+    }
+    batch_coarse_pcg_smem_kernel<T><<<ninst, 1024, smem, st>>>(in, fac, K, dinv, b, x, iters, s);
+    return;
+  }
   batch_coarse_pcg_kernel<T><<<ninst, 1024, 0, st>>>(in, fac, K, dinv, b, x, r, z, p, q, w, iters, s);
 }
 
@@ -514,7 +640,7 @@ void launch_dense_coarse(long long n, const T* A, const T* b, T* x, const int* h
                                         const T*, T*, const PcgScalars*, cudaStream_t);                   \
   template void launch_batch_coarse_pcg<T>(const BatchInst*, int, const T*, const ModalK<T>&, const T*,   \
                                            const T*, T*, T*, T*, T*, T*, T*, int, const PcgScalars*,      \
-                                           cudaStream_t);
+                                           cudaStream_t, long long, long long);
 INST(double)
 INST(float)
 #undef INST
