@@ -1057,9 +1057,9 @@ int solve_plain(Ctx& c, const Problem& P, const hexa_solve_params& prm, const do
 Ctx::Tuned autotune_mixed(Ctx& c, const Problem& P, const hexa_solve_params& prm, float* fac32,
                           const ModalK<float>& K32, double sigma, PcgEnv<float>& E, float* b32, double bnorm,
                           MG<float>& mg, bool search_ratio = false) {
-  char key[96];
-  std::snprintf(key, sizeof(key), "%d,%d,%d,%d,%g,%g,%d", P.g.nx, P.g.ny, P.g.nz, prm.diag_quirk, P.nu, prm.tol,
-                search_ratio ? 1 : 0);
+  char key[128];
+  std::snprintf(key, sizeof(key), "%d,%d,%d,%d,%g,%g,%g,%d", P.g.nx, P.g.ny, P.g.nz, prm.diag_quirk, P.nu, prm.tol,
+                prm.shift_factor, search_ratio ? 1 : 0);
   auto it = c.tuned.find(key);
   if (it != c.tuned.end()) return it->second;
   const long long n = P.g.ndof();
