@@ -54,6 +54,25 @@ def test_batch_matches_direct_solution(ctx, oracle, rng):
         assert np.linalg.norm(U[i] - u_ref) <= 1e-9 * np.linalg.norm(u_ref), i
 
 
+@pytest.mark.parametrize("faces,levels", [(1, [2, 2, 2, 2]), (1 | 2, [2, 2, 1, 1])])
+def test_batch_odd_axes_coarsen_rounded_up(ctx, rng, faces, levels):
+    """Odd axes keep coarsening (rounded up, the extra half element void)
+    unless that axis' high face is clamped; either way each instance matches
+    its own FP64 solve."""
+    dims = [(22, 11, 11), (18, 9, 9), (15, 7, 9), (13, 9, 7)]
+    grids, facs, forces = instances(rng, dims)
+    # 1e-12: with E_min = 1e-9 voids a 1e-9 residual leaves u errors near 1e-6
+    p = _lib.default_params(precision="mixed", tol=1e-12, divergence_check=0)
+    U, stats, rc = solve_batch(grids, facs, forces, clamp_faces=faces, params=p, ctx=ctx)
+    assert rc == _lib.HEXA_OK
+    assert [s["mg_levels"] for s in stats] == levels
+    p64 = _lib.default_params(precision="fp64", divergence_check=0, tol=1e-12)
+    for i, g in enumerate(grids):
+        assert stats[i]["status"] == 0 and stats[i]["true_relres"] <= 1e-12, i
+        u, s = solve(g, facs[i], forces[i], clamp_faces=faces, params=p64, ctx=ctx)
+        assert np.linalg.norm(U[i] - u) <= 1e-7 * np.linalg.norm(u), i
+
+
 def test_batch_zero_load_instance_and_determinism(ctx, rng):
     grids, facs, forces = instances(rng, DIMS[:4])
     forces[2] = np.zeros_like(forces[2])

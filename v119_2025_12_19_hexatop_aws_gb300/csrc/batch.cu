@@ -172,15 +172,33 @@ void bvcycle(BatchCtx& B, BatchMG<T>& mg, int l, const T* b, T* xout) {
   }
 }
 
-// Level count of one instance: the single-grid rule (halve while every axis
-// is even and >= 4, down to ~2500 nodes, or the requested count).
-int batch_levels(const Grid& g, int requested) {
+// Coarse grid of a batch level: every axis halved, an odd axis rounded up.
+// The extra half element of a rounded axis lies past the fine grid's high
+// face; its fine children do not exist, so it coarsens to a factor averaged
+// over the children that do (a partly void element), restriction gathers
+// only fine nodes that exist and prolongation never reads past the coarse
+// grid.  For an even axis this is the plain 2:1 halving.
+Grid batch_coarse_grid(const Grid& g) { return make_grid((g.nx + 1) / 2, (g.ny + 1) / 2, (g.nz + 1) / 2); }
+
+// Coarsest grids of a batch are solved by one CTA's Jacobi-PCG each, whose
+// time follows the largest of them, so batch hierarchies coarsen further
+// than the single-grid one (whose dense coarsest solve wants ~2500 nodes).
+constexpr long long kBatchCoarseNodes = 1000;
+
+// Level count of one instance: halve (rounding an odd axis up) while every
+// axis is >= 4, down to kBatchCoarseNodes nodes, or the requested count.  An
+// odd axis whose high face is clamped stops coarsening: the rounded-up
+// coarse grid would move that face half an element outwards.
+int batch_levels(const Grid& g, uint32_t faces, int requested) {
   int nx = g.nx, ny = g.ny, nz = g.nz, lv = 1;
   const int maxlv = requested > 0 ? requested : 16;
   while (lv < maxlv) {
-    if ((nx & 1) || (ny & 1) || (nz & 1) || nx < 4 || ny < 4 || nz < 4) break;
-    if (requested <= 0 && (long long)(nx + 1) * (ny + 1) * (nz + 1) <= 2500) break;
-    nx >>= 1; ny >>= 1; nz >>= 1;
+    if (nx < 4 || ny < 4 || nz < 4) break;
+    if (((nx & 1) && (faces & 2u)) || ((ny & 1) && (faces & 8u)) || ((nz & 1) && (faces & 32u))) break;
+    if (requested <= 0 && (long long)(nx + 1) * (ny + 1) * (nz + 1) <= kBatchCoarseNodes) break;
+    nx = (nx + 1) / 2;
+    ny = (ny + 1) / 2;
+    nz = (nz + 1) / 2;
     ++lv;
   }
   return lv;
@@ -201,7 +219,7 @@ bool build_batch_mg(Ctx& c, BatchMG<T>& mg, const std::vector<Grid>& g0, const s
     for (int i = 0; i < n; ++i) {
       if (nlev[i] <= l) continue;
       Grid g = g0[i];
-      for (int q = 0; q < l; ++q) g = make_grid(g.nx / 2, g.ny / 2, g.nz / 2);
+      for (int q = 0; q < l; ++q) g = batch_coarse_grid(g);
       V.inst.push_back(i);
       V.g.push_back(g);
       V.off.push_back(V.ndof);
@@ -233,7 +251,7 @@ bool build_batch_mg(Ctx& c, BatchMG<T>& mg, const std::vector<Grid>& g0, const s
         V.coarse.h.push_back(bi);
       } else {
         V.smooth.h.push_back(bi);
-        bi.g2 = make_grid(bi.g.nx / 2, bi.g.ny / 2, bi.g.nz / 2);
+        bi.g2 = batch_coarse_grid(bi.g);
         bi.m2.faces = faces[i];
         V.prolong.h.push_back(bi);  // off2 filled below
       }
@@ -456,7 +474,7 @@ int batch_problem(Ctx& c, int count, const hexa_grid* grids, const hexa_bc* bcs,
     }
   }
   std::vector<int> nlev(count);
-  for (int i = 0; i < count; ++i) nlev[i] = batch_levels(g0[i], prm.mg_levels);
+  for (int i = 0; i < count; ++i) nlev[i] = batch_levels(g0[i], faces[i], prm.mg_levels);
   int kchunk = 16;
   const std::string tkey = "batch/" + std::to_string(count) + "/" + std::to_string(nelem) + "/" + std::to_string(ndof);
   bool tuned = false;

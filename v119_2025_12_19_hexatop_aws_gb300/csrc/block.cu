@@ -256,27 +256,52 @@ __global__ void block_solve_kernel(const double* g, int ldg, const double* r, in
   }
 }
 
-// X_j += sum_i P_i alpha_ij ; R_j -= sum_i Q_i alpha_ij ; sums ||R_j||^2.
+// Row i of a k x k coefficient block in shared memory, read with vector
+// loads inside the DOF loop.  The loads are volatile asm so the compiler does
+// not hoist all k^2 coefficients into registers ahead of the loop.
 template <typename T, int KC>
-__global__ void __launch_bounds__(kThreads) block_update_kernel(T* __restrict__ X, T* __restrict__ R,
+__device__ __forceinline__ void coef_row(const T* row, T (&a)[KC]) {
+  const unsigned addr = (unsigned)__cvta_generic_to_shared(row);
+  if constexpr (sizeof(T) == 4 && KC % 4 == 0) {
+#pragma unroll
+    for (int q = 0; q < KC / 4; ++q) {
+      float x, y, z, w;
+      asm volatile("ld.shared.v4.f32 {%0, %1, %2, %3}, [%4];"
+                   : "=f"(x), "=f"(y), "=f"(z), "=f"(w)
+                   : "r"(addr + 16u * q));
+      a[4 * q] = x, a[4 * q + 1] = y, a[4 * q + 2] = z, a[4 * q + 3] = w;
+    }
+  } else if constexpr (sizeof(T) == 8 && KC % 2 == 0) {
+#pragma unroll
+    for (int q = 0; q < KC / 2; ++q) {
+      double x, y;
+      asm volatile("ld.shared.v2.f64 {%0, %1}, [%2];" : "=d"(x), "=d"(y) : "r"(addr + 16u * q));
+      a[2 * q] = x, a[2 * q + 1] = y;
+    }
+  } else {
+#pragma unroll
+    for (int j = 0; j < KC; ++j) a[j] = row[j];
+  }
+}
+
+// X_j += sum_i P_i alpha_ij ; R_j -= sum_i Q_i alpha_ij ; sums ||R_j||^2.
+// A thread issues all 4k loads of its DOF before any arithmetic and reads
+// the k x k coefficients as shared-memory rows (vector loads, the same
+// address across the warp): at 8 columns the pass needs about 60 registers
+// instead of holding 64 coefficients in registers at quarter occupancy.  The
+// sums over i run in the same order as a per-column loop would.
+template <typename T, int KC>
+__global__ void __launch_bounds__(kThreads, KC <= 8 ? 3 : 1) block_update_kernel(T* __restrict__ X, T* __restrict__ R,
                                                                  const T* __restrict__ P, const T* __restrict__ Q,
                                                                  const double* alpha, int k, long long n,
                                                                  RedArgs red) {
   if (halt_set(red.s ? &red.s->halt : nullptr)) return;
-  __shared__ T sa[KC][KC];
+  __shared__ __align__(16) T sa[KC][KC];
   for (int e = threadIdx.x; e < KC * KC; e += blockDim.x) {
     const int i = e / KC, j = e % KC;
     sa[i][j] = (i < k && j < k) ? (T)alpha[i * k + j] : T(0);
   }
   __syncthreads();
-  // up to 8 columns the k x k coefficients live in registers (a shared-memory
-  // read per use made the pass instruction-bound)
-  constexpr int KR = KC <= 8 ? KC : 1;
-  T ar[KR][KR];
-#pragma unroll
-  for (int i = 0; i < KR; ++i)
-#pragma unroll
-    for (int j = 0; j < KR; ++j) ar[i][j] = sa[i][j];
   double acc[KC];
   T part[KC];
 #pragma unroll
@@ -284,25 +309,33 @@ __global__ void __launch_bounds__(kThreads) block_update_kernel(T* __restrict__ 
   int cnt = 0;
   const long long stride = (long long)gridDim.x * blockDim.x;
   for (long long d = (long long)blockIdx.x * blockDim.x + threadIdx.x; d < n; d += stride) {
-    T pv[KC], qv[KC];
+    T pv[KC], qv[KC], xv[KC], rv[KC];
 #pragma unroll
     for (int i = 0; i < KC; ++i) {
-      pv[i] = i < k ? P[(long long)i * n + d] : T(0);
-      qv[i] = i < k ? Q[(long long)i * n + d] : T(0);
+      const bool in = i < k;
+      const long long o = (long long)i * n + d;
+      pv[i] = in ? P[o] : T(0);
+      qv[i] = in ? Q[o] : T(0);
+      xv[i] = in ? X[o] : T(0);
+      rv[i] = in ? R[o] : T(0);
+    }
+#pragma unroll
+    for (int i = 0; i < KC; ++i) {
+      T ar[KC];
+      coef_row<T, KC>(&sa[i][0], ar);
+#pragma unroll
+      for (int j = 0; j < KC; ++j) {
+        xv[j] = fma(pv[i], ar[j], xv[j]);
+        rv[j] = fma(-qv[i], ar[j], rv[j]);
+      }
     }
 #pragma unroll
     for (int j = 0; j < KC; ++j) {
       if (j < k) {
-        T x = X[(long long)j * n + d], r = R[(long long)j * n + d];
-#pragma unroll
-        for (int i = 0; i < KC; ++i) {
-          const T aij = KC <= 8 ? ar[i % KR][j % KR] : sa[i][j];
-          x = fma(pv[i], aij, x);
-          r = fma(-qv[i], aij, r);
-        }
-        X[(long long)j * n + d] = x;
-        R[(long long)j * n + d] = r;
-        part[j] = fma(r, r, part[j]);
+        const long long o = (long long)j * n + d;
+        X[o] = xv[j];
+        R[o] = rv[j];
+        part[j] = fma(rv[j], rv[j], part[j]);
       }
     }
     if (++cnt == 32) {
@@ -316,38 +349,38 @@ __global__ void __launch_bounds__(kThreads) block_update_kernel(T* __restrict__ 
   block_reduce_finalize<KC>(red, acc);
 }
 
-// P_j = Z_j + sum_i P_i beta_ij
+// P_j = Z_j + sum_i P_i beta_ij (all 2k loads first, coefficients as
+// shared-memory rows, like block_update_kernel)
 template <typename T, int KC>
-__global__ void __launch_bounds__(kThreads) block_p_update_kernel(T* __restrict__ P, const T* __restrict__ Z,
+__global__ void __launch_bounds__(kThreads, KC <= 8 ? 4 : 1) block_p_update_kernel(T* __restrict__ P, const T* __restrict__ Z,
                                                                    const double* beta, int k, long long n,
                                                                    const int* halt) {
   if (halt_set(halt)) return;
-  __shared__ T sb[KC][KC];
+  __shared__ __align__(16) T sb[KC][KC];
   for (int e = threadIdx.x; e < KC * KC; e += blockDim.x) {
     const int i = e / KC, j = e % KC;
     sb[i][j] = (i < k && j < k) ? (T)beta[i * k + j] : T(0);
   }
   __syncthreads();
-  constexpr int KR = KC <= 8 ? KC : 1;
-  T br[KR][KR];
-#pragma unroll
-  for (int i = 0; i < KR; ++i)
-#pragma unroll
-    for (int j = 0; j < KR; ++j) br[i][j] = sb[i][j];
   const long long stride = (long long)gridDim.x * blockDim.x;
   for (long long d = (long long)blockIdx.x * blockDim.x + threadIdx.x; d < n; d += stride) {
-    T pv[KC];
+    T pv[KC], v[KC];
 #pragma unroll
-    for (int i = 0; i < KC; ++i) pv[i] = i < k ? P[(long long)i * n + d] : T(0);
-#pragma unroll
-    for (int j = 0; j < KC; ++j) {
-      if (j < k) {
-        T v = Z[(long long)j * n + d];
-#pragma unroll
-        for (int i = 0; i < KC; ++i) v = fma(pv[i], KC <= 8 ? br[i % KR][j % KR] : sb[i][j], v);
-        P[(long long)j * n + d] = v;
-      }
+    for (int i = 0; i < KC; ++i) {
+      const bool in = i < k;
+      pv[i] = in ? P[(long long)i * n + d] : T(0);
+      v[i] = in ? Z[(long long)i * n + d] : T(0);
     }
+#pragma unroll
+    for (int i = 0; i < KC; ++i) {
+      T br[KC];
+      coef_row<T, KC>(&sb[i][0], br);
+#pragma unroll
+      for (int j = 0; j < KC; ++j) v[j] = fma(pv[i], br[j], v[j]);
+    }
+#pragma unroll
+    for (int j = 0; j < KC; ++j)
+      if (j < k) P[(long long)j * n + d] = v[j];
   }
 }
 
@@ -429,7 +462,8 @@ void launch_block_solve(const double* g, int ldg, const double* r, int ldr, int 
 template <typename T>
 void launch_block_update(T* X, T* R, const T* P, const T* Q, const double* alpha, int k, long long n,
                          const RedArgs& red, cudaStream_t st) {
-  const int g = (int)std::max<long long>(1, std::min<long long>((n + kThreads - 1) / kThreads, kBlockRedBlocks));
+  // one wave: three CTAs per SM fit (launch bounds) and the loop strides over n
+  const int g = (int)std::max<long long>(1, std::min<long long>((n + kThreads - 1) / kThreads, 152LL * 3));
 #define HEXA_BU(KCV) \
   case KCV: block_update_kernel<T, KCV><<<g, kThreads, 0, st>>>(X, R, P, Q, alpha, k, n, red); break;
   switch (block_kc(k)) {
@@ -446,7 +480,7 @@ void launch_block_update(T* X, T* R, const T* P, const T* Q, const double* alpha
 template <typename T>
 void launch_block_p_update(T* P, const T* Z, const double* beta, int k, long long n, const int* halt,
                            cudaStream_t st) {
-  const int g = (int)std::max<long long>(1, std::min<long long>((n + kThreads - 1) / kThreads, 152LL * 8));
+  const int g = (int)std::max<long long>(1, std::min<long long>((n + kThreads - 1) / kThreads, 152LL * 4));
 #define HEXA_BP(KCV) \
   case KCV: block_p_update_kernel<T, KCV><<<g, kThreads, 0, st>>>(P, Z, beta, k, n, halt); break;
   switch (block_kc(k)) {

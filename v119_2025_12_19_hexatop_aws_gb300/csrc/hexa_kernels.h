@@ -112,14 +112,16 @@ void launch_convert(TD* dst, const TS* src, long long n, cudaStream_t st);
 // coarse node mask by injection
 void launch_coarsen_mask(const Grid& gf, const uint8_t* mf, const Grid& gc, uint8_t* mc,
                          cudaStream_t st);
-// b_c = P^T r_f (full weighting, 27 fine nodes per coarse node)
+// b_c = P^T r_f (full weighting, 27 fine nodes per coarse node).  This and
+// the two passes below take ncol columns (vectors ndof of their grid apart)
+// and return the number of launches issued.
 template <typename T>
-void launch_restrict(const Grid& gf, const T* rf, const Grid& gc, const Mask& mc, T* bc,
-                     const int* halt, cudaStream_t st);
+int launch_restrict(const Grid& gf, const T* rf, const Grid& gc, const Mask& mc, T* bc,
+                    const int* halt, cudaStream_t st, int ncol = 1);
 // x_f += P x_c (trilinear)
 template <typename T>
-void launch_prolong_add(const Grid& gc, const T* xc, const Grid& gf, const Mask& mf, T* xf,
-                        const int* halt, cudaStream_t st);
+int launch_prolong_add(const Grid& gc, const T* xc, const Grid& gf, const Mask& mf, T* xf,
+                       const int* halt, cudaStream_t st, int ncol = 1);
 // `iters` Jacobi-PCG iterations on a small grid in one single-CTA launch
 // (w: 24 * nelem scratch for the element products)
 template <typename T>
@@ -127,8 +129,8 @@ void launch_coarse_pcg(const Grid& g, const Mask& m, const T* fac, const ModalK<
                        const T* b, T* x, T* r, T* z, T* p, T* q, T* w, int iters, const int* halt, cudaStream_t st);
 // x = omega * b / D (first damped-Jacobi sweep from a zero guess)
 template <typename T>
-void launch_jacobi0(const Grid& g, const Mask& m, const T* fac, const ModalK<T>& K, int quirk,
-                    T sigma, T omega, const T* b, T* x, const int* halt, cudaStream_t st);
+int launch_jacobi0(const Grid& g, const Mask& m, const T* fac, const ModalK<T>& K, int quirk,
+                   T sigma, T omega, const T* b, T* x, const int* halt, cudaStream_t st, int ncol = 1);
 
 // --------------------------------------------------------------- Helmholtz
 struct HelmK {
@@ -298,9 +300,11 @@ void launch_batch_prolong_add(const BatchInst* in, int ninst, int nblocks, const
 template <typename T>
 void launch_batch_jacobi0(const BatchInst* in, int ninst, int nblocks, const T* fac, const ModalK<T>& K, int quirk,
                           T omega, const T* b, T* x, const PcgScalars* s, cudaStream_t st);
-// x = A^-1 b with a dense symmetric n x n inverse (exact coarsest-level solve)
+// x = A^-1 b with a dense symmetric n x n inverse (exact coarsest-level solve),
+// for ncol right-hand sides n apart
 template <typename T>
-void launch_dense_coarse(long long n, const T* A, const T* b, T* x, const int* halt, cudaStream_t st);
+void launch_dense_coarse(long long n, const T* A, const T* b, T* x, const int* halt, cudaStream_t st,
+                         int ncol = 1);
 // one CTA per instance: iters Jacobi-PCG iterations on its coarsest grid
 // (vectors in shared memory when the largest grid, max_ndof / max_nelem,
 // fits; r, z, p, q, w are then unused)

@@ -30,13 +30,15 @@ __global__ void coarsen_factors_kernel(Grid gf, const T* __restrict__ ff, Grid g
     const long long t = e / gc.nx;
     const int J = (int)(t % gc.ny), K = (int)(t / gc.ny);
     T s = T(0);
+    // children past the fine grid (a coarse axis rounded up from an odd one) count as void
 #pragma unroll
     for (int c = 0; c < 2; ++c)
 #pragma unroll
       for (int b = 0; b < 2; ++b)
 #pragma unroll
         for (int a = 0; a < 2; ++a)
-          s += ff[(long long)(2 * I + a) + (long long)gf.nx * ((long long)(2 * J + b) + (long long)gf.ny * (2 * K + c))];
+          if (2 * I + a < gf.nx && 2 * J + b < gf.ny && 2 * K + c < gf.nz)
+            s += ff[(long long)(2 * I + a) + (long long)gf.nx * ((long long)(2 * J + b) + (long long)gf.ny * (2 * K + c))];
     fc[e] = T(0.25) * s;  // 2 * (sum / 8)
   }
 }
@@ -105,21 +107,31 @@ __device__ __forceinline__ void restrict_body(const Grid& gf, const T* __restric
   }
 }
 // Single-grid launches index nodes in 3D (block (32, 4), grid (x, y, z) over
-// (I, J, K)): no integer division per node.
-static inline dim3 node_grid3(const Grid& g) {
-  return dim3((unsigned)((g.NX + 31) / 32), (unsigned)((g.NY + 3) / 4), (unsigned)g.NZ);
+// (I, J, K)): no integer division per node.  With ncol columns (vectors ndof
+// apart) grid z runs over K and the column: blockIdx.z = K + NZ * column.
+static inline dim3 node_grid3(const Grid& g, int ncol = 1) {
+  return dim3((unsigned)((g.NX + 31) / 32), (unsigned)((g.NY + 3) / 4), (unsigned)(g.NZ * ncol));
 }
+// Columns per launch so that grid z = NZ * columns stays within 65535.
+static inline int cols_per_launch(const Grid& g) { return std::max(1, 65535 / g.NZ); }
 template <typename T>
 __global__ void restrict_kernel(Grid gf, const T* __restrict__ rf, Grid gc, Mask mc, T* __restrict__ bc,
                                 const int* halt) {
   if (halt && *((volatile const int*)halt)) return;
-  const int I = blockIdx.x * 32 + threadIdx.x, J = blockIdx.y * 4 + threadIdx.y, K = blockIdx.z;
-  if (I < gc.NX && J < gc.NY) restrict_node<T>(gf, rf, gc, mc, bc, I, J, K);
+  const int K = blockIdx.z % gc.NZ, col = blockIdx.z / gc.NZ;
+  const int I = blockIdx.x * 32 + threadIdx.x, J = blockIdx.y * 4 + threadIdx.y;
+  if (I < gc.NX && J < gc.NY)
+    restrict_node<T>(gf, rf + (long long)col * gf.ndof(), gc, mc, bc + (long long)col * gc.ndof(), I, J, K);
 }
 template <typename T>
-void launch_restrict(const Grid& gf, const T* rf, const Grid& gc, const Mask& mc, T* bc, const int* halt,
-                     cudaStream_t st) {
-  restrict_kernel<T><<<node_grid3(gc), dim3(32, 4), 0, st>>>(gf, rf, gc, mc, bc, halt);
+int launch_restrict(const Grid& gf, const T* rf, const Grid& gc, const Mask& mc, T* bc, const int* halt,
+                    cudaStream_t st, int ncol) {
+  const int per = cols_per_launch(gc);
+  int n = 0;
+  for (int c0 = 0; c0 < ncol; c0 += per, ++n)
+    restrict_kernel<T><<<node_grid3(gc, std::min(per, ncol - c0)), dim3(32, 4), 0, st>>>(
+        gf, rf + (long long)c0 * gf.ndof(), gc, mc, bc + (long long)c0 * gc.ndof(), halt);
+  return n;
 }
 
 template <typename T>
@@ -161,13 +173,20 @@ template <typename T>
 __global__ void prolong_add_kernel(Grid gc, const T* __restrict__ xc, Grid gf, Mask mf, T* __restrict__ xf,
                                    const int* halt) {
   if (halt && *((volatile const int*)halt)) return;
-  const int i = blockIdx.x * 32 + threadIdx.x, j = blockIdx.y * 4 + threadIdx.y, k = blockIdx.z;
-  if (i < gf.NX && j < gf.NY) prolong_add_node<T>(gc, xc, gf, mf, xf, i, j, k);
+  const int k = blockIdx.z % gf.NZ, col = blockIdx.z / gf.NZ;
+  const int i = blockIdx.x * 32 + threadIdx.x, j = blockIdx.y * 4 + threadIdx.y;
+  if (i < gf.NX && j < gf.NY)
+    prolong_add_node<T>(gc, xc + (long long)col * gc.ndof(), gf, mf, xf + (long long)col * gf.ndof(), i, j, k);
 }
 template <typename T>
-void launch_prolong_add(const Grid& gc, const T* xc, const Grid& gf, const Mask& mf, T* xf, const int* halt,
-                        cudaStream_t st) {
-  prolong_add_kernel<T><<<node_grid3(gf), dim3(32, 4), 0, st>>>(gc, xc, gf, mf, xf, halt);
+int launch_prolong_add(const Grid& gc, const T* xc, const Grid& gf, const Mask& mf, T* xf, const int* halt,
+                       cudaStream_t st, int ncol) {
+  const int per = cols_per_launch(gf);
+  int n = 0;
+  for (int c0 = 0; c0 < ncol; c0 += per, ++n)
+    prolong_add_kernel<T><<<node_grid3(gf, std::min(per, ncol - c0)), dim3(32, 4), 0, st>>>(
+        gc, xc + (long long)c0 * gc.ndof(), gf, mf, xf + (long long)c0 * gf.ndof(), halt);
+  return n;
 }
 
 template <typename T>
@@ -211,13 +230,22 @@ template <typename T>
 __global__ void jacobi0_kernel(Grid g, Mask m, const T* __restrict__ fac, ModalK<T> K, int quirk, T sigma,
                                T omega, const T* __restrict__ b, T* __restrict__ x, const int* halt) {
   if (halt && *((volatile const int*)halt)) return;
-  const int i = blockIdx.x * 32 + threadIdx.x, j = blockIdx.y * 4 + threadIdx.y, k = blockIdx.z;
-  if (i < g.NX && j < g.NY) jacobi0_node<T>(g, m, fac, K, quirk, sigma, omega, b, x, i, j, k);
+  const int k = blockIdx.z % g.NZ, col = blockIdx.z / g.NZ;
+  const int i = blockIdx.x * 32 + threadIdx.x, j = blockIdx.y * 4 + threadIdx.y;
+  const long long co = (long long)col * g.ndof();
+  if (i < g.NX && j < g.NY) jacobi0_node<T>(g, m, fac, K, quirk, sigma, omega, b + co, x + co, i, j, k);
 }
 template <typename T>
-void launch_jacobi0(const Grid& g, const Mask& m, const T* fac, const ModalK<T>& K, int quirk, T sigma, T omega,
-                    const T* b, T* x, const int* halt, cudaStream_t st) {
-  jacobi0_kernel<T><<<node_grid3(g), dim3(32, 4), 0, st>>>(g, m, fac, K, quirk, sigma, omega, b, x, halt);
+int launch_jacobi0(const Grid& g, const Mask& m, const T* fac, const ModalK<T>& K, int quirk, T sigma, T omega,
+                   const T* b, T* x, const int* halt, cudaStream_t st, int ncol) {
+  const int per = cols_per_launch(g);
+  int n = 0;
+  for (int c0 = 0; c0 < ncol; c0 += per, ++n) {
+    const long long co = (long long)c0 * g.ndof();
+    jacobi0_kernel<T><<<node_grid3(g, std::min(per, ncol - c0)), dim3(32, 4), 0, st>>>(g, m, fac, K, quirk, sigma,
+                                                                                        omega, b + co, x + co, halt);
+  }
+  return n;
 }
 
 // ---------------------------------------------------------------------------
@@ -234,6 +262,22 @@ __device__ __forceinline__ double cta_sum(double v, double* red) {
   __syncthreads();
   double t = 0.0;
   for (int w = 0; w < nw; ++w) t += red[w];  // every thread sums in the same order
+  return t;
+}
+
+// CTA sum in the accumulation type A (the FP32 coarse solves sum in FP32:
+// FP64 arithmetic runs at a small fraction of the FP32 rate on this part);
+// every thread returns the same value, summed in the same order.
+template <typename A>
+__device__ __forceinline__ A cta_sum_acc(A v, A* red) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  __syncthreads();
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+  __syncthreads();
+  A t = A(0);
+  const int nw = blockDim.x >> 5;
+  for (int w = 0; w < nw; ++w) t += red[w];
   return t;
 }
 
@@ -480,7 +524,7 @@ __global__ void __launch_bounds__(1024) batch_coarse_pcg_smem_kernel(const Batch
                                                                      const T* __restrict__ b, T* xout, int iters,
                                                                      const PcgScalars* s) {
   extern __shared__ __align__(16) unsigned char coarse_smem[];
-  __shared__ double red[32];
+  __shared__ T red[32];
   const BatchInst& I = in[blockIdx.x];
   if (batch_halted(s, I.id)) return;
   const Grid g = I.g;
@@ -496,7 +540,7 @@ __global__ void __launch_bounds__(1024) batch_coarse_pcg_smem_kernel(const Batch
   const T* gb = b + I.off;
   const T* gd = dinv + I.off;
   const T* gf = fac + I.eoff;
-  double part = 0.0;
+  T part = T(0);
   for (int e = tid; e < ne; e += nthr) sf[e] = gf[e];
   for (int i = tid; i < n3; i += nthr) {
     const T ri = gb[i], zi = gd[i] * ri;
@@ -504,9 +548,9 @@ __global__ void __launch_bounds__(1024) batch_coarse_pcg_smem_kernel(const Batch
     sr[i] = ri;
     sz[i] = zi;
     sp[i] = zi;
-    part += (double)ri * (double)zi;
+    part = fma(ri, zi, part);
   }
-  double rz = cta_sum<T>(part, red);
+  T rz = cta_sum_acc<T>(part, red);
   const T sigma = (T)I.sigma;
   for (int it = 0; it < iters; ++it) {
     for (int i = tid; i < n3; i += nthr) sq[i] = T(0);
@@ -535,7 +579,7 @@ __global__ void __launch_bounds__(1024) batch_coarse_pcg_smem_kernel(const Batch
       }
       __syncthreads();
     }
-    part = 0.0;
+    part = T(0);
     for (int nd = tid; nd < nn; nd += nthr) {
       const int i = nd % g.NX, t = nd / g.NX, j = t % g.NY, k = t / g.NY;
       const unsigned fx = fixed_bits(g, m, i, j, k, nd);
@@ -544,23 +588,23 @@ __global__ void __launch_bounds__(1024) batch_coarse_pcg_smem_kernel(const Batch
         const T pv = sp[3 * nd + c];
         const T qv = ((fx >> c) & 1u) ? T(0) : fma(sigma, pv, sq[3 * nd + c]);
         sq[3 * nd + c] = qv;
-        part += (double)pv * (double)qv;
+        part = fma(pv, qv, part);
       }
     }
-    const double pAp = cta_sum<T>(part, red);
-    if (!(pAp > 0.0)) break;  // converged to rounding or no curvature left
-    const T alpha = (T)(rz / pAp);
-    part = 0.0;
+    const T pAp = cta_sum_acc<T>(part, red);
+    if (!(pAp > T(0))) break;  // converged to rounding or no curvature left
+    const T alpha = rz / pAp;
+    part = T(0);
     for (int i = tid; i < n3; i += nthr) {
       sx[i] = fma(alpha, sp[i], sx[i]);
       const T ri = fma(-alpha, sq[i], sr[i]);
       sr[i] = ri;
       const T zi = gd[i] * ri;
       sz[i] = zi;
-      part += (double)ri * (double)zi;
+      part = fma(ri, zi, part);
     }
-    const double rz_new = cta_sum<T>(part, red);
-    const T beta = (T)(rz != 0.0 ? rz_new / rz : 0.0);
+    const T rz_new = cta_sum_acc<T>(part, red);
+    const T beta = rz != T(0) ? rz_new / rz : T(0);
     rz = rz_new;
     for (int i = tid; i < n3; i += nthr) sp[i] = fma(beta, sp[i], sz[i]);
     __syncthreads();
@@ -597,10 +641,13 @@ void launch_batch_coarse_pcg(const BatchInst* in, int ninst, const T* fac, const
 // Exact coarsest-level solve: x = A^-1 b with the dense symmetric inverse
 // (n x n, zero rows/columns at fixed DOFs).  CTA = 32 rows, 8 warps split the
 // columns; lane = row, so each column read is one coalesced 128-byte access.
+// blockIdx.y picks one of ncol right-hand sides (vectors n apart).
 template <typename T>
 __global__ void __launch_bounds__(256) dense_coarse_kernel(int n, const T* __restrict__ A, const T* __restrict__ b,
                                                            T* __restrict__ x, const int* halt) {
   if (halt && *((volatile const int*)halt)) return;
+  b += (long long)blockIdx.y * n;
+  x += (long long)blockIdx.y * n;
   __shared__ T part[8][32];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const int row = blockIdx.x * 32 + lane;
@@ -617,21 +664,21 @@ __global__ void __launch_bounds__(256) dense_coarse_kernel(int n, const T* __res
   }
 }
 template <typename T>
-void launch_dense_coarse(long long n, const T* A, const T* b, T* x, const int* halt, cudaStream_t st) {
-  dense_coarse_kernel<T><<<(int)((n + 31) / 32), 256, 0, st>>>((int)n, A, b, x, halt);
+void launch_dense_coarse(long long n, const T* A, const T* b, T* x, const int* halt, cudaStream_t st, int ncol) {
+  dense_coarse_kernel<T><<<dim3((unsigned)((n + 31) / 32), (unsigned)ncol), 256, 0, st>>>((int)n, A, b, x, halt);
 }
 
 #define INST(T)                                                                                     \
   template void launch_coarsen_factors<T>(const Grid&, const T*, const Grid&, T*, cudaStream_t);    \
-  template void launch_restrict<T>(const Grid&, const T*, const Grid&, const Mask&, T*, const int*, \
-                                   cudaStream_t);                                                   \
-  template void launch_prolong_add<T>(const Grid&, const T*, const Grid&, const Mask&, T*,          \
-                                      const int*, cudaStream_t);                                    \
-  template void launch_jacobi0<T>(const Grid&, const Mask&, const T*, const ModalK<T>&, int, T, T,  \
-                                  const T*, T*, const int*, cudaStream_t);                          \
+  template int launch_restrict<T>(const Grid&, const T*, const Grid&, const Mask&, T*, const int*,  \
+                                  cudaStream_t, int);                                               \
+  template int launch_prolong_add<T>(const Grid&, const T*, const Grid&, const Mask&, T*,           \
+                                     const int*, cudaStream_t, int);                                \
+  template int launch_jacobi0<T>(const Grid&, const Mask&, const T*, const ModalK<T>&, int, T, T,   \
+                                 const T*, T*, const int*, cudaStream_t, int);                      \
   template void launch_coarse_pcg<T>(const Grid&, const Mask&, const T*, const ModalK<T>&, T, const T*, \
                                      const T*, T*, T*, T*, T*, T*, T*, int, const int*, cudaStream_t);     \
-  template void launch_dense_coarse<T>(long long, const T*, const T*, T*, const int*, cudaStream_t);     \
+  template void launch_dense_coarse<T>(long long, const T*, const T*, T*, const int*, cudaStream_t, int); \
   template void launch_batch_restrict<T>(const BatchInst*, int, int, const T*, T*, const PcgScalars*,     \
                                          cudaStream_t);                                                   \
   template void launch_batch_prolong_add<T>(const BatchInst*, int, int, const T*, T*, const PcgScalars*,  \

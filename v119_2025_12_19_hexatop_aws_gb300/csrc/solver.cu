@@ -538,6 +538,11 @@ void vcycle_cols(Ctx& c, MG<T>& mg, ColBufs<T>& cb, int l, const T* b, T* xout, 
   Lev<T>& V = mg.L[l];
   const long long n = V.g.ndof();
   if (l == (int)mg.L.size() - 1) {
+    if (V.ainv) {  // exact: one dense multiply for all k columns
+      launch_dense_coarse<T>(n, V.ainv, b, xout, halt, c.st, k);
+      c.launches++;
+      return;
+    }
     for (int j = 0; j < k; ++j) coarse_solve<T>(c, mg, b + j * n, xout + j * n, halt);
     return;
   }
@@ -557,10 +562,8 @@ void vcycle_cols(Ctx& c, MG<T>& mg, ColBufs<T>& cb, int l, const T* b, T* xout, 
     a.ncol = k;
     op<T>(c, mode, a);
   };
-  for (int j = 0; j < k; ++j)
-    launch_jacobi0<T>(V.g, V.m, V.fac, mg.K, mg.quirk, V.sigma, cheb ? mg.inv_theta : mg.omega, b + j * n,
-                      cur + j * n, halt, c.st);
-  c.launches += k;
+  c.launches +=
+      launch_jacobi0<T>(V.g, V.m, V.fac, mg.K, mg.quirk, V.sigma, cheb ? mg.inv_theta : mg.omega, b, cur, halt, c.st, k);
   for (int s = 1; s < mg.nu1; ++s) {
     T* nx = bufw(w++);
     if (cheb) {
@@ -573,12 +576,9 @@ void vcycle_cols(Ctx& c, MG<T>& mg, ColBufs<T>& cb, int l, const T* b, T* xout, 
   }
   opk(OP_RESID, cur, cb.r[l], nullptr, T(0), T(0), mg.omega);
   Lev<T>& C = mg.L[l + 1];
-  const long long nc = C.g.ndof();
-  for (int j = 0; j < k; ++j) launch_restrict<T>(V.g, cb.r[l] + j * n, C.g, C.m, cb.b[l + 1] + j * nc, halt, c.st);
-  c.launches += k;
+  c.launches += launch_restrict<T>(V.g, cb.r[l], C.g, C.m, cb.b[l + 1], halt, c.st, k);
   vcycle_cols<T>(c, mg, cb, l + 1, cb.b[l + 1], cb.xa[l + 1], k, halt);
-  for (int j = 0; j < k; ++j) launch_prolong_add<T>(C.g, cb.xa[l + 1] + j * nc, V.g, V.m, cur + j * n, halt, c.st);
-  c.launches += k;
+  c.launches += launch_prolong_add<T>(C.g, cb.xa[l + 1], V.g, V.m, cur, halt, c.st, k);
   for (int s = 0; s < mg.nu2; ++s) {
     T* nx = bufw(w++);
     if (cheb && s > 0) {
