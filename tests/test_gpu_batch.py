@@ -73,6 +73,23 @@ def test_batch_odd_axes_coarsen_rounded_up(ctx, rng, faces, levels):
         assert np.linalg.norm(U[i] - u) <= 1e-7 * np.linalg.norm(u), i
 
 
+@pytest.mark.parametrize("dims", [[(12, 6, 6), (8, 4, 4)],      # scratch form (element products in shared memory)
+                                  [(22, 11, 11), (8, 4, 4)],    # colour form (scratch does not fit)
+                                  [(24, 12, 12), (8, 4, 4)]])   # global-memory form (vectors do not fit)
+def test_batch_coarse_solve_forms(ctx, rng, dims):
+    """One level: the preconditioner is the one-CTA coarse PCG alone, in the
+    form the largest instance of the launch fits."""
+    grids, facs, forces = instances(rng, dims, void=False)
+    p = _lib.default_params(precision="mixed", tol=1e-11, divergence_check=0, mg_levels=1, max_iter=5000)
+    U, stats, rc = solve_batch(grids, facs, forces, clamp_faces=1, params=p, ctx=ctx)
+    assert rc == _lib.HEXA_OK
+    p64 = _lib.default_params(precision="fp64", divergence_check=0, tol=1e-12)
+    for i, g in enumerate(grids):
+        assert stats[i]["status"] == 0 and stats[i]["mg_levels"] == 1, i
+        u, s = solve(g, facs[i], forces[i], clamp_faces=1, params=p64, ctx=ctx)
+        assert np.linalg.norm(U[i] - u) <= 1e-8 * np.linalg.norm(u), i
+
+
 def test_batch_zero_load_instance_and_determinism(ctx, rng):
     grids, facs, forces = instances(rng, DIMS[:4])
     forces[2] = np.zeros_like(forces[2])

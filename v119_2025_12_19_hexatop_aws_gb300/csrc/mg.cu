@@ -169,22 +169,72 @@ __device__ __forceinline__ void prolong_add_body(const Grid& gc, const T* __rest
     prolong_add_node<T>(gc, xc, gf, mf, xf, i, (int)(t % gf.NY), (int)(t / gf.NY));
   }
 }
+// Single grid: one thread per coarse node (I, J, K) adds the correction to
+// the up-to-8 fine nodes (2I + a, 2J + b, 2K + c), a, b, c in {0, 1}, from the
+// coarse corner values it loads once (prolong_add_node reloads up to 8 coarse
+// nodes per fine node); the same sums in the same order as prolong_add_node.
 template <typename T>
 __global__ void prolong_add_kernel(Grid gc, const T* __restrict__ xc, Grid gf, Mask mf, T* __restrict__ xf,
                                    const int* halt) {
   if (halt && *((volatile const int*)halt)) return;
-  const int k = blockIdx.z % gf.NZ, col = blockIdx.z / gf.NZ;
-  const int i = blockIdx.x * 32 + threadIdx.x, j = blockIdx.y * 4 + threadIdx.y;
-  if (i < gf.NX && j < gf.NY)
-    prolong_add_node<T>(gc, xc + (long long)col * gc.ndof(), gf, mf, xf + (long long)col * gf.ndof(), i, j, k);
+  const int K = blockIdx.z % gc.NZ, col = blockIdx.z / gc.NZ;
+  const int I = blockIdx.x * 32 + threadIdx.x, J = blockIdx.y * 4 + threadIdx.y;
+  if (I >= gc.NX || J >= gc.NY) return;
+  xc += (long long)col * gc.ndof();
+  xf += (long long)col * gf.ndof();
+  T X[2][2][2][3];
+#pragma unroll
+  for (int c = 0; c < 2; ++c)
+#pragma unroll
+    for (int b = 0; b < 2; ++b)
+#pragma unroll
+      for (int a = 0; a < 2; ++a) {
+        const bool in = I + a < gc.NX && J + b < gc.NY && K + c < gc.NZ;
+        const long long N = (long long)(I + a) + (long long)gc.NX * ((long long)(J + b) + (long long)gc.NY * (K + c));
+#pragma unroll
+        for (int q = 0; q < 3; ++q) X[c][b][a][q] = in ? xc[3 * N + q] : T(0);
+      }
+#pragma unroll
+  for (int c = 0; c < 2; ++c) {
+    const int k = 2 * K + c;
+    if (k >= gf.NZ) continue;
+#pragma unroll
+    for (int b = 0; b < 2; ++b) {
+      const int j = 2 * J + b;
+      if (j >= gf.NY) continue;
+#pragma unroll
+      for (int a = 0; a < 2; ++a) {
+        const int i = 2 * I + a;
+        if (i >= gf.NX) continue;
+        const long long n = (long long)i + (long long)gf.NX * ((long long)j + (long long)gf.NY * k);
+        const unsigned fx = fixed_bits(gf, mf, i, j, k, n);
+        if (fx == 7u) continue;
+        const T w = (a ? T(0.5) : T(1)) * (b ? T(0.5) : T(1)) * (c ? T(0.5) : T(1));
+        T s0 = T(0), s1 = T(0), s2 = T(0);
+#pragma unroll
+        for (int cc = 0; cc <= c; ++cc)
+#pragma unroll
+          for (int bb = 0; bb <= b; ++bb)
+#pragma unroll
+            for (int aa = 0; aa <= a; ++aa) {
+              s0 += X[cc][bb][aa][0];
+              s1 += X[cc][bb][aa][1];
+              s2 += X[cc][bb][aa][2];
+            }
+        if (!(fx & 1u)) xf[3 * n] += w * s0;
+        if (!(fx & 2u)) xf[3 * n + 1] += w * s1;
+        if (!(fx & 4u)) xf[3 * n + 2] += w * s2;
+      }
+    }
+  }
 }
 template <typename T>
 int launch_prolong_add(const Grid& gc, const T* xc, const Grid& gf, const Mask& mf, T* xf, const int* halt,
                        cudaStream_t st, int ncol) {
-  const int per = cols_per_launch(gf);
+  const int per = cols_per_launch(gc);
   int n = 0;
   for (int c0 = 0; c0 < ncol; c0 += per, ++n)
-    prolong_add_kernel<T><<<node_grid3(gf, std::min(per, ncol - c0)), dim3(32, 4), 0, st>>>(
+    prolong_add_kernel<T><<<node_grid3(gc, std::min(per, ncol - c0)), dim3(32, 4), 0, st>>>(
         gc, xc + (long long)c0 * gc.ndof(), gf, mf, xf + (long long)c0 * gf.ndof(), halt);
   return n;
 }
@@ -226,24 +276,67 @@ __device__ __forceinline__ void jacobi0_body(const Grid& g, const Mask& m, const
     jacobi0_node<T>(g, m, fac, K, quirk, sigma, omega, b, x, i, (int)(t % g.NY), (int)(t / g.NY));
   }
 }
+// Single grid: a thread walks kJ0Z nodes of its (i, j) column in z and
+// carries the factors of the 4 elements below the node from the previous
+// node (the 4 above it, loaded there), so each node loads 4 factors instead
+// of 8.  The diagonal's factor sum is built in jacobi0_node's order (the 4
+// elements below, then the 4 above, each (dy, dx) in turn; an element off
+// the grid adds +0, which leaves the sum's bits unchanged).
+constexpr int kJ0Z = 8;
 template <typename T>
 __global__ void jacobi0_kernel(Grid g, Mask m, const T* __restrict__ fac, ModalK<T> K, int quirk, T sigma,
                                T omega, const T* __restrict__ b, T* __restrict__ x, const int* halt) {
   if (halt && *((volatile const int*)halt)) return;
-  const int k = blockIdx.z % g.NZ, col = blockIdx.z / g.NZ;
+  const int nzc = (g.NZ + kJ0Z - 1) / kJ0Z;
+  const int zc = blockIdx.z % nzc, col = blockIdx.z / nzc;
   const int i = blockIdx.x * 32 + threadIdx.x, j = blockIdx.y * 4 + threadIdx.y;
+  if (i >= g.NX || j >= g.NY) return;
   const long long co = (long long)col * g.ndof();
-  if (i < g.NX && j < g.NY) jacobi0_node<T>(g, m, fac, K, quirk, sigma, omega, b + co, x + co, i, j, k);
+  b += co;
+  x += co;
+  // element (i + dx, j + dy) of layer ek, dx, dy in {-1, 0}, in the order (dy, dx)
+  const bool xl = i >= 1, xr = i < g.nx, yl = j >= 1, yr = j < g.ny;
+  auto layer = [&](int ek, T (&f)[4]) {
+    const bool zin = ek >= 0 && ek < g.nz;
+    const long long row = (long long)g.nx * ((long long)(j - 1) + (long long)g.ny * ek);
+    f[0] = (zin && yl && xl) ? fac[row + i - 1] : T(0);
+    f[1] = (zin && yl && xr) ? fac[row + i] : T(0);
+    f[2] = (zin && yr && xl) ? fac[row + g.nx + i - 1] : T(0);
+    f[3] = (zin && yr && xr) ? fac[row + g.nx + i] : T(0);
+  };
+  const int k0 = zc * kJ0Z, k1 = min(k0 + kJ0Z, g.NZ);
+  T lo[4];
+  layer(k0 - 1, lo);
+  T below = T(0);
+#pragma unroll
+  for (int q = 0; q < 4; ++q) below += lo[q];
+#pragma unroll 2
+  for (int k = k0; k < k1; ++k) {
+    T up[4];
+    layer(k, up);
+    T fs = below, nb = T(0);
+#pragma unroll
+    for (int q = 0; q < 4; ++q) fs += up[q], nb += up[q];
+    below = nb;
+    const long long n = (long long)i + (long long)g.NX * ((long long)j + (long long)g.NY * k);
+    const unsigned fx = fixed_bits(g, m, i, j, k, n);
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      const T d = fma(K.dd[quirk ? 0 : c], fs, sigma);
+      x[3 * n + c] = ((fx >> c) & 1u) ? T(0) : omega * b[3 * n + c] / d;
+    }
+  }
 }
 template <typename T>
 int launch_jacobi0(const Grid& g, const Mask& m, const T* fac, const ModalK<T>& K, int quirk, T sigma, T omega,
                    const T* b, T* x, const int* halt, cudaStream_t st, int ncol) {
-  const int per = cols_per_launch(g);
+  const int nzc = (g.NZ + kJ0Z - 1) / kJ0Z;
+  const int per = std::max(1, 65535 / nzc);
   int n = 0;
   for (int c0 = 0; c0 < ncol; c0 += per, ++n) {
     const long long co = (long long)c0 * g.ndof();
-    jacobi0_kernel<T><<<node_grid3(g, std::min(per, ncol - c0)), dim3(32, 4), 0, st>>>(g, m, fac, K, quirk, sigma,
-                                                                                        omega, b + co, x + co, halt);
+    const dim3 grid((unsigned)((g.NX + 31) / 32), (unsigned)((g.NY + 3) / 4), (unsigned)(nzc * std::min(per, ncol - c0)));
+    jacobi0_kernel<T><<<grid, dim3(32, 4), 0, st>>>(g, m, fac, K, quirk, sigma, omega, b + co, x + co, halt);
   }
   return n;
 }
@@ -512,13 +605,20 @@ __global__ void __launch_bounds__(1024) batch_coarse_pcg_kernel(const BatchInst*
                      w + 24 * I.eoff, iters);
 }
 // The same Jacobi-PCG of one instance's coarsest grid with its five vectors
-// (x, r, z, p, q) and element factors held in shared memory: every pass of an
-// iteration reads and writes shared memory instead of global memory, and the
-// element products are added into q in 8 colour passes (elements of one
-// parity in x, y and z share no node), so no element scratch is needed and
-// the sums are in a fixed order.  Grids up to about 10,000 DOFs fit in FP32
-// (5 n + nElem words).  One CTA per instance, x written to xout at the end.
-template <typename T>
+// (x, r, z, p, q) and element factors held in shared memory, so every pass of
+// an iteration reads and writes shared memory instead of global memory.  Two
+// forms of the product q = A p:
+//  * W (scratch): every element's 24 products go to a shared scratch (entry
+//    (corner cc, component c) of element e at [(3 cc + c) nElem + e]), then
+//    each node sums its up-to-8 entries in a fixed order: one pass over the
+//    elements, one over the nodes, 4 barriers per iteration;
+//  * colour: the products are added into q in 8 colour passes (elements of
+//    one parity in x, y and z share no node), so no scratch is needed, at 8
+//    barriers more per iteration.
+// Both sum in a fixed order and in T (FP32 sums: FP64 arithmetic runs at a
+// small fraction of the FP32 rate on this part).  One CTA per instance, x
+// written to xout at the end.
+template <typename T, bool W>
 __global__ void __launch_bounds__(1024) batch_coarse_pcg_smem_kernel(const BatchInst* in, const T* __restrict__ fac,
                                                                      ModalK<T> K, const T* __restrict__ dinv,
                                                                      const T* __restrict__ b, T* xout, int iters,
@@ -537,6 +637,7 @@ __global__ void __launch_bounds__(1024) batch_coarse_pcg_smem_kernel(const Batch
   T* sp = sz + n3;
   T* sq = sp + n3;
   T* sf = sq + n3;
+  T* sw = sf + ne;  // W form only: 24 nElem words
   const T* gb = b + I.off;
   const T* gd = dinv + I.off;
   const T* gf = fac + I.eoff;
@@ -553,14 +654,9 @@ __global__ void __launch_bounds__(1024) batch_coarse_pcg_smem_kernel(const Batch
   T rz = cta_sum_acc<T>(part, red);
   const T sigma = (T)I.sigma;
   for (int it = 0; it < iters; ++it) {
-    for (int i = tid; i < n3; i += nthr) sq[i] = T(0);
-    __syncthreads();
-    for (int color = 0; color < 8; ++color) {
-      const int cx = color & 1, cy = (color >> 1) & 1, cz = color >> 2;
-      const int mx = (g.nx - cx + 1) >> 1, my = (g.ny - cy + 1) >> 1, mz = (g.nz - cz + 1) >> 1;
-      const int mc = mx * my * mz;
-      for (int t = tid; t < mc; t += nthr) {
-        const int i = 2 * (t % mx) + cx, j = 2 * ((t / mx) % my) + cy, k = 2 * (t / (mx * my)) + cz;
+    if constexpr (W) {
+      for (int e = tid; e < ne; e += nthr) {
+        const int i = e % g.nx, t = e / g.nx, j = t % g.ny, k = t / g.ny;
         T h[8][3];
 #pragma unroll
         for (int cc = 0; cc < 8; ++cc) {
@@ -569,24 +665,69 @@ __global__ void __launch_bounds__(1024) batch_coarse_pcg_smem_kernel(const Batch
           for (int c = 0; c < 3; ++c) h[cc][c] = sp[3 * nd + c];
         }
         T wh[8][3];
-        coarse_element_product<T>(K, sf[i + g.nx * (j + g.ny * k)], h, wh);
+        coarse_element_product<T>(K, sf[e], h, wh);
 #pragma unroll
-        for (int cc = 0; cc < 8; ++cc) {
-          const int nd = (i + (cc & 1)) + g.NX * ((j + ((cc >> 1) & 1)) + g.NY * (k + (cc >> 2)));
+        for (int cc = 0; cc < 8; ++cc)
 #pragma unroll
-          for (int c = 0; c < 3; ++c) sq[3 * nd + c] += wh[cc][c];
-        }
+          for (int c = 0; c < 3; ++c) sw[(3 * cc + c) * ne + e] = wh[cc][c];
       }
       __syncthreads();
+    } else {
+      for (int i = tid; i < n3; i += nthr) sq[i] = T(0);
+      __syncthreads();
+      for (int color = 0; color < 8; ++color) {
+        const int cx = color & 1, cy = (color >> 1) & 1, cz = color >> 2;
+        const int mx = (g.nx - cx + 1) >> 1, my = (g.ny - cy + 1) >> 1, mz = (g.nz - cz + 1) >> 1;
+        const int mc = mx * my * mz;
+        for (int t = tid; t < mc; t += nthr) {
+          const int i = 2 * (t % mx) + cx, j = 2 * ((t / mx) % my) + cy, k = 2 * (t / (mx * my)) + cz;
+          T h[8][3];
+#pragma unroll
+          for (int cc = 0; cc < 8; ++cc) {
+            const int nd = (i + (cc & 1)) + g.NX * ((j + ((cc >> 1) & 1)) + g.NY * (k + (cc >> 2)));
+#pragma unroll
+            for (int c = 0; c < 3; ++c) h[cc][c] = sp[3 * nd + c];
+          }
+          T wh[8][3];
+          coarse_element_product<T>(K, sf[i + g.nx * (j + g.ny * k)], h, wh);
+#pragma unroll
+          for (int cc = 0; cc < 8; ++cc) {
+            const int nd = (i + (cc & 1)) + g.NX * ((j + ((cc >> 1) & 1)) + g.NY * (k + (cc >> 2)));
+#pragma unroll
+            for (int c = 0; c < 3; ++c) sq[3 * nd + c] += wh[cc][c];
+          }
+        }
+        __syncthreads();
+      }
     }
     part = T(0);
     for (int nd = tid; nd < nn; nd += nthr) {
       const int i = nd % g.NX, t = nd / g.NX, j = t % g.NY, k = t / g.NY;
       const unsigned fx = fixed_bits(g, m, i, j, k, nd);
+      T sv[3];
+      if constexpr (W) {
+        sv[0] = sv[1] = sv[2] = T(0);
+#pragma unroll
+        for (int oz = 0; oz < 2; ++oz)
+#pragma unroll
+          for (int oy = 0; oy < 2; ++oy)
+#pragma unroll
+            for (int ox = 0; ox < 2; ++ox) {
+              const int ei = i - 1 + ox, ej = j - 1 + oy, ek = k - 1 + oz;
+              if (ei < 0 || ei >= g.nx || ej < 0 || ej >= g.ny || ek < 0 || ek >= g.nz) continue;
+              const int e = ei + g.nx * (ej + g.ny * ek);
+              const int ln = (1 - ox) + 2 * (1 - oy) + 4 * (1 - oz);
+#pragma unroll
+              for (int c = 0; c < 3; ++c) sv[c] += sw[(3 * ln + c) * ne + e];
+            }
+      } else {
+#pragma unroll
+        for (int c = 0; c < 3; ++c) sv[c] = sq[3 * nd + c];
+      }
 #pragma unroll
       for (int c = 0; c < 3; ++c) {
         const T pv = sp[3 * nd + c];
-        const T qv = ((fx >> c) & 1u) ? T(0) : fma(sigma, pv, sq[3 * nd + c]);
+        const T qv = ((fx >> c) & 1u) ? T(0) : fma(sigma, pv, sv[c]);
         sq[3 * nd + c] = qv;
         part = fma(pv, qv, part);
       }
@@ -613,11 +754,11 @@ __global__ void __launch_bounds__(1024) batch_coarse_pcg_smem_kernel(const Batch
   for (int i = tid; i < n3; i += nthr) gx[i] = sx[i];
 }
 
-// Shared memory the smem form needs for the largest coarsest grid of a launch
-// (0: too large, use the global-memory form).
+// Shared memory a smem form needs for the largest coarsest grid of a launch
+// (0: too large for that form).
 template <typename T>
-size_t batch_coarse_smem_bytes(long long max_ndof, long long max_nelem) {
-  const size_t bytes = (size_t)(5 * max_ndof + max_nelem) * sizeof(T);
+size_t batch_coarse_smem_bytes(long long max_ndof, long long max_nelem, bool scratch) {
+  const size_t bytes = (size_t)(5 * max_ndof + max_nelem * (scratch ? 25 : 1)) * sizeof(T);
   return bytes <= 220u * 1024u ? bytes : 0;
 }
 
@@ -625,14 +766,20 @@ template <typename T>
 void launch_batch_coarse_pcg(const BatchInst* in, int ninst, const T* fac, const ModalK<T>& K, const T* dinv,
                              const T* b, T* x, T* r, T* z, T* p, T* q, T* w, int iters, const PcgScalars* s,
                              cudaStream_t st, long long max_ndof, long long max_nelem) {
-  const size_t smem = batch_coarse_smem_bytes<T>(max_ndof, max_nelem);
-  if (smem > 0) {
-    static bool attr = false;
-    if (!attr) {
-      cudaFuncSetAttribute(batch_coarse_pcg_smem_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
-      attr = true;
-    }
-    batch_coarse_pcg_smem_kernel<T><<<ninst, 1024, smem, st>>>(in, fac, K, dinv, b, x, iters, s);
+  const size_t smem_w = batch_coarse_smem_bytes<T>(max_ndof, max_nelem, true);
+  const size_t smem_c = batch_coarse_smem_bytes<T>(max_ndof, max_nelem, false);
+  static bool attr = false;
+  if (!attr && smem_c > 0) {
+    cudaFuncSetAttribute(batch_coarse_pcg_smem_kernel<T, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
+    cudaFuncSetAttribute(batch_coarse_pcg_smem_kernel<T, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
+    attr = true;
+  }
+  if (smem_w > 0) {
+    batch_coarse_pcg_smem_kernel<T, true><<<ninst, 1024, smem_w, st>>>(in, fac, K, dinv, b, x, iters, s);
+    return;
+  }
+  if (smem_c > 0) {
+    batch_coarse_pcg_smem_kernel<T, false><<<ninst, 1024, smem_c, st>>>(in, fac, K, dinv, b, x, iters, s);
     return;
   }
   batch_coarse_pcg_kernel<T><<<ninst, 1024, 0, st>>>(in, fac, K, dinv, b, x, r, z, p, q, w, iters, s);
