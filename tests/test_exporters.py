@@ -54,6 +54,33 @@ def test_hexa_binary_layout_and_round_trip(tmp_path):
     assert len(raw) == 36 + 20 * idx.size + 4 + struct.unpack_from("<I", raw, 36 + 20 * idx.size)[0]
 
 
+def test_hexa_binary_matches_the_reference_writer_bytes(tmp_path):
+    """Every byte before the JSON metadata equals the bytes derived step by
+    step from the reference writer (tests/golden/make_hexa_v2.py: non-dyadic
+    spacing, threshold ties, the fractional-stride subsample, sign ties and
+    zeros); the JSON is compared by content (its key order is a Julia Dict's)."""
+    import json
+    import pathlib
+    fx = json.loads((pathlib.Path(__file__).parent / "golden" / "hexa_v2_fixture.json").read_text())
+    grid = _lib.make_grid(*fx["grid"], *fx["spacing"])
+    cfg = {"external_forces": [{"F": [0, 0, -1]}], "optimization_parameters": {"volfrac": 0.3}}
+    path = tmp_path / "golden.bin"
+    n = write_hexa_binary(path, grid, np.array(fx["density"], np.float32), np.array(fx["l1"], np.float32),
+                          np.array(fx["principal"], np.float32), iteration=fx["iteration"], radius=fx["radius"],
+                          threshold=fx["threshold"], config=cfg, max_export_cells=fx["max_export_cells"])
+    assert n == fx["count"]
+    raw = path.read_bytes()
+    prefix = bytes.fromhex(fx["prefix_hex"])
+    assert raw[:len(prefix)] == prefix
+    (jlen,) = struct.unpack_from("<I", raw, len(prefix))
+    meta = json.loads(raw[len(prefix) + 4:].decode("utf-8"))
+    assert len(raw) == len(prefix) + 4 + jlen
+    assert meta["iteration"] == fx["iteration"] and meta["loads"] == cfg["external_forces"]
+    assert meta["bcs"] == [] and meta["settings"] == {"volfrac": 0.3}
+    assert np.float32(meta["radius"]) == np.float32(fx["radius"])
+    assert np.float32(meta["threshold"]) == np.float32(fx["threshold"])
+
+
 def test_hexa_binary_writes_nothing_without_active_cells(tmp_path):
     grid = _lib.make_grid(2, 2, 2)
     path = tmp_path / "none.bin"
