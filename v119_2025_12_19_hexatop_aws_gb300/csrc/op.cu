@@ -325,6 +325,15 @@ __device__ __forceinline__ void load4(const double* p, double (&v)[4]) {
 // One work item: the node columns of tile (tx, ty) for node layers [k0, k1).
 // IX is the index type: int whenever 3 * nNodes fits, which halves the
 // integer work of the address arithmetic.
+// Named barrier b (1..15) between the two neighbouring warps wy = b - 1 and
+// wy = b.  In a layer each warp first meets the warp below on its own index,
+// then the warp above on the next one: the rendezvous form a chain from warp 0
+// up, so every barrier completes, and a warp cannot reach a barrier instance
+// of the next layer before both warps have left this layer's.  With the
+// double-buffered slots, a slot is rewritten two layers later, after its
+// reader has passed the next layer's rendezvous.
+__device__ __forceinline__ void pair_barrier(int b) { asm volatile("bar.sync %0, 64;" ::"r"(b) : "memory"); }
+
 template <typename T, int MODE, int TYW, typename IX, typename A, bool INTERIOR = false>
 __device__ __forceinline__ void op_item(const A& a, int tx, int ty, int chunk,
                                         T (&xch)[2][TYW][32][4],
@@ -334,6 +343,7 @@ __device__ __forceinline__ void op_item(const A& a, int tx, int ty, int chunk,
   constexpr bool DOTB = MODE == OP_JACOBI_DOT || MODE == OP_CHEB2_DOT;
   constexpr int NX_OWN = 31, NY_OWN = TYW - 1;
   constexpr bool NEED_F = (BM == OP_JACOBI || BM == OP_CHEB2);
+  static_assert(TYW <= 16, "pairwise barriers use the named barriers 1..TYW-1");
   const Grid& g = a.g;
   const int lane = threadIdx.x, wy = threadIdx.y;
   const int i0 = tx * NX_OWN, j0 = ty * NY_OWN;
@@ -448,7 +458,14 @@ __device__ __forceinline__ void op_item(const A& a, int tx, int ty, int chunk,
     fprev = f;
     const int buf = k & 1;
     store4(&xch[buf][wy][lane][0], T0[0], T0[1], T0[2], F1);  // one vector store, no bank conflicts
-    __syncthreads();
+    if (a.pair_sync) {
+      // warp wy reads only what warp wy + 1 stored: rendezvous with the warp
+      // below (which reads this warp's slot), then with the warp above
+      if (wy >= 1) pair_barrier(wy);
+      if (wy + 1 < TYW) pair_barrier(wy + 1);
+    } else {
+      __syncthreads();
+    }
     if (own) {
       const IX n = ncol + nplane * (IX)k;
       unsigned fx = colfix;
@@ -1039,10 +1056,19 @@ static void launch_op_tma(int mode, OpArgs<float>& a, bool i32, cudaStream_t st)
 #undef HEXA_OPT_CASE
 }
 
+// Layer synchronisation of the one-row kernel (HEXA_OP_SYNC, read once): 1
+// (default) pairwise named barriers between neighbouring warps, 0 one CTA
+// barrier per layer.
+static int op_pair_sync() {
+  static const int v = env_int("HEXA_OP_SYNC", 1);
+  return v;
+}
+
 template <typename T>
 void launch_op(int mode, const OpArgs<T>& a0, cudaStream_t st) {
   constexpr int TYW = op_tyw<T>();
   OpArgs<T> a = a0;
+  a.pair_sync = op_pair_sync();
   op_tiles<T>(a.g, a.kchunk, &a.tiles_x, &a.tiles_y, &a.nchunks);
   const long long items = (long long)a.tiles_x * a.tiles_y * a.nchunks;
   const int grid = (int)std::min<long long>(items, resident_ctas<T>(mode));
@@ -1106,6 +1132,7 @@ struct ItemArgs {
   const ModalK<T>& K;
   T sigma, omega;
   int kchunk, diag_quirk;
+  int pair_sync;
 };
 
 __device__ __forceinline__ int batch_find_op(const BatchInst* in, int n, int b) {
@@ -1129,7 +1156,7 @@ __global__ void __launch_bounds__(32 * TYW, op_min_ctas<T>()) op_batch_kernel(co
   if (a.s && *((volatile const int*)&a.s[id].halt)) return;
   const ItemArgs<T> ia{I.g,      I.m,      a.x + I.off,  a.fac + I.eoff,  a.b ? a.b + I.off : a.b,
                        a.y + I.off, a.xin ? a.xin + I.off : a.xin, a.c1, a.c2, a.K, (T)I.sigma, a.omega,
-                       I.kchunk, a.diag_quirk};
+                       I.kchunk, a.diag_quirk, a.pair_sync};
   const int txs = I.tiles_x, nxy = I.tiles_x * I.tiles_y, items = nxy * I.nchunks;
   const int local = blockIdx.x - I.oblk0, nb = I.onblk;
   double acc0 = 0.0;
@@ -1168,9 +1195,11 @@ int op_batch_plan(BatchInst* in, int n, int kchunk) {
 }
 
 template <typename T>
-void launch_op_batch(int mode, const BatchOpArgs<T>& a, bool idx32, cudaStream_t st) {
+void launch_op_batch(int mode, const BatchOpArgs<T>& a0, bool idx32, cudaStream_t st) {
   constexpr int TYW = op_tyw<T>();
   const dim3 block(32, TYW);
+  BatchOpArgs<T> a = a0;
+  a.pair_sync = op_pair_sync();
 #define HEXA_OPB_CASE(M)                                                                          \
   case M:                                                                                        \
     if (idx32) op_batch_kernel<T, M, TYW, int><<<a.nblocks, block, 0, st>>>(a);                  \
