@@ -40,7 +40,6 @@ struct OpArgs {
   int ncol = 1;     // columns (x, b, xin, y advance by ndof per column): OP_APPLY,
                     // OP_RESID, OP_JACOBI and OP_CHEB2 only
   int test_stall = -1;  // FP32 staged form: layer load that CTA 0 leaves out (tests of the bounded waits)
-  int pair_sync = 1;    // y-exchange synchronised pairwise between neighbouring warps (0: one CTA barrier)
 };
 
 template <typename T>
@@ -268,7 +267,6 @@ struct BatchOpArgs {
   const T* xin;
   RedArgs red;            // group = instance id
   const PcgScalars* s;    // per-instance halts (nullable)
-  int pair_sync = 1;      // as OpArgs::pair_sync
 };
 template <typename T>
 void launch_op_batch(int mode, const BatchOpArgs<T>& a, bool idx32, cudaStream_t st);

@@ -332,6 +332,12 @@ __device__ __forceinline__ void load4(const double* p, double (&v)[4]) {
 // of the next layer before both warps have left this layer's.  With the
 // double-buffered slots, a slot is rewritten two layers later, after its
 // reader has passed the next layer's rendezvous.
+// HEXA_OP_PAIR_SYNC=0 builds the one-CTA-barrier form (measured slower on the
+// 384x192x192 grid: Chebyshev step 0.240 ms against 0.226 ms, Jacobi step
+// 0.205 against 0.199, apply with p.Ap 0.209 against 0.199, residual equal).
+#ifndef HEXA_OP_PAIR_SYNC
+#define HEXA_OP_PAIR_SYNC 1
+#endif
 __device__ __forceinline__ void pair_barrier(int b) { asm volatile("bar.sync %0, 64;" ::"r"(b) : "memory"); }
 
 template <typename T, int MODE, int TYW, typename IX, typename A, bool INTERIOR = false>
@@ -458,14 +464,14 @@ __device__ __forceinline__ void op_item(const A& a, int tx, int ty, int chunk,
     fprev = f;
     const int buf = k & 1;
     store4(&xch[buf][wy][lane][0], T0[0], T0[1], T0[2], F1);  // one vector store, no bank conflicts
-    if (a.pair_sync) {
-      // warp wy reads only what warp wy + 1 stored: rendezvous with the warp
-      // below (which reads this warp's slot), then with the warp above
-      if (wy >= 1) pair_barrier(wy);
-      if (wy + 1 < TYW) pair_barrier(wy + 1);
-    } else {
-      __syncthreads();
-    }
+#if HEXA_OP_PAIR_SYNC
+    // warp wy reads only what warp wy + 1 stored: rendezvous with the warp
+    // below (which reads this warp's slot), then with the warp above
+    if (wy >= 1) pair_barrier(wy);
+    if (wy + 1 < TYW) pair_barrier(wy + 1);
+#else
+    __syncthreads();
+#endif
     if (own) {
       const IX n = ncol + nplane * (IX)k;
       unsigned fx = colfix;
@@ -1056,19 +1062,10 @@ static void launch_op_tma(int mode, OpArgs<float>& a, bool i32, cudaStream_t st)
 #undef HEXA_OPT_CASE
 }
 
-// Layer synchronisation of the one-row kernel (HEXA_OP_SYNC, read once): 1
-// (default) pairwise named barriers between neighbouring warps, 0 one CTA
-// barrier per layer.
-static int op_pair_sync() {
-  static const int v = env_int("HEXA_OP_SYNC", 1);
-  return v;
-}
-
 template <typename T>
 void launch_op(int mode, const OpArgs<T>& a0, cudaStream_t st) {
   constexpr int TYW = op_tyw<T>();
   OpArgs<T> a = a0;
-  a.pair_sync = op_pair_sync();
   op_tiles<T>(a.g, a.kchunk, &a.tiles_x, &a.tiles_y, &a.nchunks);
   const long long items = (long long)a.tiles_x * a.tiles_y * a.nchunks;
   const int grid = (int)std::min<long long>(items, resident_ctas<T>(mode));
@@ -1132,7 +1129,6 @@ struct ItemArgs {
   const ModalK<T>& K;
   T sigma, omega;
   int kchunk, diag_quirk;
-  int pair_sync;
 };
 
 __device__ __forceinline__ int batch_find_op(const BatchInst* in, int n, int b) {
@@ -1156,7 +1152,7 @@ __global__ void __launch_bounds__(32 * TYW, op_min_ctas<T>()) op_batch_kernel(co
   if (a.s && *((volatile const int*)&a.s[id].halt)) return;
   const ItemArgs<T> ia{I.g,      I.m,      a.x + I.off,  a.fac + I.eoff,  a.b ? a.b + I.off : a.b,
                        a.y + I.off, a.xin ? a.xin + I.off : a.xin, a.c1, a.c2, a.K, (T)I.sigma, a.omega,
-                       I.kchunk, a.diag_quirk, a.pair_sync};
+                       I.kchunk, a.diag_quirk};
   const int txs = I.tiles_x, nxy = I.tiles_x * I.tiles_y, items = nxy * I.nchunks;
   const int local = blockIdx.x - I.oblk0, nb = I.onblk;
   double acc0 = 0.0;
@@ -1198,8 +1194,7 @@ template <typename T>
 void launch_op_batch(int mode, const BatchOpArgs<T>& a0, bool idx32, cudaStream_t st) {
   constexpr int TYW = op_tyw<T>();
   const dim3 block(32, TYW);
-  BatchOpArgs<T> a = a0;
-  a.pair_sync = op_pair_sync();
+  const BatchOpArgs<T>& a = a0;
 #define HEXA_OPB_CASE(M)                                                                          \
   case M:                                                                                        \
     if (idx32) op_batch_kernel<T, M, TYW, int><<<a.nblocks, block, 0, st>>>(a);                  \
