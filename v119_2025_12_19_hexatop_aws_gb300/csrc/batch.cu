@@ -419,7 +419,10 @@ int batch_problem(Ctx& c, int count, const hexa_grid* grids, const hexa_bc* bcs,
     rm.s = nullptr;
     rm.op = FIN_STORE;
     rm.nsum = 1;
-    launch_max(r64 + off[i], g0[i].ndof(), rm, 152 * 4, c.st);
+    // about 1024 values per block: the last block's fold over the block
+    // maxima is serial, so small instances get few blocks
+    const int mb = (int)std::min<long long>(152 * 4, std::max<long long>(1, (g0[i].ndof() + 1023) / 1024));
+    launch_max(r64 + off[i], g0[i].ndof(), rm, mb, c.st);
     c.launches += 2;
   }
   DevTable fine64;
