@@ -194,6 +194,21 @@ __global__ void prolong_add_kernel(Grid gc, const T* __restrict__ xc, Grid gf, M
 #pragma unroll
         for (int q = 0; q < 3; ++q) X[c][b][a][q] = in ? xc[3 * N + q] : T(0);
       }
+  // the fine values are loaded before any arithmetic, so all 48 loads of the
+  // thread are in flight together
+  T Fv[2][2][2][3];
+#pragma unroll
+  for (int c = 0; c < 2; ++c)
+#pragma unroll
+    for (int b = 0; b < 2; ++b)
+#pragma unroll
+      for (int a = 0; a < 2; ++a) {
+        const int i = 2 * I + a, j = 2 * J + b, k = 2 * K + c;
+        const bool in = i < gf.NX && j < gf.NY && k < gf.NZ;
+        const long long n = (long long)i + (long long)gf.NX * ((long long)j + (long long)gf.NY * k);
+#pragma unroll
+        for (int q = 0; q < 3; ++q) Fv[c][b][a][q] = in ? xf[3 * n + q] : T(0);
+      }
 #pragma unroll
   for (int c = 0; c < 2; ++c) {
     const int k = 2 * K + c;
@@ -221,9 +236,9 @@ __global__ void prolong_add_kernel(Grid gc, const T* __restrict__ xc, Grid gf, M
               s1 += X[cc][bb][aa][1];
               s2 += X[cc][bb][aa][2];
             }
-        if (!(fx & 1u)) xf[3 * n] += w * s0;
-        if (!(fx & 2u)) xf[3 * n + 1] += w * s1;
-        if (!(fx & 4u)) xf[3 * n + 2] += w * s2;
+        if (!(fx & 1u)) xf[3 * n] = Fv[c][b][a][0] + w * s0;
+        if (!(fx & 2u)) xf[3 * n + 1] = Fv[c][b][a][1] + w * s1;
+        if (!(fx & 4u)) xf[3 * n + 2] = Fv[c][b][a][2] + w * s2;
       }
     }
   }
