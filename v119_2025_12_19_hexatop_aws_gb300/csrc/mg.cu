@@ -134,54 +134,16 @@ int launch_restrict(const Grid& gf, const T* rf, const Grid& gc, const Mask& mc,
   return n;
 }
 
+// x_f += P x_c.  One thread per coarse node (I, J, K) adds the correction to
+// the up-to-8 fine nodes (2I + a, 2J + b, 2K + c), a, b, c in {0, 1}, from
+// the coarse corner values (I..I+a, J..J+b, K..K+c) it loads once: fine node
+// (a, b, c) gets w = 2^-(a+b+c) times their sum taken in (c, b, a) order.
+// Fixed fine DOFs are left alone.  All loads of the thread are issued before
+// its arithmetic (loading each fine value next to its update made the mixed
+// solve on the 384x192x192 grid 2.5 % slower).
 template <typename T>
-__device__ __forceinline__ void prolong_add_node(const Grid& gc, const T* __restrict__ xc, const Grid& gf,
-                                                 const Mask& mf, T* __restrict__ xf, int i, int j, int k) {
-  {
-    const long long n = (long long)i + (long long)gf.NX * ((long long)j + (long long)gf.NY * k);
-    const unsigned fx = fixed_bits(gf, mf, i, j, k, n);
-    if (fx == 7u) return;
-    const int I0 = i >> 1, J0 = j >> 1, K0 = k >> 1;
-    const int ni = (i & 1) ? 2 : 1, nj = (j & 1) ? 2 : 1, nk = (k & 1) ? 2 : 1;
-    const T wi = (i & 1) ? T(0.5) : T(1), wj = (j & 1) ? T(0.5) : T(1), wk = (k & 1) ? T(0.5) : T(1);
-    const T w = wi * wj * wk;
-    T s0 = T(0), s1 = T(0), s2 = T(0);
-    for (int c = 0; c < nk; ++c)
-      for (int b = 0; b < nj; ++b)
-        for (int a = 0; a < ni; ++a) {
-          const long long N = (long long)(I0 + a) + (long long)gc.NX * ((long long)(J0 + b) + (long long)gc.NY * (K0 + c));
-          s0 += xc[3 * N];
-          s1 += xc[3 * N + 1];
-          s2 += xc[3 * N + 2];
-        }
-    if (!(fx & 1u)) xf[3 * n] += w * s0;
-    if (!(fx & 2u)) xf[3 * n + 1] += w * s1;
-    if (!(fx & 4u)) xf[3 * n + 2] += w * s2;
-  }
-}
-template <typename T>
-__device__ __forceinline__ void prolong_add_body(const Grid& gc, const T* __restrict__ xc, const Grid& gf,
-                                                 const Mask& mf, T* __restrict__ xf, long long first, long long stride) {
-  const long long nn = gf.nnode();
-  for (long long n = first; n < nn; n += stride) {
-    const int i = (int)(n % gf.NX);
-    const long long t = n / gf.NX;
-    prolong_add_node<T>(gc, xc, gf, mf, xf, i, (int)(t % gf.NY), (int)(t / gf.NY));
-  }
-}
-// Single grid: one thread per coarse node (I, J, K) adds the correction to
-// the up-to-8 fine nodes (2I + a, 2J + b, 2K + c), a, b, c in {0, 1}, from the
-// coarse corner values it loads once (prolong_add_node reloads up to 8 coarse
-// nodes per fine node); the same sums in the same order as prolong_add_node.
-template <typename T>
-__global__ void prolong_add_kernel(Grid gc, const T* __restrict__ xc, Grid gf, Mask mf, T* __restrict__ xf,
-                                   const int* halt) {
-  if (halt && *((volatile const int*)halt)) return;
-  const int K = blockIdx.z % gc.NZ, col = blockIdx.z / gc.NZ;
-  const int I = blockIdx.x * 32 + threadIdx.x, J = blockIdx.y * 4 + threadIdx.y;
-  if (I >= gc.NX || J >= gc.NY) return;
-  xc += (long long)col * gc.ndof();
-  xf += (long long)col * gf.ndof();
+__device__ __forceinline__ void prolong_add_cnode(const Grid& gc, const T* __restrict__ xc, const Grid& gf,
+                                                  const Mask& mf, T* __restrict__ xf, int I, int J, int K) {
   T X[2][2][2][3];
 #pragma unroll
   for (int c = 0; c < 2; ++c)
@@ -194,8 +156,6 @@ __global__ void prolong_add_kernel(Grid gc, const T* __restrict__ xc, Grid gf, M
 #pragma unroll
         for (int q = 0; q < 3; ++q) X[c][b][a][q] = in ? xc[3 * N + q] : T(0);
       }
-  // the fine values are loaded before any arithmetic, so all 48 loads of the
-  // thread are in flight together
   T Fv[2][2][2][3];
 #pragma unroll
   for (int c = 0; c < 2; ++c)
@@ -242,6 +202,15 @@ __global__ void prolong_add_kernel(Grid gc, const T* __restrict__ xc, Grid gf, M
       }
     }
   }
+}
+template <typename T>
+__global__ void prolong_add_kernel(Grid gc, const T* __restrict__ xc, Grid gf, Mask mf, T* __restrict__ xf,
+                                   const int* halt) {
+  if (halt && *((volatile const int*)halt)) return;
+  const int K = blockIdx.z % gc.NZ, col = blockIdx.z / gc.NZ;
+  const int I = blockIdx.x * 32 + threadIdx.x, J = blockIdx.y * 4 + threadIdx.y;
+  if (I >= gc.NX || J >= gc.NY) return;
+  prolong_add_cnode<T>(gc, xc + (long long)col * gc.ndof(), gf, mf, xf + (long long)col * gf.ndof(), I, J, K);
 }
 template <typename T>
 int launch_prolong_add(const Grid& gc, const T* xc, const Grid& gf, const Mask& mf, T* xf, const int* halt,
@@ -291,13 +260,14 @@ __device__ __forceinline__ void jacobi0_body(const Grid& g, const Mask& m, const
     jacobi0_node<T>(g, m, fac, K, quirk, sigma, omega, b, x, i, (int)(t % g.NY), (int)(t / g.NY));
   }
 }
-// Single grid: a thread walks kJ0Z nodes of its (i, j) column in z and
-// carries the factors of the 4 elements below the node from the previous
-// node (the 4 above it, loaded there), so each node loads 4 factors instead
-// of 8.  The diagonal's factor sum is built in jacobi0_node's order (the 4
-// elements below, then the 4 above, each (dy, dx) in turn; an element off
-// the grid adds +0, which leaves the sum's bits unchanged).
-constexpr int kJ0Z = 8;
+// Single grid: a thread takes kJ0Z nodes of its (i, j) column in z, loads
+// the factors of the kJ0Z + 1 element layers around them (4 per layer) and
+// their b values before any arithmetic, and carries the factor sum of the 4
+// elements below a node from the node before (each node needs 4 new factors
+// instead of 8).  The diagonal's factor sum is built in jacobi0_node's order
+// (the 4 elements below, then the 4 above, each (dy, dx) in turn; an element
+// off the grid adds +0, which leaves the sum's bits unchanged).
+constexpr int kJ0Z = 4;
 template <typename T>
 __global__ void jacobi0_kernel(Grid g, Mask m, const T* __restrict__ fac, ModalK<T> K, int quirk, T sigma,
                                T omega, const T* __restrict__ b, T* __restrict__ x, const int* halt) {
@@ -311,34 +281,43 @@ __global__ void jacobi0_kernel(Grid g, Mask m, const T* __restrict__ fac, ModalK
   x += co;
   // element (i + dx, j + dy) of layer ek, dx, dy in {-1, 0}, in the order (dy, dx)
   const bool xl = i >= 1, xr = i < g.nx, yl = j >= 1, yr = j < g.ny;
-  auto layer = [&](int ek, T (&f)[4]) {
+  const int k0 = zc * kJ0Z;
+  T fl[kJ0Z + 1][4];
+#pragma unroll
+  for (int q = 0; q <= kJ0Z; ++q) {
+    const int ek = k0 - 1 + q;
     const bool zin = ek >= 0 && ek < g.nz;
     const long long row = (long long)g.nx * ((long long)(j - 1) + (long long)g.ny * ek);
-    f[0] = (zin && yl && xl) ? fac[row + i - 1] : T(0);
-    f[1] = (zin && yl && xr) ? fac[row + i] : T(0);
-    f[2] = (zin && yr && xl) ? fac[row + g.nx + i - 1] : T(0);
-    f[3] = (zin && yr && xr) ? fac[row + g.nx + i] : T(0);
-  };
-  const int k0 = zc * kJ0Z, k1 = min(k0 + kJ0Z, g.NZ);
-  T lo[4];
-  layer(k0 - 1, lo);
+    fl[q][0] = (zin && yl && xl) ? fac[row + i - 1] : T(0);
+    fl[q][1] = (zin && yl && xr) ? fac[row + i] : T(0);
+    fl[q][2] = (zin && yr && xl) ? fac[row + g.nx + i - 1] : T(0);
+    fl[q][3] = (zin && yr && xr) ? fac[row + g.nx + i] : T(0);
+  }
+  T bv[kJ0Z][3];
+#pragma unroll
+  for (int q = 0; q < kJ0Z; ++q) {
+    const int k = k0 + q;
+    const long long n = (long long)i + (long long)g.NX * ((long long)j + (long long)g.NY * k);
+#pragma unroll
+    for (int c = 0; c < 3; ++c) bv[q][c] = k < g.NZ ? b[3 * n + c] : T(0);
+  }
   T below = T(0);
 #pragma unroll
-  for (int q = 0; q < 4; ++q) below += lo[q];
-#pragma unroll 2
-  for (int k = k0; k < k1; ++k) {
-    T up[4];
-    layer(k, up);
+  for (int t = 0; t < 4; ++t) below += fl[0][t];
+#pragma unroll
+  for (int q = 0; q < kJ0Z; ++q) {
+    const int k = k0 + q;
+    if (k >= g.NZ) break;
     T fs = below, nb = T(0);
 #pragma unroll
-    for (int q = 0; q < 4; ++q) fs += up[q], nb += up[q];
+    for (int t = 0; t < 4; ++t) fs += fl[q + 1][t], nb += fl[q + 1][t];
     below = nb;
     const long long n = (long long)i + (long long)g.NX * ((long long)j + (long long)g.NY * k);
     const unsigned fx = fixed_bits(g, m, i, j, k, n);
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
       const T d = fma(K.dd[quirk ? 0 : c], fs, sigma);
-      x[3 * n + c] = ((fx >> c) & 1u) ? T(0) : omega * b[3 * n + c] / d;
+      x[3 * n + c] = ((fx >> c) & 1u) ? T(0) : omega * bv[q][c] / d;
     }
   }
 }
@@ -584,8 +563,15 @@ __global__ void batch_prolong_add_kernel(const BatchInst* in, int ninst, const T
                                          const PcgScalars* s) {
   const BatchInst& I = batch_inst_vec(in, ninst, blockIdx.x);
   if (batch_halted(s, I.id)) return;
-  prolong_add_body<T>(I.g2, xc + I.off2, I.g, I.m, xf + I.off,
-                      (long long)(blockIdx.x - I.vblk0) * blockDim.x + threadIdx.x, (long long)I.vnblk * blockDim.x);
+  // the instance's blocks (planned over its fine nodes) stride over its coarse nodes
+  const Grid gc = I.g2;
+  const long long nn = gc.nnode();
+  for (long long N = (long long)(blockIdx.x - I.vblk0) * blockDim.x + threadIdx.x; N < nn;
+       N += (long long)I.vnblk * blockDim.x) {
+    const int Ic = (int)(N % gc.NX);
+    const long long t = N / gc.NX;
+    prolong_add_cnode<T>(gc, xc + I.off2, I.g, I.m, xf + I.off, Ic, (int)(t % gc.NY), (int)(t / gc.NY));
+  }
 }
 template <typename T>
 void launch_batch_prolong_add(const BatchInst* in, int ninst, int nblocks, const T* xc, T* xf,
