@@ -306,8 +306,9 @@ template <typename T>
 void launch_dense_coarse(long long n, const T* A, const T* b, T* x, const int* halt, cudaStream_t st,
                          int ncol = 1);
 // one CTA per instance: iters Jacobi-PCG iterations on its coarsest grid
-// (vectors in shared memory when the largest grid, max_ndof / max_nelem,
-// fits; r, z, p, q, w are then unused)
+// (vectors and factors in shared memory when the largest grid, max_ndof /
+// max_nelem, fits, with the element products in a shared scratch when that
+// fits too; r, z, p, q, w are then unused)
 template <typename T>
 void launch_batch_coarse_pcg(const BatchInst* in, int ninst, const T* fac, const ModalK<T>& K, const T* dinv,
                              const T* b, T* x, T* r, T* z, T* p, T* q, T* w, int iters, const PcgScalars* s,
