@@ -419,7 +419,10 @@ __device__ __forceinline__ void op_item(const A& a, int tx, int ty, int chunk,
   load_corners<T, IX, INTERIOR>(g, ca, x, k0 + 1, nraw);
   T fnext = facload(k0);
 
-#pragma unroll 2
+  // three layers per unrolled step for the Chebyshev forms, two for the rest
+  // (on the 384x192x192 grid: Chebyshev step 0.2191 ms at 3 against 0.2248
+  // at 2 and 0.2475 at 1; Jacobi step 0.2006 at 3, 0.1983 at 2)
+#pragma unroll(BM == OP_CHEB2 ? 3 : 2)
   for (int k = k0; k < k1; ++k) {
     T raw[4][3];
 #pragma unroll
