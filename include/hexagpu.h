@@ -236,9 +236,9 @@ int hexa_solve_multi_rhs(hexa_ctx* ctx, const hexa_grid* g, const hexa_bc* bc, c
  * with the multigrid preconditioner only (FP32 GMG-PCG, FP64 reliable
  * updates to p->tol per instance); p->autotune picks the operator's z-brick
  * depth by timing.  Each instance's hierarchy halves every axis (an odd axis
- * rounded up, unless that axis' high face is clamped) down to at most 1000
- * nodes, or to p->mg_levels levels when that is > 0; stats[i].mg_levels
- * reports it.  stats (nullable) receives count entries; the return is
+ * rounded up, unless that axis' high face is clamped; no axis below 2
+ * elements) down to at most 1000 nodes, or to at most p->mg_levels levels
+ * when that is > 0; stats[i].mg_levels reports the count.  stats (nullable) receives count entries; the return is
  * HEXA_OK when every instance converged, HEXA_NOT_CONVERGED otherwise. */
 int hexa_solve_batch(hexa_ctx* ctx, int32_t count, const hexa_grid* grids, const hexa_bc* bcs, double nu,
                      const double* const* factors, const double* const* forces, const hexa_solve_params* p,
