@@ -218,7 +218,7 @@ MG_OVERRIDE = None
 
 
 def solver_params(name, precision, shift_factor=0.0):
-    """The north star's system is the unshifted K_ff u = f (shift_factor 0);
+    """The benchmarked system is the unshifted K_ff u = f (shift_factor 0);
     shift_factor 1e-10 gives the reference's (K_ff + sigma I) u = f.  The plain
     FP64 form uses the configuration's multigrid (4 levels and damped-Jacobi
     V(2,2) at c2; 5 levels and Chebyshev V(2,2) at c3); the mixed form is the
